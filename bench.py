@@ -1,0 +1,365 @@
+#!/usr/bin/env python
+"""STEM/CBED multislice benchmark: probe positions per second.
+
+Workload (one step): the batched STEM scan of a Si [001] supercell, 8x8 lateral
+cells (43.4 Angstrom) and 50 cells thick (199 slices of a/4 -- the reference's
+float32 floor of 271.55/1.35775), 512x512 complex64 grid, 200 keV, 30 mrad,
+Cs = 1 um, 32x32 probe positions on a uniform grid over one unit cell, all 1024
+patterns in one call, each stored as the central 256x256 float32 crop.  The
+potential slices and the probe are built once (their build time is reported
+separately); a step is probe formation -> 199 slices -> CBED for all 1024
+positions.  Inputs are synthetic only in the sense that the crystal is
+generated, not read from a CIF file.
+
+`value` is timed on device-resident inputs; `e2e` times the same call through
+the C ABI with pinned host buffers (transmission stack, probe, positions in;
+CBED stack out) copied inside the timed region.  Under torchrun each rank is
+an independent replica scanning its own 1024 positions (weak scaling, no
+collective on the data path; barriers only for timing).
+
+`--impl reference` times the reference's CPU algorithm (the oracle's port of
+namsa's MSA.multislice process pool, complex64 NumPy FFTs) on the host cores.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = 'STEM probe-positions/sec at ≤1e-3 CBED rel. error vs FP64; learned vs plain'
+UNIT = 'probe-positions/s'
+A_SI = 5.431
+WORKLOAD = 'Si[001] 8x8x50 cells, 512x512 c64, 199 slices (t=a/4), 200 keV, 30 mrad, Cs=1um, 32x32 positions, crop 256'
+# DRAM bytes per launch of the dominant pass, from the ncu capture summarised in
+# profiles/ (keyed by line length, schedule index, waves per launch); None until captured.
+NCU_TRAFFIC = {}
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument('--gpus', type=int, default=1)
+    p.add_argument('--steps', type=int, default=5)
+    p.add_argument('--warmup', type=int, default=3)
+    p.add_argument('--impl', default='ours', choices=['ours', 'reference'])
+    p.add_argument('--group', type=int, default=0, help='waves per resident group (0 = library default)')
+    p.add_argument('--row-sched', type=int, default=-1)
+    p.add_argument('--col-sched', type=int, default=-1)
+    p.add_argument('--no-e2e', action='store_true')
+    p.add_argument('--no-cpu-baseline', action='store_true')
+    p.add_argument('--cpu-sample', type=int, default=0, help='probes per CPU-baseline sample (0 = number of cores)')
+    return p.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get('RANK', 0))
+    world = int(os.environ.get('WORLD_SIZE', 1))
+    local = int(os.environ.get('LOCAL_RANK', 0))
+    return rank, world, local
+
+
+def scan_positions(rank):
+    """32x32 positions (i a/32, j a/32) in [y, x] order over one unit cell; rank r
+    scans the cell r cells along x (replicas scan distinct positions)."""
+    ii, jj = np.meshgrid(np.arange(32), np.arange(32), indexing='ij')
+    return np.column_stack([ii.ravel() * A_SI / 32, jj.ravel() * A_SI / 32 + (rank % 4) * A_SI]).astype(np.float32)
+
+
+PROBE = {'smooth_apert': True, 'apert_smooth': 50, 'spherical_phase': True,
+         'aberration_dict': {'C1': 0., 'C3': 1e4, 'C5': 0.}, 'scherzer': False}
+
+
+# ----------------------------------------------------------------------------- clocks
+class ClockSampler:
+    """nvidia-smi samples of SM clock and throttle reasons while running."""
+    QUERY = ('index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,'
+             'clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,'
+             'clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap')
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(['nvidia-smi', '-i', str(self.index), f'--query-gpu={self.QUERY}',
+                                          '--format=csv,noheader,nounits', '-lms', '200'],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {'sm_mhz': None, 'sm_max_mhz': None, 'reasons': ['nvidia-smi unavailable']}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], None, set()
+        names = ['hw_slowdown', 'hw_thermal_slowdown', 'sw_thermal_slowdown', 'sw_power_cap']
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(',')]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax = float(f[2])
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower().startswith('active'):
+                    reasons.add(n)
+        return {'sm_mhz': float(np.median(sm)) if sm else None, 'sm_max_mhz': smax, 'reasons': sorted(reasons),
+                'samples': len(sm)}
+
+
+# ----------------------------------------------------------------------------- CPU legs
+def cpu_sample(V, sim, positions, nprobe, procs):
+    """Time the oracle's port of the reference CPU path (namsa/msa.py:280-361) on
+    `nprobe` positions with `procs` processes; returns (probes/s, seconds)."""
+    from oracle import msa_oracle as O
+    geom = O.Geometry.__new__(O.Geometry)
+    geom.__dict__.update(dict(sampling=np.asarray(sim.sampling), kmax=float(sim.kmax), lam=float(sim.Lambda),
+                              semi_ang=float(sim.semi_ang), sigma=float(sim.sigma), dims=sim.dims,
+                              pix_size=sim.pix_size))
+    t0 = time.perf_counter()
+    O.cbed_cpu_pool(V, geom, PROBE, sim.slice_t, 1 / 3, positions[:nprobe], procs)
+    dt = time.perf_counter() - t0
+    return nprobe / dt, dt
+
+
+def build_workload(device_index, need_potential):
+    import torch
+    from namsa_gb300 import msa as M
+    from namsa_gb300 import structures
+    sc = structures.silicon((8, 8, 50))
+    sim = M.MSAGPU(200, 30e-3, sc, sampling=np.array([512, 512]), debye_waller=False)
+    sim.setup_device(device_index)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    sim.calc_atomic_potentials()
+    sim.build_potential_slices(A_SI / 4, keep_potential=need_potential)
+    sim.build_probe(PROBE)
+    torch.cuda.synchronize()
+    build_ms = (time.perf_counter() - t0) * 1e3
+    return sim, build_ms
+
+
+def run_reference(args):
+    rank, world, local = dist_env()
+    if rank != 0:
+        return
+    import multiprocessing as mp
+    procs = mp.cpu_count()
+    nprobe = args.cpu_sample or procs
+    # potential slices from the oracle itself (no GPU on this leg)
+    from oracle import msa_oracle as O
+    from namsa_gb300 import structures
+    sc = structures.silicon((8, 8, 50))
+    geom = O.Geometry(np.column_stack([sc['x'], sc['y'], sc['z']]), sc['atomic_number'], 200., 30e-3, [512, 512])
+    _, win = O.atom_windows(geom, np.load(os.path.join(ROOT, 'namsa_gb300', 'data', 'kirkland_params.npy')))
+    V = O.potential_slices_cpu(geom, win, A_SI / 4)
+
+    class S:  # the fields cpu_sample reads
+        pass
+    sim = S()
+    sim.sampling, sim.kmax, sim.Lambda, sim.semi_ang = geom.sampling, geom.kmax, geom.lam, 30e-3
+    sim.sigma, sim.dims, sim.pix_size, sim.slice_t = geom.sigma, geom.dims, geom.pix_size, A_SI / 4
+    pos = scan_positions(0)
+    for _ in range(args.warmup):
+        cpu_sample(V, sim, pos, nprobe, procs)
+    times = []
+    for _ in range(args.steps):
+        _, dt = cpu_sample(V, sim, pos, nprobe, procs)
+        times.append(dt)
+    ms = 1e3 * float(np.mean(times))
+    value = nprobe / (ms / 1e3)
+    line = {'metric': METRIC, 'value': value, 'unit': UNIT, 'n_gpus': args.gpus, 'steps': args.steps,
+            'warmup': args.warmup, 'ms_per_step': ms, 'higher_is_better': True, 'scaling': 'weak',
+            'vs_baseline': None, 'dtype': 'c64', 'data': 'synthetic (generated Si supercell)',
+            'config': {'workload': WORKLOAD, 'sample_probes_per_step': nprobe, 'slices': V.shape[0]},
+            'impl': 'reference',
+            'cpu_baseline': {'value': value, 'unit': UNIT, 'cores': procs, 'kind': 'port',
+                             'sample': f'{nprobe} of the 1024 positions per step, 199 slices, 512^2, '
+                                       f'process pool of {procs} (reference CPU MSA path restated in oracle/)'},
+            'e2e': {'value': value, 'unit': UNIT, 'h2d_bytes_per_step': 0, 'd2h_bytes_per_step': 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args):
+    import torch
+    import torch.distributed as dist
+    from namsa_gb300 import engine
+
+    rank, world, local = dist_env()
+    if world > 1:
+        dist.init_process_group('nccl', init_method='env://')
+    torch.cuda.set_device(local)
+    dev = torch.device('cuda', local)
+    want_cpu = (rank == 0 and world == 1 and not args.no_cpu_baseline)
+
+    sim, build_ms = build_workload(local, need_potential=want_cpu)
+    pos_np = scan_positions(rank)
+    P = len(pos_np)
+    pos = torch.from_numpy(pos_np).to(dev)
+    kmax32 = np.float32(sim.kmax)
+    kband = np.float32(sim.kmax / 3)
+    plan = engine.Plan(512, 512, args.group)
+    r, c, g = plan.schedule
+    plan.set_schedule(r if args.row_sched < 0 else args.row_sched, c if args.col_sched < 0 else args.col_sched)
+    crop = 256
+    out = torch.empty((P, crop, crop), dtype=torch.float32, device=dev)
+
+    def step(o=out):
+        plan.multislice(sim.trans, sim.psi_k_dev, sim.norm_dev, pos, kmax32, sim.Lambda, sim.slice_t, kband,
+                        crop=crop, out=o)
+
+    for _ in range(max(args.warmup, 3)):
+        step()
+    torch.cuda.synchronize()
+    if world > 1:
+        dist.barrier()
+    clocks = ClockSampler(local)
+    clocks.start()
+    time.sleep(0.3)
+    st = torch.cuda.current_stream()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    if world > 1:
+        dist.barrier()
+    e0.record(st)
+    for _ in range(args.steps):
+        step()
+    e1.record(st)
+    torch.cuda.synchronize()
+    if world > 1:
+        dist.barrier()
+    clk = clocks.stop()
+    ms = e0.elapsed_time(e1) / args.steps
+    t = torch.tensor([ms], dtype=torch.float64, device=dev)
+    if world > 1:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    ms_max = float(t.item())
+    value = world * P / (ms_max / 1e3)
+
+    # ---- end to end through the C ABI with pinned host buffers
+    e2e = None
+    if not args.no_e2e:
+        h_trans = sim.trans.cpu().pin_memory()
+        h_psik = sim.psi_k_dev.cpu().pin_memory()
+        h_pos = torch.from_numpy(pos_np).pin_memory()
+        h_out = torch.empty((P, crop, crop), dtype=torch.float32).pin_memory()
+        d_trans = torch.empty_like(sim.trans)
+        d_psik = torch.empty_like(sim.psi_k_dev)
+        d_pos = torch.empty_like(pos)
+
+        def e2e_step():
+            d_trans.copy_(h_trans, non_blocking=True)
+            d_psik.copy_(h_psik, non_blocking=True)
+            d_pos.copy_(h_pos, non_blocking=True)
+            plan.multislice(d_trans, d_psik, sim.norm_dev, d_pos, kmax32, sim.Lambda, sim.slice_t, kband,
+                            crop=crop, out=out)
+            h_out.copy_(out, non_blocking=True)
+        for _ in range(2):
+            e2e_step()
+        torch.cuda.synchronize()
+        if world > 1:
+            dist.barrier()
+        e0.record(st)
+        for _ in range(args.steps):
+            e2e_step()
+        e1.record(st)
+        torch.cuda.synchronize()
+        t2 = torch.tensor([e0.elapsed_time(e1) / args.steps], dtype=torch.float64, device=dev)
+        if world > 1:
+            dist.all_reduce(t2, op=dist.ReduceOp.MAX)
+        bi = h_trans.numel() * 8 + h_psik.numel() * 8 + h_pos.numel() * 4
+        bo = h_out.numel() * 4
+        e2e = {'value': world * P / (float(t2.item()) / 1e3), 'unit': UNIT, 'h2d_bytes_per_step': int(bi),
+               'd2h_bytes_per_step': int(bo), 'ms_per_step': float(t2.item())}
+        del d_trans, h_trans
+
+    # ---- dominant pass timing and roofline
+    row_ms, col_ms, gw = plan.profile(sim.trans, sim.psi_k_dev, sim.norm_dev, pos, kmax32, sim.Lambda, sim.slice_t,
+                                      kband, iters=40)
+    N = 512 * 512
+    dom = 'row' if row_ms >= col_ms else 'col'
+    dom_ms = max(row_ms, col_ms)
+    alg_bytes = 16.0 * N * gw + 8.0 * N
+    alg_flops = (10.0 * N * math.log2(512) + 15.0 * N) * gw
+    peaks = {}
+    pk_path = os.path.join(ROOT, 'MEASURED_PEAKS.json')
+    if os.path.exists(pk_path):
+        peaks = json.load(open(pk_path))
+    hbm_peak = peaks.get('hbm_gbs')
+    peak_src = 'measured' if hbm_peak else 'fallback'
+    hbm_peak = hbm_peak or 6800.0
+    achieved = alg_bytes / (dom_ms / 1e3) / 1e9
+    sm_clock = (clk.get('sm_mhz') or 1900.0)
+    fp32_peak = 152 * 128 * 2 * sm_clock * 1e6 / 1e12
+    roof = {'bound': 'hbm', 'achieved': achieved, 'peak': hbm_peak, 'unit': 'GB/s', 'frac': achieved / hbm_peak,
+            'traffic': NCU_TRAFFIC.get((512, plan.schedule[0] if dom == 'row' else plan.schedule[1], gw)),
+            'kernel': f'{dom}_pass_kernel (512, {gw} waves per launch)', 'peak_source': f'{peak_src} hbm_gbs',
+            'launch_ms': dom_ms, 'row_pass_ms': row_ms, 'col_pass_ms': col_ms,
+            'fp32': {'achieved_tflops': alg_flops / (dom_ms / 1e3) / 1e12, 'peak_tflops': fp32_peak,
+                     'frac': alg_flops / (dom_ms / 1e3) / 1e12 / fp32_peak,
+                     'peak_source': f'nominal 152 SM x 128 FP32 lanes x 2 at the sampled {sm_clock:.0f} MHz'}}
+
+    groups = math.ceil(P / plan.schedule[2])
+    launches = args.steps * (1 + groups * (1 + 2 * sim.num_slices))
+    line = {'metric': METRIC, 'value': value, 'unit': UNIT, 'n_gpus': world, 'steps': args.steps,
+            'warmup': args.warmup, 'ms_per_step': ms_max, 'higher_is_better': True, 'scaling': 'weak',
+            'vs_baseline': None, 'dtype': 'c64',
+            'data': 'synthetic (generated Si supercell; inputs resident in HBM for value, pinned host for e2e)',
+            'config': {'workload': WORKLOAD, 'global_batch': world * P, 'probes_per_gpu': P,
+                       'grid': [512, 512], 'slices': int(sim.num_slices), 'crop': crop,
+                       'parallelism': f'replicas x{world}' if world > 1 else 'single GPU',
+                       'l2': 'inputs larger than L2 (transmission stack 398 MiB, CBED out 256 MiB)',
+                       'schedule': {'row': engine.schedules(512)[plan.schedule[0]],
+                                    'col': engine.schedules(512)[plan.schedule[1]], 'group': plan.schedule[2]},
+                       'potential_and_probe_build_ms': build_ms},
+            'gpu_launches': int(launches), 'clocks': clk, 'e2e': e2e, 'roofline': roof}
+
+    if want_cpu:
+        import multiprocessing as mp
+        procs = mp.cpu_count()
+        nprobe = args.cpu_sample or procs
+        V = sim.potential.cpu().numpy()
+        v, dt = cpu_sample(V, sim, pos_np, nprobe, procs)
+        line['cpu_baseline'] = {'value': v, 'unit': UNIT, 'cores': procs, 'kind': 'port',
+                                'sample': f'{nprobe} of the 1024 positions, 199 slices, 512^2, {dt:.1f} s wall, '
+                                          f'reference CPU MSA path (oracle port), process pool of {procs}'}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    plan.close()
+    if world > 1:
+        dist.destroy_process_group()
+
+
+def main():
+    args = parse()
+    if args.impl == 'reference':
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == '__main__':
+    main()

@@ -1,0 +1,166 @@
+/*
+ * msx.h -- C ABI of the GB300 multislice engine (libmsx.so).
+ *
+ * The engine replaces the GPU path of namsa's MSAGPU simulator
+ * (namsa/msa.py:529-992 with the kernels of namsa/probe_kernels.cu and
+ * namsa/potential_kernels.cu, launched through pycuda and cuFFT).  In the
+ * reference that path is reached through the kernel loader
+ * (namsa/cuda_kernels.py:8-57: ProbeKernels / PotentialKernels return
+ * dicts of pycuda Functions taking raw device pointers).  This header is the
+ * equivalent plugin boundary: plain pointers, sizes and a stream handle.
+ *
+ * Conventions
+ *  - Every call returns an int status: MSX_OK (0) or a negative MSX_ERR_*.
+ *    msx_last_error() copies the message of the last failure of the calling
+ *    thread.
+ *  - All array arguments named *_dev are device pointers owned by the caller,
+ *    contiguous, row-major.  complex64 arrays are interleaved (re, im) float
+ *    pairs.  Nothing is synchronised: work is ordered on `stream`
+ *    (a cudaStream_t, NULL = the legacy default stream).
+ *  - A plan owns its workspace and is not re-entrant; distinct plans may be
+ *    used from distinct threads.
+ *  - Supported grid line lengths (msx_supported_size): 64, 128, 256, 384,
+ *    512, 768, 1024 on each axis.
+ */
+#ifndef MSX_H_
+#define MSX_H_
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define MSX_OK 0
+#define MSX_ERR_INVALID -1      /* bad argument (size, pointer, range)          */
+#define MSX_ERR_UNSUPPORTED -2  /* grid line length without a compiled schedule */
+#define MSX_ERR_CUDA -3         /* CUDA runtime error (launch, configuration)   */
+#define MSX_ERR_ALLOC -4        /* device allocation failed                     */
+
+#if defined(__GNUC__)
+#define MSX_API __attribute__((visibility("default")))
+#else
+#define MSX_API
+#endif
+
+typedef struct msx_plan msx_plan;
+
+/* Library version (major*10000 + minor*100 + patch). */
+MSX_API int msx_version(void);
+
+/* Copies the last error message of the calling thread into buf (NUL-terminated).
+ * Returns the message length. */
+MSX_API int msx_last_error(char* buf, size_t len);
+
+/* 1 if n is a supported grid line length, else 0. */
+MSX_API int msx_supported_size(int n);
+
+/* Number of compiled FFT schedules for line length n, and the name of one. */
+MSX_API int msx_num_schedules(int n);
+MSX_API int msx_schedule_name(int n, int index, char* buf, size_t len);
+
+/*
+ * Projected Kirkland potential windows of `nspecies` species.
+ * Replaces MSA.calc_atomic_potentials / MSA._get_potential
+ * (namsa/msa.py:137-146, 180-196) and bin_2d_array (namsa/utils.py:101-108),
+ * which the reference evaluates on the host with scipy.
+ *   coeff_dev     (nspecies, 4, 3) float64 Kirkland a, b, c, d rows
+ *   n0, n1        oversampled grid points per axis (floor(range/pix) * oversample)
+ *   windows_out   (nspecies, n0/oversample, n1/oversample) float32
+ */
+MSX_API int msx_atom_windows(const double* coeff_dev, int nspecies, int n0, int n1, int oversample, double potential_range,
+                     float* windows_out_dev, void* stream);
+
+/*
+ * Transmission slices t = exp(i sigma V) of the supercell.
+ * Replaces MSAGPU.build_potential_slices (namsa/msa.py:580-647) and the
+ * BuildScatteringPotential kernel (namsa/potential_kernels.cu:5-60).
+ *   sites_dev          (nsites, 4) int32 rows (species index, y pixel, x pixel, unused),
+ *                      grouped by slice in supercell order
+ *   slice_offsets_dev  (num_slices + 1) int32: sites of slice s are [off[s], off[s+1])
+ *   windows_dev        (nspecies, window_h, window_w) float32
+ *   trans_out_dev      (num_slices, ny, nx) complex64
+ *   potential_out_dev  (num_slices, ny, nx) float32 summed potential V, or NULL
+ */
+MSX_API int msx_build_transmission(const int* sites_dev, const int* slice_offsets_dev, int num_slices, const float* windows_dev,
+                           int window_h, int window_w, int ny, int nx, float sigma, float* trans_out_dev,
+                           float* potential_out_dev, void* stream);
+
+/*
+ * k-space probe psi_k = A(k) exp(-i chi(k)) and its normalisation.
+ * Replaces MSAGPU.build_probe (namsa/msa.py:669-735) with the soft_aperture,
+ * hard_aperture, spherical_phase_error and mult_wise_c2d_re2d kernels
+ * (namsa/probe_kernels.cu:126-134, 180-222).
+ *   kmax               float32 k-grid extent (1/Angstrom)
+ *   k_semi             float32 aperture radius semi_angle/lambda
+ *   c1, c3, c5         defocus and spherical aberrations (Angstrom)
+ *   smooth_aperture    1: 1/(1+exp(-160 (k_semi-k))), 0: k < k_semi
+ *   psi_k_out_dev      (ny, nx) complex64
+ *   aperture_out_dev   (ny, nx) float32 or NULL
+ *   normalization_dev  1 float64: sum |fftshift(ifft2(psi_k))|^2 (unnormalised ifft), or NULL
+ */
+MSX_API int msx_build_probe(int ny, int nx, float kmax, double lambda, float k_semi, double c1, double c3, double c5,
+                    int smooth_aperture, float* psi_k_out_dev, float* aperture_out_dev, double* normalization_dev,
+                    void* stream);
+
+/*
+ * Multislice plan for an (ny, nx) grid.  `group` is the number of probe
+ * wavefunctions kept resident per group (0 = pick by size).  Replaces the
+ * per-batch cuFFT plans and allocations of MSAGPU.multislice
+ * (namsa/msa.py:843-881) and plan_simulation's batching
+ * (namsa/msa.py:445-461).
+ */
+MSX_API int msx_plan_create(int ny, int nx, int group, msx_plan** plan);
+MSX_API int msx_plan_destroy(msx_plan* plan);
+
+/* Selects the FFT schedule of the row (x) and column (y) passes (index into
+ * msx_num_schedules of nx / ny) and the group size; group 0 keeps the
+ * current one.  The workspace grows when needed. */
+MSX_API int msx_plan_set_schedule(msx_plan* plan, int row_schedule, int col_schedule, int group);
+
+/* Reports the current row/column schedule indices and group size. */
+MSX_API int msx_plan_get_schedule(const msx_plan* plan, int* row_schedule, int* col_schedule, int* group);
+
+/* 1 = record the launch sequence of msx_multislice in a CUDA graph and
+ * replay it while the arguments repeat (default 1); 0 = launch directly. */
+MSX_API int msx_plan_set_graph(msx_plan* plan, int enable);
+
+/*
+ * STEM/CBED multislice over num_probes positions.
+ * Replaces MSAGPU.multislice / MSAGPU.__propagate_beams
+ * (namsa/msa.py:767-992): probe stack with phase ramps, inverse FFT and
+ * fftshift (build_probes_stack, fftshift_2d_stack), then for each slice
+ * psi <- ifft2(P mask fft2(psi t_s / N)), then |fft2(psi / N) sqrt(N)|^2 / norm.
+ *   trans_dev          (num_slices, ny, nx) complex64 transmission slices
+ *   psi_k_dev          (ny, nx) complex64 k-space probe (msx_build_probe)
+ *   normalization_dev  1 float64 (msx_build_probe)
+ *   positions_dev      (num_probes, 2) float32 [y, x] in Angstrom, the reference's
+ *                      probe_positions layout
+ *   kmax               float32 k-grid extent; lambda, slice_t in Angstrom
+ *   k_band             float32 radius of the bandwidth mask in 1/Angstrom, the reference's
+ *                      float32(bandwidth * kmax) (msa.py:833; default bandwidth 1/3)
+ *   cbed_out_dev       (num_probes, crop_y, crop_x) float32: rows ny/2-crop_y/2 ..
+ *                      and columns nx/2-crop_x/2 .. of the CBED; crop = ny, nx keeps all
+ */
+MSX_API int msx_multislice(msx_plan* plan, const float* trans_dev, int num_slices, const float* psi_k_dev,
+                   const double* normalization_dev, const float* positions_dev, int num_probes, float kmax,
+                   double lambda, double slice_t, float k_band, float* cbed_out_dev, int crop_y, int crop_x,
+                   void* stream);
+
+/*
+ * Diagnostics: times one row pass and one column pass of the plan's first
+ * group, `iters` times each, with CUDA events on `stream` (one slice of
+ * msx_multislice per iteration).  ms_out[0] = mean row-pass ms, ms_out[1] =
+ * mean column-pass ms, ms_out[2] = waves per launch.  Synchronises `stream`.
+ * No counterpart in the reference (its launches are timed by host clocks,
+ * namsa/msa.py:847-909).
+ */
+MSX_API int msx_plan_profile(msx_plan* plan, const float* trans_dev, int num_slices, const float* psi_k_dev,
+                             const double* normalization_dev, const float* positions_dev, int num_probes, float kmax,
+                             double lambda, double slice_t, float k_band, int iters, float* ms_out, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* MSX_H_ */

@@ -1,0 +1,92 @@
+"""ctypes binding of libmsx.so (the C ABI declared in include/msx.h).
+
+The library is built in-tree by ``namsa_gb300.build``.  There is no CPU
+fallback: if the shared object is missing or fails to load, importing the
+engine raises ``MsxLibraryError``.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, 'libmsx.so')
+
+MSX_OK = 0
+MSX_ERR_INVALID = -1
+MSX_ERR_UNSUPPORTED = -2
+MSX_ERR_CUDA = -3
+MSX_ERR_ALLOC = -4
+
+# (name, restype, argtypes) for every entry point of include/msx.h
+_c = ctypes
+_vp = _c.c_void_p
+SIGNATURES = [
+    ('msx_version', _c.c_int, []),
+    ('msx_last_error', _c.c_int, [_c.c_char_p, _c.c_size_t]),
+    ('msx_supported_size', _c.c_int, [_c.c_int]),
+    ('msx_num_schedules', _c.c_int, [_c.c_int]),
+    ('msx_schedule_name', _c.c_int, [_c.c_int, _c.c_int, _c.c_char_p, _c.c_size_t]),
+    ('msx_atom_windows', _c.c_int, [_vp, _c.c_int, _c.c_int, _c.c_int, _c.c_int, _c.c_double, _vp, _vp]),
+    ('msx_build_transmission', _c.c_int, [_vp, _vp, _c.c_int, _vp, _c.c_int, _c.c_int, _c.c_int, _c.c_int,
+                                          _c.c_float, _vp, _vp, _vp]),
+    ('msx_build_probe', _c.c_int, [_c.c_int, _c.c_int, _c.c_float, _c.c_double, _c.c_float, _c.c_double,
+                                   _c.c_double, _c.c_double, _c.c_int, _vp, _vp, _vp, _vp]),
+    ('msx_plan_create', _c.c_int, [_c.c_int, _c.c_int, _c.c_int, _c.POINTER(_vp)]),
+    ('msx_plan_destroy', _c.c_int, [_vp]),
+    ('msx_plan_set_schedule', _c.c_int, [_vp, _c.c_int, _c.c_int, _c.c_int]),
+    ('msx_plan_get_schedule', _c.c_int, [_vp, _c.POINTER(_c.c_int), _c.POINTER(_c.c_int), _c.POINTER(_c.c_int)]),
+    ('msx_plan_set_graph', _c.c_int, [_vp, _c.c_int]),
+    ('msx_multislice', _c.c_int, [_vp, _vp, _c.c_int, _vp, _vp, _vp, _c.c_int, _c.c_float, _c.c_double,
+                                  _c.c_double, _c.c_float, _vp, _c.c_int, _c.c_int, _vp]),
+    ('msx_plan_profile', _c.c_int, [_vp, _vp, _c.c_int, _vp, _vp, _vp, _c.c_int, _c.c_float, _c.c_double,
+                                    _c.c_double, _c.c_float, _c.c_int, _c.POINTER(_c.c_float), _vp]),
+]
+
+
+class MsxLibraryError(ImportError):
+    """libmsx.so is missing or does not load."""
+
+
+class MsxError(RuntimeError):
+    """A libmsx call returned a non-zero status."""
+
+    def __init__(self, code, message):
+        super().__init__(f'libmsx error {code}: {message}')
+        self.code = code
+
+
+_lib = None
+
+
+def load():
+    """Load libmsx.so once and attach the ctypes signatures."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise MsxLibraryError(f'{LIB_PATH} not found; build it with `python -m namsa_gb300.build`')
+    try:
+        lib = ctypes.CDLL(LIB_PATH)
+    except OSError as exc:
+        raise MsxLibraryError(f'cannot load {LIB_PATH}: {exc}') from exc
+    for name, res, args in SIGNATURES:
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = lib
+    return lib
+
+
+def last_error():
+    lib = load()
+    buf = ctypes.create_string_buffer(1024)
+    lib.msx_last_error(buf, len(buf))
+    return buf.value.decode(errors='replace')
+
+
+def check(rc):
+    """Raise MsxError when a libmsx call failed."""
+    if rc != MSX_OK:
+        raise MsxError(rc, last_error())
+    return rc

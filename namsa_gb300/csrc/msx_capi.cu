@@ -1,0 +1,454 @@
+// C ABI of libmsx.so (declared in include/msx.h): argument checks, plans,
+// schedule tables and the multislice launch sequence.
+#include "msx.h"
+#include "msx_internal.h"
+
+#include <cstdarg>
+#include <cstdint>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+using namespace msx;
+
+namespace {
+
+thread_local std::string g_err;
+
+int fail(int code, const char* fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  g_err = buf;
+  return code;
+}
+
+int cuda_fail(cudaError_t e, const char* what) {
+  return fail(MSX_ERR_CUDA, "%s: %s (%s)", what, cudaGetErrorString(e), cudaGetErrorName(e));
+}
+
+#define MSX_CUDA(call, what)                   \
+  do {                                         \
+    cudaError_t e_ = (call);                   \
+    if (e_ != cudaSuccess) return cuda_fail(e_, what); \
+  } while (0)
+
+int schedule_table(int n, const SchedOps** ops) {
+  switch (n) {
+    case 64: return schedules_64(ops);
+    case 128: return schedules_128(ops);
+    case 256: return schedules_256(ops);
+    case 384: return schedules_384(ops);
+    case 512: return schedules_512(ops);
+    case 768: return schedules_768(ops);
+    case 1024: return schedules_1024(ops);
+    default: *ops = nullptr; return 0;
+  }
+}
+
+// cudaFuncSetAttribute must run once per device for every kernel of a schedule.
+constexpr int kMaxDevices = 64;
+constexpr int kMaxSchedPerSize = 8;
+bool g_configured[kMaxDevices][8][kMaxSchedPerSize];
+
+int size_slot(int n) {
+  switch (n) {
+    case 64: return 0; case 128: return 1; case 256: return 2; case 384: return 3;
+    case 512: return 4; case 768: return 5; case 1024: return 6; default: return 7;
+  }
+}
+
+int ensure_configured(int device, int n, int idx, const SchedOps& op) {
+  if (device < 0 || device >= kMaxDevices || idx >= kMaxSchedPerSize) return fail(MSX_ERR_INVALID, "device/schedule index out of range");
+  bool& done = g_configured[device][size_slot(n)][idx];
+  if (!done) {
+    MSX_CUDA(op.configure(), "configuring pass kernels");
+    done = true;
+  }
+  return MSX_OK;
+}
+
+bool aligned(const void* p, size_t a) { return (reinterpret_cast<uintptr_t>(p) % a) == 0; }
+
+}  // namespace
+
+struct msx_plan {
+  int ny = 0, nx = 0, device = 0;
+  int group = 0;
+  int row_sched = 0, col_sched = 0;
+  const SchedOps* row_ops = nullptr;
+  const SchedOps* col_ops = nullptr;
+  float2* psi = nullptr;
+  size_t psi_waves = 0;
+  float2* ptab = nullptr;
+  float2* tw_row = nullptr;
+  float2* tw_col = nullptr;
+  cudaStream_t work = nullptr;
+  cudaEvent_t ev_in = nullptr, ev_out = nullptr;
+  bool use_graph = true;
+  cudaGraphExec_t gexec = nullptr;
+  std::vector<unsigned char> gkey;
+};
+
+namespace {
+
+int upload_twiddles(const SchedOps& op, float2** dst) {
+  std::vector<float2> h(op.tw_words > 0 ? op.tw_words : 1);
+  op.host_twiddles(h.data());
+  if (*dst) cudaFree(*dst);
+  *dst = nullptr;
+  cudaError_t e = cudaMalloc(dst, sizeof(float2) * h.size());
+  if (e != cudaSuccess) return fail(MSX_ERR_ALLOC, "twiddle table allocation failed: %s", cudaGetErrorString(e));
+  MSX_CUDA(cudaMemcpy(*dst, h.data(), sizeof(float2) * h.size(), cudaMemcpyHostToDevice), "twiddle upload");
+  return MSX_OK;
+}
+
+int ensure_workspace(msx_plan* p, size_t waves) {
+  if (waves <= p->psi_waves) return MSX_OK;
+  if (p->psi) cudaFree(p->psi);
+  p->psi = nullptr;
+  p->psi_waves = 0;
+  cudaError_t e = cudaMalloc(&p->psi, sizeof(float2) * waves * (size_t)p->ny * p->nx);
+  if (e != cudaSuccess) return fail(MSX_ERR_ALLOC, "workspace of %zu waves (%d x %d) failed: %s", waves, p->ny, p->nx,
+                                    cudaGetErrorString(e));
+  p->psi_waves = waves;
+  return MSX_OK;
+}
+
+void drop_graph(msx_plan* p) {
+  if (p->gexec) cudaGraphExecDestroy(p->gexec);
+  p->gexec = nullptr;
+  p->gkey.clear();
+}
+
+int auto_group(int ny, int nx) {
+  // Keep a group's waves (complex64) within about 48 MiB so that the row and
+  // column passes of one slice find them in L2.
+  const size_t wave = sizeof(float2) * (size_t)ny * nx;
+  size_t g = (48u << 20) / wave;
+  if (g < 4) g = 4;
+  if (g > 512) g = 512;
+  return (int)g;
+}
+
+struct MsArgs {
+  const float* trans; int num_slices; const float* psik; const double* norm; const float* pos; int num_probes;
+  float kmax; double lambda, slice_t; float k_band; float* cbed; int crop_y, crop_x;
+  int group, row_sched, col_sched;
+};
+
+int enqueue_multislice(msx_plan* p, const MsArgs& a, cudaStream_t st) {
+  const int ny = p->ny, nx = p->nx;
+  MSX_CUDA(launch_ptab(ny, nx, a.kmax, a.lambda, a.slice_t, a.k_band, p->ptab, st), "propagator table");
+  const size_t wave = (size_t)ny * nx;
+  const int y0 = ny / 2 - a.crop_y / 2, x0 = nx / 2 - a.crop_x / 2;
+  const float2* trans = reinterpret_cast<const float2*>(a.trans);
+  for (int g0 = 0; g0 < a.num_probes; g0 += a.group) {
+    const int gn = (a.num_probes - g0 < a.group) ? a.num_probes - g0 : a.group;
+    ColArgs c{};
+    c.psi = p->psi;
+    c.ptab = p->ptab;
+    c.psik = reinterpret_cast<const float2*>(a.psik);
+    c.pos_yx = a.pos + 2 * (size_t)g0;
+    c.tw = p->tw_col;
+    c.norm = a.norm;
+    c.cbed = a.cbed + (size_t)g0 * a.crop_y * a.crop_x;
+    c.G = gn;
+    c.Nx = nx;
+    c.kmax = a.kmax;
+    c.y0 = y0;
+    c.crop_y = a.crop_y;
+    if (a.num_slices == 0) {
+      c.x_begin = x0;
+      c.ncols = a.crop_x;
+      MSX_CUDA(p->col_ops->col(COL_INIT_FINAL, c, st), "probe-only pass");
+      continue;
+    }
+    c.x_begin = 0;
+    c.ncols = nx;
+    MSX_CUDA(p->col_ops->col(COL_INIT, c, st), "probe formation pass");
+    for (int s = 0; s < a.num_slices; ++s) {
+      MSX_CUDA(p->row_ops->row(p->psi, trans + (size_t)s * wave, p->tw_row, gn, ny, st), "row pass");
+      if (s + 1 < a.num_slices) {
+        MSX_CUDA(p->col_ops->col(COL_MID, c, st), "column pass");
+      } else {
+        ColArgs f = c;
+        f.x_begin = x0;
+        f.ncols = a.crop_x;
+        MSX_CUDA(p->col_ops->col(COL_FINAL, f, st), "final column pass");
+      }
+    }
+  }
+  return MSX_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int msx_version(void) { return 1 * 10000 + 0 * 100 + 0; }
+
+int msx_last_error(char* buf, size_t len) {
+  if (buf && len) {
+    std::strncpy(buf, g_err.c_str(), len - 1);
+    buf[len - 1] = '\0';
+  }
+  return (int)g_err.size();
+}
+
+int msx_supported_size(int n) {
+  const SchedOps* ops;
+  return schedule_table(n, &ops) > 0 ? 1 : 0;
+}
+
+int msx_num_schedules(int n) {
+  const SchedOps* ops;
+  return schedule_table(n, &ops);
+}
+
+int msx_schedule_name(int n, int index, char* buf, size_t len) {
+  const SchedOps* ops;
+  const int cnt = schedule_table(n, &ops);
+  if (index < 0 || index >= cnt) return fail(MSX_ERR_INVALID, "no schedule %d for length %d", index, n);
+  if (buf && len) {
+    std::strncpy(buf, ops[index].name, len - 1);
+    buf[len - 1] = '\0';
+  }
+  return MSX_OK;
+}
+
+int msx_atom_windows(const double* coeff_dev, int nspecies, int n0, int n1, int oversample, double potential_range,
+                     float* windows_out_dev, void* stream) {
+  if (!coeff_dev || !windows_out_dev) return fail(MSX_ERR_INVALID, "null pointer");
+  if (nspecies <= 0 || oversample <= 0 || n0 < 2 || n1 < 2 || n0 % oversample || n1 % oversample)
+    return fail(MSX_ERR_INVALID, "bad window grid %d x %d (oversample %d, %d species)", n0, n1, oversample, nspecies);
+  if (!(potential_range > 0)) return fail(MSX_ERR_INVALID, "potential range must be positive");
+  if ((size_t)(n0 / oversample) * (n1 / oversample) > 24000)
+    return fail(MSX_ERR_INVALID, "window %d x %d too large", n0 / oversample, n1 / oversample);
+  MSX_CUDA(launch_atom_windows(coeff_dev, nspecies, n0, n1, oversample, potential_range, windows_out_dev,
+                               (cudaStream_t)stream), "atom windows");
+  return MSX_OK;
+}
+
+int msx_build_transmission(const int* sites_dev, const int* slice_offsets_dev, int num_slices, const float* windows_dev,
+                           int window_h, int window_w, int ny, int nx, float sigma, float* trans_out_dev,
+                           float* potential_out_dev, void* stream) {
+  if (num_slices < 0 || ny <= 0 || nx <= 0 || window_h <= 0 || window_w <= 0)
+    return fail(MSX_ERR_INVALID, "bad sizes (slices %d, grid %d x %d, window %d x %d)", num_slices, ny, nx, window_h,
+                window_w);
+  if (num_slices == 0) return MSX_OK;
+  if (!sites_dev || !slice_offsets_dev || !windows_dev || !trans_out_dev) return fail(MSX_ERR_INVALID, "null pointer");
+  if (!aligned(sites_dev, 16)) return fail(MSX_ERR_INVALID, "sites must be 16-byte aligned (int32 rows of 4)");
+  if (!aligned(trans_out_dev, 8)) return fail(MSX_ERR_INVALID, "transmission output must be 8-byte aligned");
+  if (num_slices > 65535) return fail(MSX_ERR_INVALID, "at most 65535 slices");
+  MSX_CUDA(launch_potential(reinterpret_cast<const int4*>(sites_dev), slice_offsets_dev, num_slices, windows_dev, window_h,
+                            window_w, ny, nx, sigma, reinterpret_cast<float2*>(trans_out_dev), potential_out_dev,
+                            (cudaStream_t)stream), "transmission slices");
+  return MSX_OK;
+}
+
+int msx_build_probe(int ny, int nx, float kmax, double lambda, float k_semi, double c1, double c3, double c5,
+                    int smooth_aperture, float* psi_k_out_dev, float* aperture_out_dev, double* normalization_dev,
+                    void* stream) {
+  if (ny < 2 || nx < 2 || ny > 65535) return fail(MSX_ERR_INVALID, "bad grid %d x %d", ny, nx);
+  if (!psi_k_out_dev) return fail(MSX_ERR_INVALID, "null psi_k output");
+  if (!aligned(psi_k_out_dev, 8)) return fail(MSX_ERR_INVALID, "psi_k must be 8-byte aligned");
+  if (!(lambda > 0) || !(kmax > 0)) return fail(MSX_ERR_INVALID, "lambda and kmax must be positive");
+  MSX_CUDA(launch_probe(ny, nx, kmax, lambda, k_semi, c1, c3, c5, smooth_aperture,
+                        reinterpret_cast<float2*>(psi_k_out_dev), aperture_out_dev, normalization_dev,
+                        (cudaStream_t)stream), "probe");
+  return MSX_OK;
+}
+
+int msx_plan_create(int ny, int nx, int group, msx_plan** out) {
+  if (!out) return fail(MSX_ERR_INVALID, "null plan pointer");
+  *out = nullptr;
+  if (!msx_supported_size(ny) || !msx_supported_size(nx))
+    return fail(MSX_ERR_UNSUPPORTED, "grid %d x %d: supported line lengths are 64, 128, 256, 384, 512, 768, 1024", ny, nx);
+  if (group < 0) return fail(MSX_ERR_INVALID, "group must be >= 0");
+  int device = 0;
+  MSX_CUDA(cudaGetDevice(&device), "cudaGetDevice");
+  msx_plan* p = new msx_plan();
+  p->ny = ny;
+  p->nx = nx;
+  p->device = device;
+  int rc = msx_plan_set_schedule(p, 0, 0, group > 0 ? group : auto_group(ny, nx));
+  if (rc == MSX_OK) {
+    cudaError_t e = cudaMalloc(&p->ptab, sizeof(float2) * (size_t)ny * nx);
+    if (e != cudaSuccess) rc = fail(MSX_ERR_ALLOC, "propagator table allocation failed");
+  }
+  if (rc == MSX_OK) {
+    cudaError_t e = cudaStreamCreateWithFlags(&p->work, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&p->ev_in, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&p->ev_out, cudaEventDisableTiming);
+    if (e != cudaSuccess) rc = cuda_fail(e, "plan stream/events");
+  }
+  if (rc != MSX_OK) {
+    msx_plan_destroy(p);
+    return rc;
+  }
+  *out = p;
+  return MSX_OK;
+}
+
+int msx_plan_destroy(msx_plan* p) {
+  if (!p) return MSX_OK;
+  drop_graph(p);
+  if (p->psi) cudaFree(p->psi);
+  if (p->ptab) cudaFree(p->ptab);
+  if (p->tw_row) cudaFree(p->tw_row);
+  if (p->tw_col) cudaFree(p->tw_col);
+  if (p->ev_in) cudaEventDestroy(p->ev_in);
+  if (p->ev_out) cudaEventDestroy(p->ev_out);
+  if (p->work) cudaStreamDestroy(p->work);
+  delete p;
+  return MSX_OK;
+}
+
+int msx_plan_set_schedule(msx_plan* p, int row_schedule, int col_schedule, int group) {
+  if (!p) return fail(MSX_ERR_INVALID, "null plan");
+  const SchedOps *rops, *cops;
+  const int nr = schedule_table(p->nx, &rops), nc = schedule_table(p->ny, &cops);
+  if (row_schedule < 0 || row_schedule >= nr || col_schedule < 0 || col_schedule >= nc)
+    return fail(MSX_ERR_INVALID, "schedule (%d, %d) out of range (%d, %d)", row_schedule, col_schedule, nr, nc);
+  if (group < 0 || group > 65535) return fail(MSX_ERR_INVALID, "group %d out of range", group);
+  int rc = ensure_configured(p->device, p->nx, row_schedule, rops[row_schedule]);
+  if (rc == MSX_OK) rc = ensure_configured(p->device, p->ny, col_schedule, cops[col_schedule]);
+  if (rc != MSX_OK) return rc;
+  if (!p->row_ops || p->row_sched != row_schedule) {
+    rc = upload_twiddles(rops[row_schedule], &p->tw_row);
+    if (rc != MSX_OK) return rc;
+  }
+  if (!p->col_ops || p->col_sched != col_schedule) {
+    rc = upload_twiddles(cops[col_schedule], &p->tw_col);
+    if (rc != MSX_OK) return rc;
+  }
+  p->row_sched = row_schedule;
+  p->col_sched = col_schedule;
+  p->row_ops = &rops[row_schedule];
+  p->col_ops = &cops[col_schedule];
+  if (group > 0) p->group = group;
+  drop_graph(p);
+  return ensure_workspace(p, (size_t)p->group);
+}
+
+int msx_plan_get_schedule(const msx_plan* p, int* row_schedule, int* col_schedule, int* group) {
+  if (!p) return fail(MSX_ERR_INVALID, "null plan");
+  if (row_schedule) *row_schedule = p->row_sched;
+  if (col_schedule) *col_schedule = p->col_sched;
+  if (group) *group = p->group;
+  return MSX_OK;
+}
+
+int msx_plan_set_graph(msx_plan* p, int enable) {
+  if (!p) return fail(MSX_ERR_INVALID, "null plan");
+  p->use_graph = enable != 0;
+  if (!p->use_graph) drop_graph(p);
+  return MSX_OK;
+}
+
+int msx_multislice(msx_plan* p, const float* trans_dev, int num_slices, const float* psi_k_dev,
+                   const double* normalization_dev, const float* positions_dev, int num_probes, float kmax,
+                   double lambda, double slice_t, float k_band, float* cbed_out_dev, int crop_y, int crop_x,
+                   void* stream) {
+  if (!p) return fail(MSX_ERR_INVALID, "null plan");
+  if (num_probes < 0 || num_slices < 0) return fail(MSX_ERR_INVALID, "negative probe or slice count");
+  if (num_probes == 0) return MSX_OK;
+  if (crop_y <= 0 || crop_x <= 0 || crop_y > p->ny || crop_x > p->nx)
+    return fail(MSX_ERR_INVALID, "crop %d x %d outside the %d x %d grid", crop_y, crop_x, p->ny, p->nx);
+  if (!psi_k_dev || !normalization_dev || !positions_dev || !cbed_out_dev || (num_slices > 0 && !trans_dev))
+    return fail(MSX_ERR_INVALID, "null pointer");
+  if (!aligned(trans_dev, 8) || !aligned(psi_k_dev, 8) || !aligned(positions_dev, 8) || !aligned(normalization_dev, 8))
+    return fail(MSX_ERR_INVALID, "complex inputs, positions and the normalisation must be 8-byte aligned");
+  if (!(kmax > 0) || !(lambda > 0) || !(slice_t >= 0) || !(k_band >= 0))
+    return fail(MSX_ERR_INVALID, "kmax, lambda must be positive; slice thickness and k_band non-negative");
+  int dev = 0;
+  MSX_CUDA(cudaGetDevice(&dev), "cudaGetDevice");
+  if (dev != p->device) return fail(MSX_ERR_INVALID, "plan belongs to device %d, current device is %d", p->device, dev);
+
+  MsArgs a;
+  std::memset(&a, 0, sizeof(a));  // the struct doubles as the graph cache key: no stray padding bytes
+  a.trans = trans_dev; a.num_slices = num_slices; a.psik = psi_k_dev; a.norm = normalization_dev;
+  a.pos = positions_dev; a.num_probes = num_probes; a.kmax = kmax; a.lambda = lambda; a.slice_t = slice_t;
+  a.k_band = k_band; a.cbed = cbed_out_dev; a.crop_y = crop_y; a.crop_x = crop_x;
+  a.group = p->group; a.row_sched = p->row_sched; a.col_sched = p->col_sched;
+  cudaStream_t caller = (cudaStream_t)stream;
+  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+  MSX_CUDA(cudaStreamIsCapturing(caller, &cap), "cudaStreamIsCapturing");
+  if (cap != cudaStreamCaptureStatusNone || !p->use_graph) return enqueue_multislice(p, a, caller);
+
+  // Run on the plan's stream, ordered after and before the caller's stream.
+  MSX_CUDA(cudaEventRecord(p->ev_in, caller), "cudaEventRecord");
+  MSX_CUDA(cudaStreamWaitEvent(p->work, p->ev_in, 0), "cudaStreamWaitEvent");
+  std::vector<unsigned char> key(sizeof(MsArgs));
+  std::memcpy(key.data(), &a, sizeof(MsArgs));
+  if (!p->gexec || key != p->gkey) {
+    drop_graph(p);
+    cudaGraph_t graph = nullptr;
+    MSX_CUDA(cudaStreamBeginCapture(p->work, cudaStreamCaptureModeThreadLocal), "cudaStreamBeginCapture");
+    const int rc = enqueue_multislice(p, a, p->work);
+    cudaError_t e = cudaStreamEndCapture(p->work, &graph);
+    if (rc != MSX_OK) {
+      if (graph) cudaGraphDestroy(graph);
+      return rc;
+    }
+    if (e != cudaSuccess) return cuda_fail(e, "cudaStreamEndCapture");
+    e = cudaGraphInstantiate(&p->gexec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (e != cudaSuccess) {
+      p->gexec = nullptr;
+      return cuda_fail(e, "cudaGraphInstantiate");
+    }
+    p->gkey = key;
+  }
+  MSX_CUDA(cudaGraphLaunch(p->gexec, p->work), "cudaGraphLaunch");
+  MSX_CUDA(cudaEventRecord(p->ev_out, p->work), "cudaEventRecord");
+  MSX_CUDA(cudaStreamWaitEvent(caller, p->ev_out, 0), "cudaStreamWaitEvent");
+  return MSX_OK;
+}
+
+int msx_plan_profile(msx_plan* p, const float* trans_dev, int num_slices, const float* psi_k_dev,
+                     const double* normalization_dev, const float* positions_dev, int num_probes, float kmax,
+                     double lambda, double slice_t, float k_band, int iters, float* ms_out, void* stream) {
+  if (!p || !ms_out) return fail(MSX_ERR_INVALID, "null plan or output");
+  if (iters <= 0 || num_slices <= 0 || num_probes <= 0 || !trans_dev || !psi_k_dev || !normalization_dev || !positions_dev)
+    return fail(MSX_ERR_INVALID, "profile needs slices, probes, inputs and iters > 0");
+  const int ny = p->ny, nx = p->nx;
+  const int gn = num_probes < p->group ? num_probes : p->group;
+  const size_t wave = (size_t)ny * nx;
+  cudaStream_t st = (cudaStream_t)stream;
+  cudaEvent_t ev[4];
+  for (auto& e : ev) MSX_CUDA(cudaEventCreate(&e), "cudaEventCreate");
+  MSX_CUDA(launch_ptab(ny, nx, kmax, lambda, slice_t, k_band, p->ptab, st), "propagator table");
+  ColArgs c{};
+  c.psi = p->psi; c.ptab = p->ptab; c.psik = reinterpret_cast<const float2*>(psi_k_dev); c.pos_yx = positions_dev;
+  c.tw = p->tw_col; c.norm = normalization_dev; c.cbed = nullptr; c.G = gn; c.Nx = nx; c.kmax = kmax;
+  c.x_begin = 0; c.ncols = nx; c.y0 = 0; c.crop_y = 0;
+  MSX_CUDA(p->col_ops->col(COL_INIT, c, st), "probe formation pass");
+  float row_ms = 0, col_ms = 0;
+  const float2* trans = reinterpret_cast<const float2*>(trans_dev);
+  for (int i = 0; i < iters; ++i) {
+    const int s = i % num_slices;
+    MSX_CUDA(cudaEventRecord(ev[0], st), "cudaEventRecord");
+    MSX_CUDA(p->row_ops->row(p->psi, trans + (size_t)s * wave, p->tw_row, gn, ny, st), "row pass");
+    MSX_CUDA(cudaEventRecord(ev[1], st), "cudaEventRecord");
+    MSX_CUDA(p->col_ops->col(COL_MID, c, st), "column pass");
+    MSX_CUDA(cudaEventRecord(ev[2], st), "cudaEventRecord");
+    MSX_CUDA(cudaEventSynchronize(ev[2]), "cudaEventSynchronize");
+    float a = 0, b = 0;
+    MSX_CUDA(cudaEventElapsedTime(&a, ev[0], ev[1]), "cudaEventElapsedTime");
+    MSX_CUDA(cudaEventElapsedTime(&b, ev[1], ev[2]), "cudaEventElapsedTime");
+    row_ms += a;
+    col_ms += b;
+  }
+  for (auto& e : ev) cudaEventDestroy(e);
+  ms_out[0] = row_ms / iters;
+  ms_out[1] = col_ms / iters;
+  ms_out[2] = (float)gn;
+  return MSX_OK;
+}
+
+}  // extern "C"

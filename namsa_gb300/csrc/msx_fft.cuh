@@ -1,0 +1,348 @@
+// Register/shared-memory FFT building blocks for the multislice passes.
+//
+// A "line" is one row or one column of a wave (length N).  T threads share a
+// line and each holds E = N/T complex values; thread t always holds the
+// elements with index t + T*m (m = 0..E-1), in natural order.  A line
+// transform is a sequence of Stockham stages (radices R1*R2*...*Rs = N, each
+// Ri dividing E).  Stage i performs E/Ri radix-Ri butterflies per thread in
+// registers; between stages the values are exchanged through shared memory.
+// Because the Stockham output of the last stage lands in exactly the slots the
+// first stage reads, a transform with s stages costs s-1 exchanges and no
+// bit-reversal pass, and a forward transform can follow an inverse one (or a
+// point-wise multiply) directly in registers.
+//
+// Twiddles inside a butterfly are compile-time constants (cos/sin of 2*pi*m/R
+// evaluated by constexpr Taylor series after exact octant reduction); the
+// inter-stage twiddles W_{Ns*R}^{k*r} come from a per-plan table computed in
+// double precision on the host and staged into shared memory.
+#pragma once
+#include <cuda_runtime.h>
+#include <utility>
+
+namespace msx {
+
+// ----------------------------------------------------------------- complex helpers
+__host__ __device__ __forceinline__ float2 cadd(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
+__host__ __device__ __forceinline__ float2 csub(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
+__host__ __device__ __forceinline__ float2 cmul(float2 a, float2 b) {
+  return make_float2(fmaf(a.x, b.x, -a.y * b.y), fmaf(a.x, b.y, a.y * b.x));
+}
+// a * conj(b)
+__host__ __device__ __forceinline__ float2 cmulc(float2 a, float2 b) {
+  return make_float2(fmaf(a.x, b.x, a.y * b.y), fmaf(a.y, b.x, -a.x * b.y));
+}
+__host__ __device__ __forceinline__ float2 cscale(float2 a, float s) { return make_float2(a.x * s, a.y * s); }
+
+// ----------------------------------------------------------------- constexpr trig
+// sin and cos of x for |x| <= pi/4 by Taylor series (terms to x^25: error far
+// below double rounding).
+__host__ __device__ constexpr double ce_sin_small(double x) {
+  double x2 = x * x, term = x, sum = x;
+  for (int n = 1; n < 13; ++n) { term *= -x2 / double((2 * n) * (2 * n + 1)); sum += term; }
+  return sum;
+}
+__host__ __device__ constexpr double ce_cos_small(double x) {
+  double x2 = x * x, term = 1.0, sum = 1.0;
+  for (int n = 1; n < 13; ++n) { term *= -x2 / double((2 * n - 1) * (2 * n)); sum += term; }
+  return sum;
+}
+constexpr double kHalfPi = 1.57079632679489661923132169163975144;
+// cos(2*pi*m/R) (want_sin = false) or sin(2*pi*m/R) (want_sin = true).
+// The angle is split exactly into a quadrant and a remainder in [0, pi/4].
+__host__ __device__ constexpr double ce_trig2pi(long m, long R, bool want_sin) {
+  long a = ((m % R) + R) % R;
+  long q = (4 * a) / R;            // quadrant 0..3
+  long rem = 4 * a - q * R;        // angle within quadrant = (pi/2)*rem/R
+  double c = 0, s = 0;
+  if (2 * rem <= R) {
+    double phi = kHalfPi * double(rem) / double(R);
+    c = ce_cos_small(phi); s = ce_sin_small(phi);
+  } else {
+    double psi = kHalfPi * double(R - rem) / double(R);
+    c = ce_sin_small(psi); s = ce_cos_small(psi);
+  }
+  double cq = c, sq = s;
+  if (q == 1) { cq = -s; sq = c; }
+  else if (q == 2) { cq = -c; sq = -s; }
+  else if (q == 3) { cq = s; sq = -c; }
+  return want_sin ? sq : cq;
+}
+
+// v * exp(sign * 2*pi*i * M / R), sign = -1 forward, +1 inverse, M a compile-time constant.
+template <int R, int M, bool INV>
+__host__ __device__ __forceinline__ float2 twc(float2 v) {
+  constexpr int m = ((M % R) + R) % R;
+  if constexpr (m == 0) {
+    return v;
+  } else if constexpr (2 * m == R) {
+    return make_float2(-v.x, -v.y);
+  } else if constexpr (4 * m == R) {           // fwd: -i   inv: +i
+    return INV ? make_float2(-v.y, v.x) : make_float2(v.y, -v.x);
+  } else if constexpr (4 * m == 3 * R) {       // fwd: +i   inv: -i
+    return INV ? make_float2(v.y, -v.x) : make_float2(-v.y, v.x);
+  } else if constexpr ((8 * m) % R == 0) {     // odd multiples of pi/4
+    constexpr float h = 0.70710678118654752440f;
+    constexpr int o = (8 * m) / R;             // 1, 3, 5, 7
+    // e^{-i pi o/4} (fwd) = (cx + i sx)/sqrt2 with the signs below
+    constexpr float cx = (o == 1 || o == 7) ? 1.f : -1.f;
+    constexpr float sxf = (o == 1 || o == 3) ? -1.f : 1.f;  // sign of sin for forward
+    constexpr float sx = INV ? -sxf : sxf;
+    // (a + ib)(cx + i sx) = (a cx - b sx) + i (a sx + b cx)
+    return make_float2(h * (cx * v.x - sx * v.y), h * (sx * v.x + cx * v.y));
+  } else {
+    constexpr float c = (float)ce_trig2pi(m, R, false);
+    constexpr float s = (INV ? 1.f : -1.f) * (float)ce_trig2pi(m, R, true);
+    return make_float2(fmaf(v.x, c, -v.y * s), fmaf(v.x, s, v.y * c));
+  }
+}
+
+// ----------------------------------------------------------------- register DFT codelets
+template <int R, bool INV> struct Dft;
+
+template <bool INV> struct Dft<1, INV> {
+  static __host__ __device__ __forceinline__ void run(float2 (&)[1]) {}
+};
+
+template <bool INV> struct Dft<2, INV> {
+  static __host__ __device__ __forceinline__ void run(float2 (&v)[2]) {
+    float2 a = v[0], b = v[1];
+    v[0] = cadd(a, b);
+    v[1] = csub(a, b);
+  }
+};
+
+template <bool INV> struct Dft<3, INV> {
+  static __host__ __device__ __forceinline__ void run(float2 (&v)[3]) {
+    constexpr float s3 = 0.86602540378443864676f;  // sin(2 pi / 3)
+    float2 t1 = cadd(v[1], v[2]);
+    float2 t2 = make_float2(fmaf(-0.5f, t1.x, v[0].x), fmaf(-0.5f, t1.y, v[0].y));
+    float2 h = cscale(csub(v[1], v[2]), s3);
+    v[0] = cadd(v[0], t1);
+    // forward: X1 = t2 - i h, X2 = t2 + i h
+    float2 m1 = make_float2(t2.x + h.y, t2.y - h.x);
+    float2 m2 = make_float2(t2.x - h.y, t2.y + h.x);
+    v[1] = INV ? m2 : m1;
+    v[2] = INV ? m1 : m2;
+  }
+};
+
+template <bool INV> struct Dft<4, INV> {
+  static __host__ __device__ __forceinline__ void run(float2 (&v)[4]) {
+    float2 a = cadd(v[0], v[2]), b = csub(v[0], v[2]);
+    float2 c = cadd(v[1], v[3]), d = csub(v[1], v[3]);
+    // -i d = (d.y, -d.x); +i d = (-d.y, d.x)
+    float2 jd = INV ? make_float2(-d.y, d.x) : make_float2(d.y, -d.x);
+    v[0] = cadd(a, c);
+    v[2] = csub(a, c);
+    v[1] = cadd(b, jd);
+    v[3] = csub(b, jd);
+  }
+};
+
+// Composite DFT of size A*B by one Cooley-Tukey step in registers:
+// X[ka + A*kb] = sum_b W_B^{b kb} W_{AB}^{b ka} sum_a x[b + B a] W_A^{a ka}.
+template <int A, int B, bool INV, int b, int... ka>
+__host__ __device__ __forceinline__ void ct_twiddle(float2 (&u)[A], float2 (&tmp)[A * B], std::integer_sequence<int, ka...>) {
+  ((tmp[b + B * ka] = twc<A * B, b * ka, INV>(u[ka])), ...);
+}
+template <int A, int B, bool INV, int b>
+__host__ __device__ __forceinline__ void ct_first(float2 (&v)[A * B], float2 (&tmp)[A * B]) {
+  float2 u[A];
+#pragma unroll
+  for (int a = 0; a < A; ++a) u[a] = v[b + B * a];
+  Dft<A, INV>::run(u);
+  ct_twiddle<A, B, INV, b>(u, tmp, std::make_integer_sequence<int, A>{});
+}
+template <int A, int B, bool INV, int... bs>
+__host__ __device__ __forceinline__ void ct_first_all(float2 (&v)[A * B], float2 (&tmp)[A * B], std::integer_sequence<int, bs...>) {
+  (ct_first<A, B, INV, bs>(v, tmp), ...);
+}
+template <int A, int B, bool INV>
+__host__ __device__ __forceinline__ void dft_ct(float2 (&v)[A * B]) {
+  float2 tmp[A * B];
+  ct_first_all<A, B, INV>(v, tmp, std::make_integer_sequence<int, B>{});
+#pragma unroll
+  for (int ka = 0; ka < A; ++ka) {
+    float2 w[B];
+#pragma unroll
+    for (int b = 0; b < B; ++b) w[b] = tmp[b + B * ka];
+    Dft<B, INV>::run(w);
+#pragma unroll
+    for (int kb = 0; kb < B; ++kb) v[ka + A * kb] = w[kb];
+  }
+}
+
+template <bool INV> struct Dft<8, INV> {
+  static __host__ __device__ __forceinline__ void run(float2 (&v)[8]) { dft_ct<2, 4, INV>(v); }
+};
+template <bool INV> struct Dft<6, INV> {
+  static __host__ __device__ __forceinline__ void run(float2 (&v)[6]) { dft_ct<2, 3, INV>(v); }
+};
+template <bool INV> struct Dft<12, INV> {
+  static __host__ __device__ __forceinline__ void run(float2 (&v)[12]) { dft_ct<4, 3, INV>(v); }
+};
+template <bool INV> struct Dft<16, INV> {
+  static __host__ __device__ __forceinline__ void run(float2 (&v)[16]) { dft_ct<4, 4, INV>(v); }
+};
+template <bool INV> struct Dft<24, INV> {
+  static __host__ __device__ __forceinline__ void run(float2 (&v)[24]) { dft_ct<8, 3, INV>(v); }
+};
+template <bool INV> struct Dft<32, INV> {
+  static __host__ __device__ __forceinline__ void run(float2 (&v)[32]) { dft_ct<4, 8, INV>(v); }
+};
+
+// ----------------------------------------------------------------- shared-memory indexers
+// Row lines: each line owns a private buffer; one float2 of padding every 32
+// keeps the stride-32 writes of a radix-32 stage free of bank conflicts.
+struct PaddedLine {
+  float2* base;
+  __host__ __device__ __forceinline__ float2& operator[](int i) const { return base[i + (i >> 5)]; }
+  static constexpr int words(int n) { return n + n / 32; }
+};
+// Column lines: C columns interleaved element by element (address i*C + c), so
+// a warp whose lanes are consecutive columns touches consecutive words.
+template <int C>
+struct InterleavedLine {
+  float2* base;  // already offset by the column
+  __host__ __device__ __forceinline__ float2& operator[](int i) const { return base[i * C]; }
+};
+
+template <bool CTA>
+__device__ __forceinline__ void line_sync() {
+  if constexpr (CTA) __syncthreads();
+  else __syncwarp();
+}
+
+// ----------------------------------------------------------------- Stockham line transform
+// Twiddle table layout for a radix list (R1, ..., Rs): stage i (i >= 2) with
+// Ns = R1*...*R(i-1) stores W_{Ns Ri}^{k r} at offset_i + (r-1)*Ns + k for
+// r = 1..Ri-1, k = 0..Ns-1 (forward sign; the inverse uses the conjugate).
+template <int... Rs> struct Radices;
+
+template <int N, int T, class Rad> struct LineFFT;
+
+template <int N, int T, int... Rs>
+struct LineFFT<N, T, Radices<Rs...>> {
+  static constexpr int E = N / T;
+  static_assert(N % T == 0, "threads must divide the line");
+  static constexpr int kStages = sizeof...(Rs);
+  static_assert((Rs * ...) == N, "radices must multiply to the line length");
+
+  static constexpr int tw_words() {
+    int ns = 1, total = 0;
+    int rs[] = {Rs...};
+    for (int i = 0; i < kStages; ++i) { if (i > 0) total += (rs[i] - 1) * ns; ns *= rs[i]; }
+    return total;
+  }
+
+  // Radix-R butterflies of one Stockham stage for thread t: reads its slots of
+  // v, writes the butterfly outputs (slot order q + r*Q) to out.
+  template <int R, int Ns, int TwOff, bool INV>
+  static __host__ __device__ __forceinline__ void butterflies(const float2 (&v)[E], float2 (&out)[E],
+                                                              const float2* __restrict__ tw, int t) {
+    static_assert(E % R == 0, "radix must divide the elements per thread");
+    constexpr int Q = E / R;
+#pragma unroll
+    for (int q = 0; q < Q; ++q) {
+      float2 u[R];
+#pragma unroll
+      for (int r = 0; r < R; ++r) u[r] = v[q + r * Q];
+      if constexpr (Ns > 1) {
+        const int k = (t + T * q) % Ns;
+#pragma unroll
+        for (int r = 1; r < R; ++r) {
+          const float2 w = tw[TwOff + (r - 1) * Ns + k];
+          u[r] = INV ? cmulc(u[r], w) : cmul(u[r], w);
+        }
+      }
+      Dft<R, INV>::run(u);
+#pragma unroll
+      for (int r = 0; r < R; ++r) out[q + r * Q] = u[r];
+    }
+  }
+  // Stockham destinations of the butterfly outputs of thread t.
+  template <int R, int Ns, class Buf>
+  static __host__ __device__ __forceinline__ void scatter(const float2 (&out)[E], const Buf& buf, int t) {
+    constexpr int Q = E / R;
+#pragma unroll
+    for (int q = 0; q < Q; ++q) {
+      const int j = t + T * q;
+      const int idxD = (j / Ns) * Ns * R + (j % Ns);
+#pragma unroll
+      for (int r = 0; r < R; ++r) buf[idxD + r * Ns] = out[q + r * Q];
+    }
+  }
+  template <class Buf>
+  static __host__ __device__ __forceinline__ void gather(float2 (&v)[E], const Buf& buf, int t) {
+#pragma unroll
+    for (int m = 0; m < E; ++m) v[m] = buf[t + T * m];
+  }
+
+  template <bool INV, bool CTA, int Ns, int TwOff, class Buf, int R0, int... Rest>
+  static __device__ __forceinline__ void stages(float2 (&v)[E], const Buf& buf, const float2* tw, int t) {
+    float2 out[E];
+    butterflies<R0, Ns, TwOff, INV>(v, out, tw, t);
+    if constexpr (sizeof...(Rest) == 0) {
+#pragma unroll
+      for (int m = 0; m < E; ++m) v[m] = out[m];
+    } else {
+      line_sync<CTA>();   // previous readers of buf are done
+      scatter<R0, Ns>(out, buf, t);
+      line_sync<CTA>();
+      gather(v, buf, t);
+      constexpr int nextOff = (Ns > 1) ? TwOff + (R0 - 1) * Ns : TwOff;
+      stages<INV, CTA, Ns * R0, nextOff, Buf, Rest...>(v, buf, tw, t);
+    }
+  }
+
+  // In-place line transform of the E values held by thread t (unnormalised).
+  // All T threads of the line must call it together.
+  template <bool INV, bool CTA, class Buf>
+  static __device__ __forceinline__ void run(float2 (&v)[E], const Buf& buf, const float2* tw, int t) {
+    stages<INV, CTA, 1, 0, Buf, Rs...>(v, buf, tw, t);
+  }
+
+  // Host emulation of run() on a whole line (data[N] in natural order), used
+  // by the host-side unit test of the index arithmetic and the codelets.
+  template <bool INV, int Ns, int TwOff, int R0, int... Rest>
+  static void host_stages(float2 (*v)[E], float2* scratch, const float2* tw) {
+    float2 out[T][E];
+    for (int t = 0; t < T; ++t) butterflies<R0, Ns, TwOff, INV>(v[t], out[t], tw, t);
+    if constexpr (sizeof...(Rest) == 0) {
+      for (int t = 0; t < T; ++t) for (int m = 0; m < E; ++m) v[t][m] = out[t][m];
+    } else {
+      PaddedLine buf{scratch};
+      for (int t = 0; t < T; ++t) scatter<R0, Ns>(out[t], buf, t);
+      for (int t = 0; t < T; ++t) gather(v[t], buf, t);
+      constexpr int nextOff = (Ns > 1) ? TwOff + (R0 - 1) * Ns : TwOff;
+      host_stages<INV, Ns * R0, nextOff, Rest...>(v, scratch, tw);
+    }
+  }
+  template <bool INV>
+  static void host_run(float2* data, const float2* tw) {
+    static float2 v[T][E];
+    static float2 scratch[PaddedLine::words(N)];
+    for (int t = 0; t < T; ++t) for (int m = 0; m < E; ++m) v[t][m] = data[t + T * m];
+    host_stages<INV, 1, 0, Rs...>(v, scratch, tw);
+    for (int t = 0; t < T; ++t) for (int m = 0; m < E; ++m) data[t + T * m] = v[t][m];
+  }
+  // Inter-stage twiddle table in the layout documented above (forward sign).
+  static void host_twiddles(float2* tw) {
+    int rs[] = {Rs...};
+    int ns = 1, off = 0;
+    for (int i = 0; i < kStages; ++i) {
+      if (i > 0) {
+        for (int r = 1; r < rs[i]; ++r)
+          for (int k = 0; k < ns; ++k) {
+            long num = (long)k * r, den = (long)ns * rs[i];
+            tw[off + (r - 1) * ns + k] = make_float2((float)ce_trig2pi(num, den, false),
+                                                     -(float)ce_trig2pi(num, den, true));
+          }
+        off += (rs[i] - 1) * ns;
+      }
+      ns *= rs[i];
+    }
+  }
+};
+
+}  // namespace msx

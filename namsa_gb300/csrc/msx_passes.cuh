@@ -1,0 +1,241 @@
+// Multislice passes over a group of G waves resident in the plan workspace.
+//
+// Between passes a wave is stored "mixed": y in real space, x in reciprocal
+// space, both in natural order, complex64, (G, Ny, Nx) row-major.  One slice of
+// the reference's loop (namsa/msa.py:971-981:  psi <- ifft2(P * fft2(psi * t_i / N)))
+// becomes two passes:
+//
+//   row pass  (per row):    inverse FFT_x -> * t_i -> forward FFT_x
+//   col pass  (per column): forward FFT_y -> * P/N -> inverse FFT_y
+//
+// The probe formation (msa.py:959-964: ramp, inverse FFT, fftshift) is one
+// column pass that builds psi_k * ramp * (-1)^(kx+ky) (the sign realises the
+// fftshift of an even grid) and applies the inverse FFT_y; the first row pass
+// then finishes the inverse transform.  The final column pass applies P/N
+// after the forward FFT_y and writes |psi|^2 * N / normalisation for the
+// crop window: the reference's closing ifft2 -> /N -> fft2 -> *sqrt(N)
+// (msa.py:981-989) is the identity times N, so it is folded into that scale.
+#pragma once
+#include "msx_fft.cuh"
+#include <cuda_runtime.h>
+
+namespace msx {
+
+// A schedule fixes the line transform (threads per line T, radices) and the
+// launch shape for one line length N.  Several schedules exist per N; the
+// autotuner in the host library picks one per grid size.  COL_C columns share
+// a column-pass CTA (COL_C * T = 256 threads); MINB is the minimum number of
+// resident CTAs requested from the register allocator.
+constexpr int kThreads = 256;
+constexpr int kWarps = kThreads / 32;
+
+template <int N_, int T_, int COL_C_, int MINB_, int... Rs>
+struct Sched {
+  static constexpr int N = N_;
+  static constexpr int T = T_;
+  static constexpr int C = COL_C_;
+  static constexpr int MINB = MINB_;
+  using FFT = LineFFT<N_, T_, Radices<Rs...>>;
+  static constexpr int E = FFT::E;
+  static constexpr int TW = FFT::tw_words();
+  static constexpr int TW_PAD = (TW + 31) / 32 * 32;
+  static constexpr int LPW = 32 / T;                 // row lines per warp
+  static constexpr int ROW_LINES = LPW * kWarps;     // row lines per CTA
+  static constexpr int ROW_LINE_WORDS = PaddedLine::words(N);
+  static constexpr size_t row_smem() { return sizeof(float2) * (TW_PAD + (size_t)ROW_LINES * ROW_LINE_WORDS); }
+  static constexpr size_t col_smem() { return sizeof(float2) * (TW_PAD + (size_t)C * N); }
+  static_assert(C * T == kThreads, "column CTA shape");
+  static_assert(T <= 32 && 32 % T == 0, "a row line must live inside one warp");
+};
+
+template <int TW>
+__device__ __forceinline__ void load_twiddles(float2* dst, const float2* __restrict__ src) {
+  for (int i = threadIdx.x; i < TW; i += blockDim.x) dst[i] = src[i];
+  __syncthreads();
+}
+
+// ---------------------------------------------------------------- row pass
+// Lines are ordered (y, p) with the wave index fastest so the waves of one CTA
+// share the transmission row.
+template <class S>
+__global__ void __launch_bounds__(kThreads, S::MINB)
+row_pass_kernel(float2* __restrict__ psi, const float2* __restrict__ trans, const float2* __restrict__ tw_g,
+                int G, int Ny) {
+  constexpr int NX = S::N;
+  extern __shared__ float2 smem[];
+  float2* tw = smem;
+  load_twiddles<S::TW>(tw, tw_g);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int lw = lane / S::T, t = lane % S::T;
+  const int total = G * Ny;
+  const int line = blockIdx.x * S::ROW_LINES + warp * S::LPW + lw;
+  const bool valid = line < total;
+  const int ln = valid ? line : total - 1;
+  const int y = ln / G, p = ln - y * G;
+  float2* row = psi + ((size_t)p * Ny + y) * NX;
+  float2 v[S::E];
+#pragma unroll
+  for (int m = 0; m < S::E; ++m) v[m] = row[t + S::T * m];
+  PaddedLine buf{smem + S::TW_PAD + (warp * S::LPW + lw) * S::ROW_LINE_WORDS};
+  S::FFT::template run<true, false>(v, buf, tw, t);
+  const float2* trow = trans + (size_t)y * NX;
+#pragma unroll
+  for (int m = 0; m < S::E; ++m) v[m] = cmul(v[m], __ldg(trow + t + S::T * m));
+  S::FFT::template run<false, false>(v, buf, tw, t);
+  if (valid) {
+#pragma unroll
+    for (int m = 0; m < S::E; ++m) row[t + S::T * m] = v[m];
+  }
+}
+
+// ---------------------------------------------------------------- column passes
+enum ColMode { COL_INIT = 0, COL_MID = 1, COL_FINAL = 2, COL_INIT_FINAL = 3 };
+
+struct ColArgs {
+  float2* psi;             // (G, Ny, Nx) group workspace
+  const float2* ptab;      // (Ny, Nx) propagator * mask / (Ny*Nx)
+  const float2* psik;      // (Ny, Nx) k-space probe (init)
+  const float* pos_yx;     // (G, 2) probe positions of the group, [y, x] Angstrom (init)
+  const float2* tw;        // twiddle table for the y lines
+  const double* norm;      // device normalisation sum |ifft2_u(psi_k)|^2 (final)
+  float* cbed;             // (G, crop_y, crop_x) output of the group (final)
+  int G, Nx;
+  int x_begin, ncols;      // columns handled: x_begin .. x_begin + ncols - 1
+  int y0, crop_y;          // output rows y0 .. y0 + crop_y - 1 (final)
+  float kmax;              // k-grid extent (float32 like the reference)
+};
+
+template <class S, int MODE>
+__global__ void __launch_bounds__(kThreads, S::MINB) col_pass_kernel(ColArgs a) {
+  constexpr int NY = S::N;
+  extern __shared__ float2 smem[];
+  float2* tw = smem;
+  load_twiddles<S::TW>(tw, a.tw);
+  const int p = blockIdx.x % a.G;
+  const int tile = blockIdx.x / a.G;
+  const int c = threadIdx.x % S::C, t = threadIdx.x / S::C;
+  const int xl = tile * S::C + c;
+  const bool valid = xl < a.ncols;
+  const int x = a.x_begin + (valid ? xl : a.ncols - 1);
+  const int Nx = a.Nx;
+  float2* __restrict__ col = a.psi + (size_t)p * NY * Nx + x;
+  const float2* __restrict__ pcol = a.ptab + x;
+  InterleavedLine<S::C> buf{smem + S::TW_PAD + c};
+  float2 v[S::E];
+
+  if constexpr (MODE == COL_INIT || MODE == COL_INIT_FINAL) {
+    // psi_k * exp(2 pi i (-kx x_p - ky y_p)) * (-1)^(kx_idx + ky_idx); k on the centred
+    // grid j*kmax/(N-1) - kmax/2 (probe_kernels.cu:11-16, 37-57, 239-253).  The phase
+    // is formed and reduced in double precision, then evaluated in float.
+    const double km = (double)a.kmax;
+    const double py = (double)a.pos_yx[2 * p], px = (double)a.pos_yx[2 * p + 1];
+    const double kx = (double)x * km / (double)(a.Nx - 1) - km * 0.5;
+    const double phx = -kx * px;
+#pragma unroll
+    for (int m = 0; m < S::E; ++m) {
+      const int ky_i = t + S::T * m;
+      const double ky = (double)ky_i * km / (double)(NY - 1) - km * 0.5;
+      double ph = fma(-ky, py, phx);
+      ph -= rint(ph);
+      float sn, cs;
+      sincospif(2.0f * (float)ph, &sn, &cs);
+      float2 val = cmul(__ldg(a.psik + ky_i * Nx + x), make_float2(cs, sn));
+      if ((x + ky_i) & 1) val = make_float2(-val.x, -val.y);
+      v[m] = val;
+    }
+  } else {
+#pragma unroll
+    for (int m = 0; m < S::E; ++m) v[m] = col[(t + S::T * m) * Nx];
+  }
+
+  if constexpr (MODE == COL_INIT) {
+    S::FFT::template run<true, true>(v, buf, tw, t);
+  } else if constexpr (MODE == COL_MID) {
+    S::FFT::template run<false, true>(v, buf, tw, t);
+#pragma unroll
+    for (int m = 0; m < S::E; ++m) v[m] = cmul(v[m], __ldg(pcol + (t + S::T * m) * Nx));
+    S::FFT::template run<true, true>(v, buf, tw, t);
+  } else if constexpr (MODE == COL_FINAL) {
+    S::FFT::template run<false, true>(v, buf, tw, t);
+#pragma unroll
+    for (int m = 0; m < S::E; ++m) v[m] = cmul(v[m], __ldg(pcol + (t + S::T * m) * Nx));
+  }
+  // COL_INIT_FINAL (no slices): fft2(ifft2_u(Y)) = N*Y, so v already holds Y.
+
+  if constexpr (MODE == COL_FINAL || MODE == COL_INIT_FINAL) {
+    const double ntot = (double)NY * (double)a.Nx;
+    // COL_FINAL: I = N |P/N * fft2_u(psi t)|^2 / norm ; COL_INIT_FINAL: I = N |Y|^2 / norm
+    const float scale = (float)(ntot / *a.norm);
+    if (valid) {
+      float* out = a.cbed + (size_t)p * a.crop_y * a.ncols + xl;
+#pragma unroll
+      for (int m = 0; m < S::E; ++m) {
+        const int ky = t + S::T * m - a.y0;
+        if (ky >= 0 && ky < a.crop_y) out[(size_t)ky * a.ncols] = fmaf(v[m].x, v[m].x, v[m].y * v[m].y) * scale;
+      }
+    }
+  } else {
+    if (valid) {
+#pragma unroll
+      for (int m = 0; m < S::E; ++m) col[(t + S::T * m) * Nx] = v[m];
+    }
+  }
+}
+
+// ---------------------------------------------------------------- launchers
+// Type-erased entry points of one schedule, collected by the host library.
+struct SchedOps {
+  int n;                      // line length
+  const char* name;
+  int tw_words;
+  void (*host_twiddles)(float2*);
+  cudaError_t (*configure)();
+  cudaError_t (*row)(float2* psi, const float2* trans, const float2* tw, int G, int Ny, cudaStream_t st);
+  cudaError_t (*col)(int mode, const ColArgs& a, cudaStream_t st);
+};
+
+template <class S> struct SchedImpl {
+  static void host_twiddles(float2* tw) { S::FFT::host_twiddles(tw); }
+  static cudaError_t configure() {
+    cudaError_t e = cudaFuncSetAttribute(row_pass_kernel<S>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)S::row_smem());
+    const int cs = (int)S::col_smem();
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(col_pass_kernel<S, COL_INIT>, cudaFuncAttributeMaxDynamicSharedMemorySize, cs);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(col_pass_kernel<S, COL_MID>, cudaFuncAttributeMaxDynamicSharedMemorySize, cs);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(col_pass_kernel<S, COL_FINAL>, cudaFuncAttributeMaxDynamicSharedMemorySize, cs);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(col_pass_kernel<S, COL_INIT_FINAL>, cudaFuncAttributeMaxDynamicSharedMemorySize, cs);
+    return e;
+  }
+  static cudaError_t row(float2* psi, const float2* trans, const float2* tw, int G, int Ny, cudaStream_t st) {
+    const int lines = G * Ny;
+    const int blocks = (lines + S::ROW_LINES - 1) / S::ROW_LINES;
+    row_pass_kernel<S><<<blocks, kThreads, S::row_smem(), st>>>(psi, trans, tw, G, Ny);
+    return cudaGetLastError();
+  }
+  static cudaError_t col(int mode, const ColArgs& a, cudaStream_t st) {
+    const int tiles = (a.ncols + S::C - 1) / S::C;
+    const dim3 grid(tiles * a.G);
+    const size_t sm = S::col_smem();
+    switch (mode) {
+      case COL_INIT: col_pass_kernel<S, COL_INIT><<<grid, kThreads, sm, st>>>(a); break;
+      case COL_MID: col_pass_kernel<S, COL_MID><<<grid, kThreads, sm, st>>>(a); break;
+      case COL_FINAL: col_pass_kernel<S, COL_FINAL><<<grid, kThreads, sm, st>>>(a); break;
+      default: col_pass_kernel<S, COL_INIT_FINAL><<<grid, kThreads, sm, st>>>(a); break;
+    }
+    return cudaGetLastError();
+  }
+  static SchedOps ops(const char* name) {
+    return SchedOps{S::N, name, S::TW, &host_twiddles, &configure, &row, &col};
+  }
+};
+
+// Schedules compiled for each line length (one translation unit per length).
+int schedules_64(const SchedOps** out);
+int schedules_128(const SchedOps** out);
+int schedules_256(const SchedOps** out);
+int schedules_384(const SchedOps** out);
+int schedules_512(const SchedOps** out);
+int schedules_768(const SchedOps** out);
+int schedules_1024(const SchedOps** out);
+
+}  // namespace msx

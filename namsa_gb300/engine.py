@@ -1,0 +1,181 @@
+"""Torch-tensor wrappers over the libmsx C ABI.
+
+Every function takes and returns CUDA tensors; the work is queued on the
+current torch stream.  Shapes and dtypes are checked here, argument ranges
+in the library.  There is no CPU path.
+"""
+from __future__ import annotations
+
+import ctypes
+
+import torch
+
+from . import _lib
+
+_vp = ctypes.c_void_p
+
+
+def _stream():
+    return _vp(torch.cuda.current_stream().cuda_stream)
+
+
+def _ptr(t):
+    return _vp(0) if t is None else _vp(t.data_ptr())
+
+
+def _need(t, dtype, name, ndim=None):
+    if not isinstance(t, torch.Tensor):
+        raise TypeError(f'{name} must be a torch tensor')
+    if not t.is_cuda:
+        raise ValueError(f'{name} must be a CUDA tensor')
+    if t.dtype != dtype:
+        raise TypeError(f'{name} must be {dtype}, got {t.dtype}')
+    if not t.is_contiguous():
+        raise ValueError(f'{name} must be contiguous')
+    if ndim is not None and t.dim() != ndim:
+        raise ValueError(f'{name} must have {ndim} dimensions, got {tuple(t.shape)}')
+    return t
+
+
+def lib():
+    return _lib.load()
+
+
+def supported_size(n):
+    return bool(lib().msx_supported_size(int(n)))
+
+
+def schedules(n):
+    """Names of the compiled FFT schedules for line length n."""
+    out = []
+    buf = ctypes.create_string_buffer(64)
+    for i in range(lib().msx_num_schedules(int(n))):
+        _lib.check(lib().msx_schedule_name(int(n), i, buf, len(buf)))
+        out.append(buf.value.decode())
+    return out
+
+
+def atom_windows(coeff, n0, n1, oversample=2, potential_range=8.0):
+    """Kirkland projected-potential windows, (nspecies, n0/os, n1/os) float32.
+
+    ``coeff`` is (nspecies, 4, 3) float64 on the device (rows a, b, c, d)."""
+    _need(coeff, torch.float64, 'coeff', 3)
+    ns = coeff.shape[0]
+    out = torch.empty((ns, n0 // oversample, n1 // oversample), dtype=torch.float32, device=coeff.device)
+    _lib.check(lib().msx_atom_windows(_ptr(coeff), ns, int(n0), int(n1), int(oversample), float(potential_range),
+                                      _ptr(out), _stream()))
+    return out
+
+
+def build_transmission(sites, offsets, windows, ny, nx, sigma, want_potential=False):
+    """Transmission slices (S, ny, nx) complex64 and optionally V (S, ny, nx) float32.
+
+    ``sites``: (nsites, 4) int32 (species index, y pixel, x pixel, 0) grouped by slice;
+    ``offsets``: (S+1,) int32 slice boundaries into ``sites``."""
+    _need(sites, torch.int32, 'sites', 2)
+    _need(offsets, torch.int32, 'offsets', 1)
+    _need(windows, torch.float32, 'windows', 3)
+    if sites.shape[1] != 4:
+        raise ValueError('sites must have 4 columns')
+    S = offsets.shape[0] - 1
+    dev = windows.device
+    trans = torch.empty((S, ny, nx), dtype=torch.complex64, device=dev)
+    pot = torch.empty((S, ny, nx), dtype=torch.float32, device=dev) if want_potential else None
+    if S > 0:
+        if sites.shape[0] == 0:  # no atoms: keep a valid pointer for the kernel
+            sites = torch.zeros((1, 4), dtype=torch.int32, device=dev)
+        _lib.check(lib().msx_build_transmission(_ptr(sites), _ptr(offsets), S, _ptr(windows), windows.shape[1],
+                                                windows.shape[2], int(ny), int(nx), float(sigma), _ptr(trans),
+                                                _ptr(pot), _stream()))
+    return trans, pot
+
+
+def build_probe(ny, nx, kmax, lam, k_semi, c1, c3, c5, smooth, device=None):
+    """k-space probe (ny, nx) complex64, aperture (ny, nx) float32 and the
+    normalisation (1,) float64, all on the device."""
+    dev = torch.device('cuda', torch.cuda.current_device()) if device is None else device
+    psik = torch.empty((ny, nx), dtype=torch.complex64, device=dev)
+    ap = torch.empty((ny, nx), dtype=torch.float32, device=dev)
+    norm = torch.empty((1,), dtype=torch.float64, device=dev)
+    _lib.check(lib().msx_build_probe(int(ny), int(nx), float(kmax), float(lam), float(k_semi), float(c1), float(c3),
+                                     float(c5), int(bool(smooth)), _ptr(psik), _ptr(ap), _ptr(norm), _stream()))
+    return psik, ap, norm
+
+
+class Plan:
+    """A multislice plan: resident wave workspace, schedules and graph cache."""
+
+    def __init__(self, ny, nx, group=0):
+        self.ny, self.nx = int(ny), int(nx)
+        h = _vp()
+        _lib.check(lib().msx_plan_create(self.ny, self.nx, int(group), ctypes.byref(h)))
+        self._h = h
+
+    @property
+    def handle(self):
+        if self._h is None:
+            raise RuntimeError('plan is closed')
+        return self._h
+
+    def close(self):
+        if getattr(self, '_h', None) is not None:
+            lib().msx_plan_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_schedule(self, row=None, col=None, group=0):
+        r, c, _ = self.schedule
+        _lib.check(lib().msx_plan_set_schedule(self.handle, int(r if row is None else row),
+                                               int(c if col is None else col), int(group)))
+
+    @property
+    def schedule(self):
+        r, c, g = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+        _lib.check(lib().msx_plan_get_schedule(self.handle, ctypes.byref(r), ctypes.byref(c), ctypes.byref(g)))
+        return r.value, c.value, g.value
+
+    def set_graph(self, enable):
+        _lib.check(lib().msx_plan_set_graph(self.handle, int(bool(enable))))
+
+    def multislice(self, trans, psik, norm, positions, kmax, lam, slice_t, k_band, crop=None, out=None):
+        """CBED stack (P, crop_y, crop_x) float32 for positions (P, 2) [y, x] float32.
+
+        ``kmax`` and ``k_band`` are float32 values (the reference passes
+        ``float32(kmax)`` and ``float32(bandwidth * kmax)`` to its kernels)."""
+        _need(trans, torch.complex64, 'trans', 3)
+        _need(psik, torch.complex64, 'psi_k', 2)
+        _need(norm, torch.float64, 'normalization', 1)
+        _need(positions, torch.float32, 'positions', 2)
+        S, ny, nx = trans.shape
+        if (ny, nx) != (self.ny, self.nx) or tuple(psik.shape) != (ny, nx):
+            raise ValueError(f'grid mismatch: plan {self.ny}x{self.nx}, trans {tuple(trans.shape)}, psi_k {tuple(psik.shape)}')
+        if positions.shape[1] != 2:
+            raise ValueError('positions must be (P, 2) [y, x]')
+        cy, cx = (ny, nx) if crop is None else ((crop, crop) if isinstance(crop, int) else crop)
+        P = positions.shape[0]
+        if out is None:
+            out = torch.empty((P, cy, cx), dtype=torch.float32, device=trans.device)
+        else:
+            _need(out, torch.float32, 'out', 3)
+            if tuple(out.shape) != (P, cy, cx):
+                raise ValueError('out has the wrong shape')
+        _lib.check(lib().msx_multislice(self.handle, _ptr(trans), S, _ptr(psik), _ptr(norm), _ptr(positions), P,
+                                        float(kmax), float(lam), float(slice_t), float(k_band), _ptr(out),
+                                        int(cy), int(cx), _stream()))
+        return out
+
+    def profile(self, trans, psik, norm, positions, kmax, lam, slice_t, k_band, iters=20):
+        """Mean duration (ms) of one row pass and one column pass over the plan's
+        first group, timed with CUDA events on the current stream; also returns
+        the waves per launch."""
+        out = (ctypes.c_float * 3)()
+        S = trans.shape[0]
+        _lib.check(lib().msx_plan_profile(self.handle, _ptr(trans), S, _ptr(psik), _ptr(norm), _ptr(positions),
+                                          positions.shape[0], float(kmax), float(lam), float(slice_t), float(k_band),
+                                          int(iters), out, _stream()))
+        return float(out[0]), float(out[1]), int(out[2])

@@ -1,0 +1,116 @@
+"""Generate the golden fixtures in this folder from the reference's own CPU code.
+
+Run in a container where the reference checkout is available (the path is the
+first argument, default ``/root/reference``).  The reference package imports
+pycuda/skcuda/mpi4py/h5py/pymatgen at module load; none of these is used by
+the ``MSA`` CPU class, so they are replaced by empty stub modules, and the
+NumPy aliases removed in NumPy 2 (``np.int``, ``np.float``, ``np.bool``) are
+restored.  Nothing of the reference is modified.
+
+Fixtures written (all ``.npz``):
+
+* ``optics.npz``      -- wavelength and interaction parameter at five voltages
+                         (namsa/optics.py:4-12, 100-108) and Scherzer defocus.
+* ``si_small.npz``    -- Si 2x2x4 cells at 128^2, 100 keV, 20 mrad: the Kirkland
+                         window, the CPU potential slices, ``build_probe``
+                         outputs and exit waves of ``multislice`` at 3 positions.
+* ``si_config1.npz``  -- Si 4x4x20 cells at 256^2, 80 slices, 100 keV, 20 mrad,
+                         probe at the origin: window, slice checksums and exit wave.
+* ``positions.npz``   -- ``generate_probe_positions`` for both of its branches.
+"""
+import os
+import sys
+import types
+
+import numpy as np
+import scipy.integrate  # noqa: F401  (imported before the NumPy aliases are restored)
+import scipy.special  # noqa: F401
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(HERE, '..', '..'))
+from oracle.msa_oracle import si_supercell  # noqa: E402
+
+
+class _Stub(types.ModuleType):
+    def __getattr__(self, k):
+        if k.startswith('__'):
+            raise AttributeError(k)
+        return type(k, (), {})
+
+
+def import_reference(ref_root):
+    for name in ['pycuda', 'pycuda.driver', 'pycuda.gpuarray', 'pycuda.compiler', 'pycuda.tools', 'skcuda',
+                 'skcuda.fft', 'skcuda.cufft', 'h5py', 'mpi4py', 'pymatgen', 'pymatgen.core', 'pymatgen.io',
+                 'pymatgen.io.cif', 'pymatgen.analysis', 'pymatgen.analysis.diffraction',
+                 'pymatgen.analysis.diffraction.xrd', 'pymatgen.symmetry', 'pymatgen.symmetry.analyzer']:
+        sys.modules.setdefault(name, _Stub(name))
+    np.int = int
+    np.float = float
+    np.bool = bool
+    sys.path.insert(0, ref_root)
+    import namsa.msa as msa
+    import namsa.optics as optics
+    return msa, optics
+
+
+def main(ref_root='/root/reference'):
+    msa, optics = import_reference(ref_root)
+    volts = np.array([80e3, 100e3, 120e3, 200e3, 300e3])
+    np.savez_compressed(os.path.join(HERE, 'optics.npz'), volts=volts,
+                        lam=np.array([optics.voltage2Lambda(v) for v in volts]),
+                        sigma=np.array([optics.sigma_int(v) for v in volts]),
+                        scherzer_c1=np.array([optics.scherzer_params(optics.voltage2Lambda(v), 1e4)[0] for v in volts]))
+
+    pd = {'smooth_apert': True, 'apert_smooth': 50, 'spherical_phase': True,
+          'aberration_dict': {'C1': 20., 'C3': 1e4, 'C5': 0.}, 'scherzer': False}
+
+    # small Si case: 2x2x4 cells, 128^2
+    sc = si_supercell(2, 2, 4)
+    m = msa.MSA(100, 20e-3, sc, sampling=np.array([128, 128]), debye_waller=False)
+    m.calc_atomic_potentials()
+    t = 5.431 / 4
+    m.build_potential_slices(t)
+    pos = np.array([[0., 0.], [1.3, -0.7], [-2.1, 2.9]])
+    probe_x, probe_k, aperture = m.build_probe(pos[1], pd)
+    m.probe_positions = pos
+    m.num_probes = len(pos)
+    waves = m.multislice(probe_grid=True, save_probes=False, bandwidth=1 / 3)
+    np.savez_compressed(os.path.join(HERE, 'si_small.npz'), xyz=np.column_stack([sc['x'], sc['y'], sc['z']]),
+                        Z=sc['atomic_number'], sampling=np.array([128, 128]), energy=100., semi_angle=20e-3,
+                        slice_t=t, window=m.cached_pots[14], V=m.potential_slices, positions=pos,
+                        probe_x=probe_x, probe_k=probe_k, aperture=aperture, waves=waves,
+                        dims=m.dims, kmax=m.kmax, pix_size=m.pix_size, sigma=m.sigma)
+
+    # config 1: Si 4x4x20 cells, 256^2, 80 slices, probe at the origin
+    sc = si_supercell(4, 4, 20)
+    m = msa.MSA(100, 20e-3, sc, sampling=np.array([256, 256]), debye_waller=False)
+    m.calc_atomic_potentials()
+    m.build_potential_slices(t)
+    pd1 = {'smooth_apert': True, 'apert_smooth': 50, 'spherical_phase': True,
+           'aberration_dict': {'C1': 0., 'C3': 0., 'C5': 0.}, 'scherzer': False}
+    m.build_probe(np.array([0., 0.]), pd1)
+    wave = m.multislice(probe_pos=np.array([0., 0.]), probe_grid=False, save_probes=False)
+    V = m.potential_slices
+    np.savez_compressed(os.path.join(HERE, 'si_config1.npz'), sampling=np.array([256, 256]), energy=100.,
+                        semi_angle=20e-3, slice_t=t, window=m.cached_pots[14], V_sum=V.astype(np.float64).sum((1, 2)),
+                        V_rows=V[:, ::37, :].copy(), wave=wave, num_slices=V.shape[0],
+                        dims=m.dims, kmax=m.kmax, pix_size=m.pix_size, sigma=m.sigma)
+
+    # probe positions, both branches
+    res = {}
+    m2 = msa.MSA(200, 30e-3, si_supercell(8, 8, 2), sampling=np.array([512, 512]), debye_waller=False)
+    for name, kw in [('steps', dict(probe_step=np.array([0.5, 0.5]), probe_range=np.array([[0.25, 0.75], [0.25, 0.75]]))),
+                     ('steps2', dict(probe_step=np.array([1.0, 0.7]), probe_range=np.array([[0., 1.], [0.1, 0.6]]))),
+                     ('grid', dict(grid_steps=np.array([8, 8]))),
+                     ('grid2', dict(grid_steps=np.array([4, 6]), fraction=0.25, origin=np.array([0.1, 0.2])))]:
+        m2.generate_probe_positions(**kw)
+        res[name + '_pos'] = m2.probe_positions
+        res[name + '_steps'] = m2.grid_steps
+        res[name + '_range'] = m2.grid_range
+    res['dims'] = m2.dims
+    np.savez_compressed(os.path.join(HERE, 'positions.npz'), **res)
+    print('golden fixtures written to', HERE)
+
+
+if __name__ == '__main__':
+    main(*sys.argv[1:])

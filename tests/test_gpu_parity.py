@@ -1,0 +1,235 @@
+"""Parity of the CUDA engine (through the libmsx C ABI) with the oracle.
+
+Tolerances: integer/discrete results (summed potential V, masks) are compared
+bit for bit; floating results against the FP64 oracle with the relative L2
+bounds stated per test (the bar for the CBED metric is 1e-3 vs FP64; the
+FP32 engine is held to 1e-4 or tighter)."""
+import numpy as np
+import pytest
+import torch
+
+from namsa_gb300 import _lib, engine
+from namsa_gb300 import msa as M
+from oracle import msa_oracle as O
+
+pytestmark = pytest.mark.gpu
+DEV = 'cuda'
+KIRK = M.kirkland_table()
+
+
+def geom_of(ny, nx, kmax, lam):
+    g = O.Geometry.__new__(O.Geometry)
+    g.sampling = np.array([ny, nx])
+    g.kmax = kmax
+    g.lam = lam
+    return g
+
+
+def crystal_geom(sc, energy, semi, n):
+    xyz = np.column_stack([sc['x'], sc['y'], sc['z']]).astype(np.float32)
+    return O.Geometry(xyz, sc['atomic_number'], energy, semi, n)
+
+
+def engine_cbed(trans, psik, norm, pos, kmax, lam, slice_t, bandwidth, crop=None, group=0, sched=(0, 0), graph=True):
+    ny, nx = psik.shape
+    plan = engine.Plan(ny, nx, group)
+    plan.set_schedule(sched[0], sched[1])
+    plan.set_graph(graph)
+    out = plan.multislice(torch.from_numpy(np.ascontiguousarray(trans.astype(np.complex64))).to(DEV),
+                          torch.from_numpy(np.ascontiguousarray(psik.astype(np.complex64))).to(DEV),
+                          torch.tensor([norm], dtype=torch.float64, device=DEV),
+                          torch.from_numpy(np.ascontiguousarray(pos.astype(np.float32))).to(DEV),
+                          np.float32(kmax), lam, slice_t, np.float32(bandwidth * kmax), crop=crop)
+    res = out.cpu().numpy()
+    plan.close()
+    return res
+
+
+def random_case(ny, nx, S, P, seed, lam=0.025, slice_t=1.5):
+    rng = np.random.default_rng(seed)
+    kmax = float(min(ny, nx)) / 20.0
+    g = geom_of(ny, nx, kmax, lam)
+    g.semi_ang = 0.025
+    pd = {'smooth_apert': True, 'spherical_phase': True, 'aberration_dict': {'C1': 15., 'C3': 1e4, 'C5': 0.},
+          'scherzer': False}
+    psik, _, norm = O.probe_gpu(g, pd)
+    psik = psik.astype(np.complex64)
+    norm = float(np.sum(np.abs(np.fft.ifft2(psik.astype(np.complex128)) * ny * nx) ** 2))
+    V = rng.standard_normal((S, ny, nx))
+    trans = np.exp(0.3j * V).astype(np.complex64)
+    pos = rng.uniform(-8, 8, size=(P, 2)).astype(np.float32)
+    return g, trans, psik, norm, pos, kmax, lam, slice_t
+
+
+def oracle_cbed(g, trans, psik, norm, pos, slice_t, bandwidth, crop=None):
+    P, _ = O.propagator_gpu(g, slice_t, bandwidth)
+    return O.multislice_gpu(trans.astype(np.complex128), psik.astype(np.complex128), P, pos, norm, g, crop=crop)
+
+
+# ----------------------------------------------------------------------------- setup kernels
+@pytest.mark.parametrize('zs,pix', [((14,), (0.08486, 0.08486)), ((8, 22, 38, 79), (0.061, 0.0732))])
+def test_atom_windows(zs, pix):
+    n0, n1 = M.window_grid(np.array(pix))
+    coeff = torch.from_numpy(np.ascontiguousarray(KIRK[np.array(zs) - 1])).to(DEV)
+    w = engine.atom_windows(coeff, n0, n1).cpu().numpy()
+    for i, z in enumerate(zs):
+        ref = O.atom_potential(KIRK[z - 1], np.array(pix))
+        assert w[i].shape == ref.shape
+        assert np.abs(w[i] - ref).max() <= 4e-7 * np.abs(ref).max()
+
+
+@pytest.mark.parametrize('case', ['si_small', 'srtio3_rect'])
+def test_transmission_bit_exact(case):
+    if case == 'si_small':
+        sc, energy, n, t = O.si_supercell(2, 2, 4), 100., (128, 128), 5.431 / 4
+    else:
+        sc, energy, n, t = O.srtio3_supercell(4, 3, 3), 300., (256, 384), 3.905 / 2
+    geom = crystal_geom(sc, energy, 20e-3, n)
+    _, win = O.atom_windows(geom, KIRK)
+    S = geom.num_slices(t)
+    sites, offs = M.slice_sites(geom.xyz, geom.Z, geom.pix_size, t, S)
+    trans, V = engine.build_transmission(torch.from_numpy(sites).to(DEV), torch.from_numpy(offs).to(DEV),
+                                         torch.from_numpy(win).to(DEV), n[0], n[1], np.float32(geom.sigma),
+                                         want_potential=True)
+    Vref = O.potential_slices_gpu(O.slice_sites_gpu(geom, t), win, n, mode='f32')
+    np.testing.assert_array_equal(V.cpu().numpy(), Vref)
+    tref = O.transmission(Vref, geom.sigma, mode='f32')
+    assert np.abs(trans.cpu().numpy() - tref).max() < 5e-7
+
+
+@pytest.mark.parametrize('smooth,scherzer', [(True, False), (False, True)])
+def test_probe(smooth, scherzer):
+    sc = O.si_supercell(8, 8, 1)
+    geom = crystal_geom(sc, 200., 30e-3, (512, 512))
+    pd = {'smooth_apert': smooth, 'spherical_phase': True, 'aberration_dict': {'C1': 10., 'C3': 1e4, 'C5': 1e5},
+          'scherzer': scherzer}
+    psik_ref, ap_ref, norm_ref = O.probe_gpu(geom, pd)
+    C1 = O.scherzer_defocus(geom.lam, 1e4) if scherzer else 10.
+    psik, ap, norm = engine.build_probe(512, 512, np.float32(geom.kmax), geom.lam, np.float32(geom.semi_ang / geom.lam),
+                                        C1, 1e4, 1e5, smooth)
+    assert np.abs(psik.cpu().numpy() - psik_ref).max() < 1e-6
+    assert np.abs(ap.cpu().numpy() - ap_ref).max() < 1e-6
+    if not smooth:
+        np.testing.assert_array_equal(ap.cpu().numpy(), ap_ref)
+    assert abs(norm.item() - norm_ref) < 1e-6 * norm_ref
+
+
+# ----------------------------------------------------------------------------- multislice
+@pytest.mark.parametrize('n', [64, 128, 256, 384, 512, 768, 1024])
+def test_multislice_every_size_and_schedule(n):
+    g, trans, psik, norm, pos, kmax, lam, st = random_case(n, n, S=3, P=3, seed=n)
+    ref = oracle_cbed(g, trans, psik, norm, pos, st, 1 / 3)
+    for k in range(len(engine.schedules(n))):
+        got = engine_cbed(trans, psik, norm, pos, kmax, lam, st, 1 / 3, sched=(k, k))
+        err = O.rel_l2(got, ref)
+        assert err.max() < 2e-5, (n, k, err)
+
+
+@pytest.mark.parametrize('ny,nx', [(256, 512), (384, 768), (128, 64)])
+def test_multislice_rectangular(ny, nx):
+    g, trans, psik, norm, pos, kmax, lam, st = random_case(ny, nx, S=4, P=2, seed=ny + nx)
+    ref = oracle_cbed(g, trans, psik, norm, pos, st, 1 / 3)
+    got = engine_cbed(trans, psik, norm, pos, kmax, lam, st, 1 / 3)
+    assert O.rel_l2(got, ref).max() < 2e-5
+
+
+def test_groups_crop_graph_determinism():
+    g, trans, psik, norm, pos, kmax, lam, st = random_case(128, 128, S=5, P=7, seed=3)
+    ref = oracle_cbed(g, trans, psik, norm, pos, st, 0.4, crop=64)
+    a = engine_cbed(trans, psik, norm, pos, kmax, lam, st, 0.4, crop=64, group=3)
+    b = engine_cbed(trans, psik, norm, pos, kmax, lam, st, 0.4, crop=64, group=3, graph=False)
+    c = engine_cbed(trans, psik, norm, pos, kmax, lam, st, 0.4, crop=64, group=7)
+    assert a.shape == (7, 64, 64)
+    assert O.rel_l2(a, ref).max() < 2e-5
+    np.testing.assert_array_equal(a, b)
+    np.testing.assert_array_equal(a, c)
+
+
+def test_zero_slices_and_single_probe():
+    g, trans, psik, norm, pos, kmax, lam, st = random_case(64, 64, S=0, P=1, seed=5)
+    trans = np.zeros((0, 64, 64), np.complex64)
+    ref = oracle_cbed(g, trans, psik, norm, pos, st, 1 / 3)
+    got = engine_cbed(trans, psik, norm, pos, kmax, lam, st, 1 / 3)
+    assert O.rel_l2(got, ref).max() < 1e-6
+
+
+def test_errors_surface_as_exceptions():
+    with pytest.raises(_lib.MsxError) as e:
+        engine.Plan(500, 512)
+    assert e.value.code == _lib.MSX_ERR_UNSUPPORTED
+    g, trans, psik, norm, pos, kmax, lam, st = random_case(64, 64, S=1, P=1, seed=6)
+    plan = engine.Plan(64, 64)
+    with pytest.raises(_lib.MsxError):
+        plan.multislice(torch.from_numpy(trans).to(DEV), torch.from_numpy(psik).to(DEV),
+                        torch.tensor([norm], dtype=torch.float64, device=DEV), torch.from_numpy(pos).to(DEV),
+                        np.float32(kmax), lam, st, np.float32(kmax / 3), crop=100)
+
+
+# ----------------------------------------------------------------------------- full pipelines
+def test_config1_pipeline_vs_fp64():
+    """Plain single-probe CBED, Si [001] 4x4x20 cells, 256^2, 80 slices, 100 keV,
+    20 mrad, probe at the cell centre: the MSAGPU surface end to end against
+    the FP64 oracle (its own windows, slices, probe and propagation)."""
+    sc = O.si_supercell(4, 4, 20)
+    t = 5.431 / 4
+    pd = {'smooth_apert': True, 'apert_smooth': 50, 'spherical_phase': True,
+          'aberration_dict': {'C1': 0., 'C3': 0., 'C5': 0.}, 'scherzer': False}
+    sim = M.MSAGPU(100, 20e-3, sc, sampling=np.array([256, 256]), debye_waller=False)
+    sim.setup_device(0)
+    sim.calc_atomic_potentials()
+    sim.build_potential_slices(t)
+    assert sim.num_slices == 80
+    sim.build_probe(pd)
+    sim.probe_positions = np.array([[0., 0.]])
+    sim.num_probes = 1
+    sim.multislice(bandwidth=1 / 3)
+    got = sim.probes
+
+    geom = crystal_geom(sc, 100., 20e-3, (256, 256))
+    _, win = O.atom_windows(geom, KIRK)
+    V = O.potential_slices_gpu(O.slice_sites_gpu(geom, t), win, geom.sampling, mode='f64')
+    tr = O.transmission(V, geom.sigma)
+    psik, _, norm = O.probe_gpu(geom, pd)
+    P, _ = O.propagator_gpu(geom, t, 1 / 3)
+    ref = O.multislice_gpu(tr, psik, P, np.array([[0., 0.]]), norm, geom)
+    err = O.rel_l2(got, ref)
+    assert got.shape == (1, 256, 256)
+    assert err.max() < 1e-4, err
+    assert 0.9 < got.sum() <= 1.0 + 1e-5
+
+
+def test_config2_scan_sampled_vs_fp64():
+    """Batched STEM scan, Si [001] 8x8x50 cells, 512^2, 199 slices, 200 keV,
+    30 mrad, Cs 1 um, 32x32 positions over one unit cell, central 256^2 crop.
+    All 1024 patterns run; 4 of them are checked against the FP64 oracle,
+    all of them for finiteness, range and run-to-run bit identity."""
+    a = 5.431
+    sc = O.si_supercell(8, 8, 50)
+    t = a / 4
+    pd = {'smooth_apert': True, 'apert_smooth': 50, 'spherical_phase': True,
+          'aberration_dict': {'C1': 0., 'C3': 1e4, 'C5': 0.}, 'scherzer': False}
+    sim = M.MSAGPU(200, 30e-3, sc, sampling=np.array([512, 512]), debye_waller=False)
+    sim.setup_device(0)
+    sim.calc_atomic_potentials()
+    sim.build_potential_slices(t)
+    assert sim.num_slices == 199
+    sim.build_probe(pd)
+    ii, jj = np.meshgrid(np.arange(32), np.arange(32), indexing='ij')
+    sim.probe_positions = np.column_stack([ii.ravel() * a / 32, jj.ravel() * a / 32])
+    sim.num_probes = 1024
+    sim.multislice(bandwidth=1 / 3, crop=256)
+    got = sim.probes.copy()
+    sim.multislice(bandwidth=1 / 3, crop=256)
+    np.testing.assert_array_equal(sim.probes, got)
+    assert got.shape == (1024, 256, 256) and np.isfinite(got).all() and got.min() >= 0
+    tot = got.astype(np.float64).sum((1, 2))
+    assert (tot > 0.5).all() and (tot < 1.0 + 1e-5).all()
+
+    geom = crystal_geom(sc, 200., 30e-3, (512, 512))
+    tr = sim.trans.cpu().numpy().astype(np.complex128)
+    psik, _, norm = O.probe_gpu(geom, pd)
+    P, _ = O.propagator_gpu(geom, t, 1 / 3)
+    pick = np.array([0, 333, 517, 1023])
+    ref = O.multislice_gpu(tr, psik, P, sim.probe_positions[pick], norm, geom, crop=256)
+    err = O.rel_l2(got[pick], ref)
+    assert err.max() < 1e-4, err

@@ -1,0 +1,92 @@
+"""Host-side logic of the MSAGPU surface against the oracle and the golden
+fixtures made from the reference.  CPU only (no CUDA calls)."""
+import os
+
+import numpy as np
+import pytest
+
+from namsa_gb300 import msa as M
+from namsa_gb300 import optics
+from oracle import msa_oracle as O
+
+G = os.path.join(os.path.dirname(__file__), 'golden')
+
+
+def test_optics_match_golden():
+    g = np.load(os.path.join(G, 'optics.npz'))
+    np.testing.assert_allclose(optics.voltage2Lambda(g['volts']), g['lam'], rtol=1e-15)
+    np.testing.assert_allclose(optics.sigma_int(g['volts']), g['sigma'], rtol=1e-15)
+    np.testing.assert_allclose(optics.scherzer_defocus(g['lam'], 1e4), g['scherzer_c1'], rtol=1e-15)
+
+
+def test_kirkland_table():
+    k = M.kirkland_table()
+    assert k.shape == (103, 4, 3) and k.dtype == np.float64
+    assert np.all(k[:, 1] > 0) and np.all(k[:, 3] > 0)
+
+
+@pytest.mark.parametrize('cells,n,t,expected', [((4, 4, 20), 256, 5.431 / 4, 80), ((8, 8, 50), 512, 5.431 / 4, 199)])
+def test_num_slices(cells, n, t, expected):
+    sc = O.si_supercell(*cells)
+    xyz = np.column_stack([sc['x'], sc['y'], sc['z']]).astype(np.float32)
+    dims = xyz.max(0) - xyz.min(0)
+    assert M.num_slices_of(dims[-1], t) == expected
+    geom = O.Geometry(xyz, sc['atomic_number'], 100., 20e-3, [n, n])
+    assert geom.num_slices(t) == expected
+
+
+def test_slice_sites_match_oracle():
+    sc = O.srtio3_supercell(3, 3, 4)
+    xyz = np.column_stack([sc['x'], sc['y'], sc['z']]).astype(np.float32)
+    geom = O.Geometry(xyz, sc['atomic_number'], 300., 25e-3, [128, 128])
+    t = 3.905 / 2
+    S = geom.num_slices(t)
+    sites, offs = M.slice_sites(xyz, sc['atomic_number'], geom.pix_size, t, S)
+    ref = O.slice_sites_gpu(geom, t)
+    assert len(offs) == S + 1 and offs[-1] == sum(len(r) for r in ref)
+    for s in range(S):
+        np.testing.assert_array_equal(sites[offs[s]:offs[s + 1], :3], ref[s])
+    assert sites.dtype == np.int32 and sites.shape[1] == 4
+
+
+def test_window_grid():
+    sc = O.si_supercell(4, 4, 20)
+    xyz = np.column_stack([sc['x'], sc['y'], sc['z']]).astype(np.float32)
+    geom = O.Geometry(xyz, sc['atomic_number'], 100., 20e-3, [256, 256])
+    assert M.window_grid(geom.pix_size) == (188, 188)
+
+
+@pytest.mark.parametrize('name,kw', [
+    ('steps', dict(probe_step=np.array([0.5, 0.5]), probe_range=np.array([[0.25, 0.75], [0.25, 0.75]]))),
+    ('grid2', dict(grid_steps=np.array([4, 6]), fraction=0.25, origin=np.array([0.1, 0.2]))),
+])
+def test_positions_match_golden(name, kw):
+    g = np.load(os.path.join(G, 'positions.npz'))
+    pos, st, rg = M.probe_positions_grid(g['dims'], **kw)
+    np.testing.assert_array_equal(pos, g[name + '_pos'])
+    np.testing.assert_array_equal(st, g[name + '_steps'])
+    np.testing.assert_array_equal(rg, g[name + '_range'])
+
+
+def test_plan_heuristic():
+    # 1024 probes of 512^2 need 2 GiB: with 3 GB free the reference halves... by 0.75 steps
+    n = M.max_probes_for(1024, np.array([512, 512]), 0, 3e9)
+    assert n * 512 * 512 * 8 / 1024e6 <= 0.5 * 3e9 / 1024e6
+    assert int(n / 0.75) * 512 * 512 * 8 / 1024e6 > 0.5 * 3e9 / 1024e6 or n == 1024
+    assert M.max_probes_for(10, np.array([64, 64]), 0, 1e12) == 10
+
+
+def test_supercell_loader_and_detector(tmp_path):
+    sc = O.si_supercell(1, 1, 1)
+    arr = M.load_supercell(sc)
+    assert arr is not sc and len(arr) == len(sc)
+    p = tmp_path / 'si.xyz'
+    with open(p, 'w') as f:
+        f.write(f'{len(sc)}\ncomment\n')
+        for r in sc:
+            f.write(f"{r['atomic_number']} {r['x']} {r['y']} {r['z']} {r['occ']} {r['DW']}\n")
+        f.write('-1\n')
+    arr2 = M.load_supercell(str(p))
+    np.testing.assert_allclose(arr2['x'], sc['x'], rtol=1e-6)
+    det = M.annular_detector(np.array([64, 64]), np.array([0.1, 0.1]), 0.025, 0.05, 0.1)
+    assert det.shape == (64, 64) and det.dtype == bool and 0 < det.sum() < 64 * 64
