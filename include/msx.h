@@ -148,6 +148,21 @@ MSX_API int msx_multislice(msx_plan* plan, const float* trans_dev, int num_slice
                    void* stream);
 
 /*
+ * Autotuner: times every (row schedule, column schedule, group size) of the
+ * plan's grid on the given inputs -- `iters` slices of row + column passes
+ * per candidate, CUDA events on `stream` -- and keeps the fastest.  Group
+ * sizes range over resident sets of 8 MiB to 1 GiB of waves (capped by
+ * num_probes and max_workspace_bytes, 0 = 1 GiB).  Writes the best time per
+ * wave and slice (ns) to *best_ns_per_wave_slice when non-NULL.  Synchronises
+ * `stream`.  No counterpart in the reference (its batch size comes from a
+ * free-memory heuristic, namsa/msa.py:445-461).
+ */
+MSX_API int msx_plan_autotune(msx_plan* plan, const float* trans_dev, int num_slices, const float* psi_k_dev,
+                              const double* normalization_dev, const float* positions_dev, int num_probes, float kmax,
+                              double lambda, double slice_t, float k_band, int iters, size_t max_workspace_bytes,
+                              float* best_ns_per_wave_slice, void* stream);
+
+/*
  * Diagnostics: times one row pass and one column pass of the plan's first
  * group, `iters` times each, with CUDA events on `stream` (one slice of
  * msx_multislice per iteration).  ms_out[0] = mean row-pass ms, ms_out[1] =

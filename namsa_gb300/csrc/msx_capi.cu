@@ -451,4 +451,67 @@ int msx_plan_profile(msx_plan* p, const float* trans_dev, int num_slices, const 
   return MSX_OK;
 }
 
+int msx_plan_autotune(msx_plan* p, const float* trans_dev, int num_slices, const float* psi_k_dev,
+                      const double* normalization_dev, const float* positions_dev, int num_probes, float kmax,
+                      double lambda, double slice_t, float k_band, int iters, size_t max_workspace_bytes,
+                      float* best_ns_per_wave_slice, void* stream) {
+  if (!p) return fail(MSX_ERR_INVALID, "null plan");
+  if (iters <= 0 || num_slices <= 0 || num_probes <= 0 || !trans_dev || !psi_k_dev || !normalization_dev || !positions_dev)
+    return fail(MSX_ERR_INVALID, "autotune needs slices, probes, inputs and iters > 0");
+  const SchedOps *rops, *cops;
+  const int nr = schedule_table(p->nx, &rops), nc = schedule_table(p->ny, &cops);
+  const size_t wave_bytes = sizeof(float2) * (size_t)p->ny * p->nx;
+  if (max_workspace_bytes == 0) max_workspace_bytes = (size_t)1 << 30;
+  // candidate groups: resident sets of 8 MiB .. 1 GiB, and every probe at once
+  std::vector<int> groups;
+  for (size_t mb : {8, 16, 24, 32, 48, 64, 96, 128, 192, 256, 512, 1024}) {
+    size_t g = (mb << 20) / wave_bytes;
+    if (g < 1) g = 1;
+    if (g > (size_t)num_probes) g = (size_t)num_probes;
+    if (g * wave_bytes > max_workspace_bytes) continue;
+    if (groups.empty() || groups.back() != (int)g) groups.push_back((int)g);
+  }
+  if (groups.empty()) groups.push_back(1);
+  cudaStream_t st = (cudaStream_t)stream;
+  cudaEvent_t e0, e1;
+  MSX_CUDA(cudaEventCreate(&e0), "cudaEventCreate");
+  MSX_CUDA(cudaEventCreate(&e1), "cudaEventCreate");
+  const int orig_r = p->row_sched, orig_c = p->col_sched, orig_g = p->group;
+  float best = 1e30f;
+  int br = orig_r, bc = orig_c, bg = orig_g;
+  const float2* trans = reinterpret_cast<const float2*>(trans_dev);
+  const size_t wave = (size_t)p->ny * p->nx;
+  int rc = MSX_OK;
+  for (int r = 0; r < nr && rc == MSX_OK; ++r)
+    for (int cidx = 0; cidx < nc && rc == MSX_OK; ++cidx)
+      for (int g : groups) {
+        rc = msx_plan_set_schedule(p, r, cidx, g);
+        if (rc != MSX_OK) break;
+        MSX_CUDA(launch_ptab(p->ny, p->nx, kmax, lambda, slice_t, k_band, p->ptab, st), "propagator table");
+        ColArgs c{};
+        c.psi = p->psi; c.ptab = p->ptab; c.psik = reinterpret_cast<const float2*>(psi_k_dev); c.pos_yx = positions_dev;
+        c.tw = p->tw_col; c.norm = normalization_dev; c.G = g; c.Nx = p->nx; c.kmax = kmax; c.x_begin = 0; c.ncols = p->nx;
+        MSX_CUDA(p->col_ops->col(COL_INIT, c, st), "probe formation pass");
+        for (int pass = 0; pass < 2; ++pass) {  // pass 0 warms caches and clocks
+          MSX_CUDA(cudaEventRecord(e0, st), "cudaEventRecord");
+          for (int i = 0; i < iters; ++i) {
+            MSX_CUDA(p->row_ops->row(p->psi, trans + (size_t)(i % num_slices) * wave, p->tw_row, g, p->ny, st), "row pass");
+            MSX_CUDA(p->col_ops->col(COL_MID, c, st), "column pass");
+          }
+          MSX_CUDA(cudaEventRecord(e1, st), "cudaEventRecord");
+        }
+        MSX_CUDA(cudaEventSynchronize(e1), "cudaEventSynchronize");
+        float ms = 0;
+        MSX_CUDA(cudaEventElapsedTime(&ms, e0, e1), "cudaEventElapsedTime");
+        const float ns = ms * 1e6f / ((float)iters * (float)g);
+        if (ns < best) { best = ns; br = r; bc = cidx; bg = g; }
+      }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (rc != MSX_OK) return rc;
+  rc = msx_plan_set_schedule(p, br, bc, bg);
+  if (best_ns_per_wave_slice) *best_ns_per_wave_slice = best;
+  return rc;
+}
+
 }  // extern "C"

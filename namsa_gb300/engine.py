@@ -179,3 +179,14 @@ class Plan:
                                           positions.shape[0], float(kmax), float(lam), float(slice_t), float(k_band),
                                           int(iters), out, _stream()))
         return float(out[0]), float(out[1]), int(out[2])
+
+    def autotune(self, trans, psik, norm, positions, kmax, lam, slice_t, k_band, iters=8, max_workspace_bytes=0):
+        """Pick the fastest (row schedule, column schedule, group) on these inputs;
+        returns (schedule tuple, ns per wave and slice)."""
+        best = ctypes.c_float()
+        S = trans.shape[0]
+        _lib.check(lib().msx_plan_autotune(self.handle, _ptr(trans), S, _ptr(psik), _ptr(norm), _ptr(positions),
+                                           positions.shape[0], float(kmax), float(lam), float(slice_t),
+                                           float(k_band), int(iters), int(max_workspace_bytes), ctypes.byref(best),
+                                           _stream()))
+        return self.schedule, float(best.value)
