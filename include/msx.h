@@ -148,6 +148,32 @@ MSX_API int msx_multislice(msx_plan* plan, const float* trans_dev, int num_slice
                    void* stream);
 
 /*
+ * msx_multislice without any device allocation, for callers that cannot call
+ * cudaMalloc: applications whose device memory is entirely owned by their own
+ * pool or allocator, plugin hosts that forbid allocation inside their callbacks,
+ * and latency-critical loops that must not take cudaMalloc's implicit device
+ * synchronisation.  No counterpart in the reference.
+ *
+ * Arguments are those of msx_multislice with the grid size given directly
+ * (no plan).  Scratch -- twiddle tables, the propagator table and the resident
+ * wave group -- lives in one static 32 MiB device array compiled into the
+ * library; every GPU that loads the library holds it until the process exits.
+ * A grid needs (2048 + 2*ny*nx) complex64 words of it at least, so every
+ * supported size fits (1024 x 1024 runs 2 waves at a time); larger requests
+ * return MSX_ERR_INVALID.  The first call on a device looks up the array's
+ * device address (cudaGetSymbolAddress) with that device current; make that
+ * first call before any stream capture.  All calls share the array and it keeps
+ * the last call's contents (nothing in it needs to start at zero): calls whose
+ * work overlaps on the GPU -- on different streams, or from different host
+ * threads -- race on it and must be serialised by the caller.  Uses the first
+ * FFT schedule of each line length.
+ */
+MSX_API int msx_multislice_noalloc(const float* trans_dev, int num_slices, const float* psi_k_dev,
+                                   const double* normalization_dev, const float* positions_dev, int num_probes,
+                                   int ny, int nx, float kmax, double lambda, double slice_t, float k_band,
+                                   float* cbed_out_dev, int crop_y, int crop_x, void* stream);
+
+/*
  * Autotuner: times every (row schedule, column schedule, group size) of the
  * plan's grid on the given inputs -- `iters` slices of row + column passes
  * per candidate, CUDA events on `stream` -- and keeps the fastest.  Group

@@ -39,6 +39,8 @@ SIGNATURES = [
     ('msx_plan_set_graph', _c.c_int, [_vp, _c.c_int]),
     ('msx_multislice', _c.c_int, [_vp, _vp, _c.c_int, _vp, _vp, _vp, _c.c_int, _c.c_float, _c.c_double,
                                   _c.c_double, _c.c_float, _vp, _c.c_int, _c.c_int, _vp]),
+    ('msx_multislice_noalloc', _c.c_int, [_vp, _c.c_int, _vp, _vp, _vp, _c.c_int, _c.c_int, _c.c_int, _c.c_float,
+                                          _c.c_double, _c.c_double, _c.c_float, _vp, _c.c_int, _c.c_int, _vp]),
     ('msx_plan_autotune', _c.c_int, [_vp, _vp, _c.c_int, _vp, _vp, _vp, _c.c_int, _c.c_float, _c.c_double,
                                      _c.c_double, _c.c_float, _c.c_int, _c.c_size_t, _c.POINTER(_c.c_float), _vp]),
     ('msx_plan_profile', _c.c_int, [_vp, _vp, _c.c_int, _vp, _vp, _vp, _c.c_int, _c.c_float, _c.c_double,

@@ -75,6 +75,8 @@ bool aligned(const void* p, size_t a) { return (reinterpret_cast<uintptr_t>(p) %
 
 }  // namespace
 
+void msx::set_last_error(const char* msg) { g_err = msg; }
+
 struct msx_plan {
   int ny = 0, nx = 0, device = 0;
   int group = 0;
