@@ -57,6 +57,8 @@ def parse():
     p.add_argument('--no-e2e', action='store_true')
     p.add_argument('--no-cpu-baseline', action='store_true')
     p.add_argument('--cpu-sample', type=int, default=0, help='probes per CPU-baseline sample (0 = number of cores)')
+    p.add_argument('--probes', type=int, default=1024, help='positions per GPU (the first N of the 32x32 scan)')
+    p.add_argument('--autotune', action='store_true', help='pick schedules and group size by msx_plan_autotune')
     return p.parse_args()
 
 
@@ -216,7 +218,7 @@ def run_ours(args):
     want_cpu = (rank == 0 and world == 1 and not args.no_cpu_baseline)
 
     sim, build_ms = build_workload(local, need_potential=want_cpu)
-    pos_np = scan_positions(rank)
+    pos_np = scan_positions(rank)[:args.probes]
     P = len(pos_np)
     pos = torch.from_numpy(pos_np).to(dev)
     kmax32 = np.float32(sim.kmax)
@@ -224,6 +226,11 @@ def run_ours(args):
     plan = engine.Plan(512, 512, args.group)
     r, c, g = plan.schedule
     plan.set_schedule(r if args.row_sched < 0 else args.row_sched, c if args.col_sched < 0 else args.col_sched)
+    tuned = None
+    if args.autotune:
+        sched, ns = plan.autotune(sim.trans, sim.psi_k_dev, sim.norm_dev, pos, kmax32, sim.Lambda, sim.slice_t, kband)
+        tuned = {'row': engine.schedules(512)[sched[0]], 'col': engine.schedules(512)[sched[1]], 'group': sched[2],
+                 'ns_per_wave_slice': ns}
     crop = 256
     out = torch.empty((P, crop, crop), dtype=torch.float32, device=dev)
 
@@ -334,7 +341,7 @@ def run_ours(args):
                        'l2': 'inputs larger than L2 (transmission stack 398 MiB, CBED out 256 MiB)',
                        'schedule': {'row': engine.schedules(512)[plan.schedule[0]],
                                     'col': engine.schedules(512)[plan.schedule[1]], 'group': plan.schedule[2]},
-                       'potential_and_probe_build_ms': build_ms},
+                       'potential_and_probe_build_ms': build_ms, 'autotuned': tuned},
             'gpu_launches': int(launches), 'clocks': clk, 'e2e': e2e, 'roofline': roof}
 
     if want_cpu:
