@@ -59,6 +59,10 @@ def parse():
     p.add_argument('--cpu-sample', type=int, default=0, help='probes per CPU-baseline sample (0 = number of cores)')
     p.add_argument('--probes', type=int, default=1024, help='positions per GPU (the first N of the 32x32 scan)')
     p.add_argument('--autotune', action='store_true', help='pick schedules and group size by msx_plan_autotune')
+    p.add_argument('--no-tma', action='store_true', help='plain one-CTA-per-tile passes instead of the persistent ones')
+    p.add_argument('--workload', default='scan', choices=['scan', 'uneven'],
+                   help='scan: the 512^2 Si [001] 1024-position scan; uneven: 64 seeded random crystals in one batch')
+    p.add_argument('--branches', type=int, default=4, help='concurrent graph branches of the uneven batch')
     return p.parse_args()
 
 
@@ -224,6 +228,7 @@ def run_ours(args):
     kmax32 = np.float32(sim.kmax)
     kband = np.float32(sim.kmax / 3)
     plan = engine.Plan(512, 512, args.group)
+    plan.set_tma(not args.no_tma)
     r, c, g = plan.schedule
     plan.set_schedule(r if args.row_sched < 0 else args.row_sched, c if args.col_sched < 0 else args.col_sched)
     tuned = None
@@ -341,7 +346,8 @@ def run_ours(args):
                        'l2': 'inputs larger than L2 (transmission stack 398 MiB, CBED out 256 MiB)',
                        'schedule': {'row': engine.schedules(512)[plan.schedule[0]],
                                     'col': engine.schedules(512)[plan.schedule[1]], 'group': plan.schedule[2]},
-                       'potential_and_probe_build_ms': build_ms, 'autotuned': tuned},
+                       'potential_and_probe_build_ms': build_ms, 'autotuned': tuned,
+                       'passes': 'plain' if args.no_tma else 'persistent TMA-pipelined'},
             'gpu_launches': int(launches), 'clocks': clk, 'e2e': e2e, 'roofline': roof}
 
     if want_cpu:
@@ -360,10 +366,52 @@ def run_ours(args):
         dist.destroy_process_group()
 
 
+def run_uneven(args):
+    """64 seeded random crystals (grids 256..768^2, 50-500 A, 80-300 kV, 16-256
+    positions each) in one graph-captured batch; probes/s over the whole batch."""
+    import torch
+    from namsa_gb300 import engine, workloads
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    dev = torch.device('cuda', local)
+    t0 = time.perf_counter()
+    specs, sims, jobs = workloads.random_batch(1234 + rank, count=64, device=dev)
+    torch.cuda.synchronize()
+    build_s = time.perf_counter() - t0
+    batch = engine.Batch(branches=args.branches)
+    for _ in range(max(args.warmup, 3)):
+        batch.run(jobs)
+    torch.cuda.synchronize()
+    st = torch.cuda.current_stream()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(st)
+    for _ in range(args.steps):
+        batch.run(jobs)
+    e1.record(st)
+    torch.cuda.synchronize()
+    batch.check()
+    ms = e0.elapsed_time(e1) / args.steps
+    P = sum(j['positions'].shape[0] for j in jobs)
+    ps, psp = workloads.work_units(jobs)
+    grids = {}
+    for s in specs:
+        grids[s['n']] = grids.get(s['n'], 0) + 1
+    line = {'metric': METRIC, 'value': P / (ms / 1e3), 'unit': UNIT, 'n_gpus': 1, 'steps': args.steps,
+            'warmup': args.warmup, 'ms_per_step': ms, 'higher_is_better': True, 'scaling': 'weak',
+            'vs_baseline': None, 'dtype': 'c64', 'data': 'synthetic (64 seeded random cubic crystals)',
+            'config': {'workload': 'uneven batch of 64 random crystals, one CUDA graph', 'probes': P,
+                       'probe_slices': ps, 'probe_slice_pixels_per_s': psp / (ms / 1e3),
+                       'grids': grids, 'branches': args.branches, 'build_s': build_s}}
+    print(json.dumps(line), flush=True)
+    batch.close()
+
+
 def main():
     args = parse()
     if args.impl == 'reference':
         run_reference(args)
+    elif args.workload == 'uneven':
+        run_uneven(args)
     else:
         run_ours(args)
 

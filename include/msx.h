@@ -36,6 +36,7 @@ extern "C" {
 #define MSX_ERR_UNSUPPORTED -2  /* grid line length without a compiled schedule */
 #define MSX_ERR_CUDA -3         /* CUDA runtime error (launch, configuration)   */
 #define MSX_ERR_ALLOC -4        /* device allocation failed                     */
+#define MSX_ERR_TIMEOUT -5      /* a bounded wait inside a kernel gave up       */
 
 #if defined(__GNUC__)
 #define MSX_API __attribute__((visibility("default")))
@@ -44,6 +45,22 @@ extern "C" {
 #endif
 
 typedef struct msx_plan msx_plan;
+typedef struct msx_batch msx_batch;
+
+/* One crystal of an uneven batch (msx_batch_run): the arguments of
+ * msx_multislice for one grid. */
+typedef struct msx_job {
+  int ny, nx;                       /* grid (supported line lengths)            */
+  int num_slices, num_probes;
+  int crop_y, crop_x;
+  float kmax, k_band;               /* float32 k extent and mask radius          */
+  double lambda, slice_t;
+  const float* trans_dev;           /* (num_slices, ny, nx) complex64            */
+  const float* psi_k_dev;           /* (ny, nx) complex64                        */
+  const double* normalization_dev;  /* 1 float64                                 */
+  const float* positions_dev;       /* (num_probes, 2) [y, x] Angstrom           */
+  float* cbed_out_dev;              /* (num_probes, crop_y, crop_x) float32      */
+} msx_job;
 
 /* Library version (major*10000 + minor*100 + patch). */
 MSX_API int msx_version(void);
@@ -121,6 +138,16 @@ MSX_API int msx_plan_set_schedule(msx_plan* plan, int row_schedule, int col_sche
 /* Reports the current row/column schedule indices and group size. */
 MSX_API int msx_plan_get_schedule(const msx_plan* plan, int* row_schedule, int* col_schedule, int* group);
 
+/* 1 = run the per-slice passes as persistent, TMA-pipelined kernels (default);
+ * 0 = one CTA per tile, plain loads.  Both give the same results. */
+MSX_API int msx_plan_set_tma(msx_plan* plan, int enable);
+
+/* Synchronises the device and reports whether a pipelined pass of this plan
+ * gave up on a bounded wait since the last check (MSX_ERR_TIMEOUT; the error
+ * word is then cleared).  Kernels never trap: a stuck copy makes the pass
+ * return early and flag the plan instead. */
+MSX_API int msx_plan_check(msx_plan* plan);
+
 /* 1 = record the launch sequence of msx_multislice in a CUDA graph and
  * replay it while the arguments repeat (default 1); 0 = launch directly. */
 MSX_API int msx_plan_set_graph(msx_plan* plan, int enable);
@@ -172,6 +199,23 @@ MSX_API int msx_multislice_noalloc(const float* trans_dev, int num_slices, const
                                    const double* normalization_dev, const float* positions_dev, int num_probes,
                                    int ny, int nx, float kmax, double lambda, double slice_t, float k_band,
                                    float* cbed_out_dev, int crop_y, int crop_x, void* stream);
+
+/*
+ * Uneven batches.  Replaces the reference's fan-out over materials and probe
+ * blocks (MPI ranks with one crystal each, scripts/sim_batch.py:201,
+ * namsa/msa.py:1014-1081) by one CUDA graph on one GPU: jobs of different grid
+ * size, thickness, voltage and probe count are spread over `branches`
+ * concurrent streams (0 = 4), longest first, each branch keeping one plan per
+ * grid size.  The graph is captured on the first call for a job list and
+ * replayed while the list repeats; it runs ordered on `stream`.
+ */
+MSX_API int msx_batch_create(int branches, msx_batch** batch);
+MSX_API int msx_batch_destroy(msx_batch* batch);
+/* Schedule and group size used for the (ny, nx) plans of the batch. */
+MSX_API int msx_batch_set_schedule(msx_batch* batch, int ny, int nx, int row_schedule, int col_schedule, int group);
+MSX_API int msx_batch_run(msx_batch* batch, const msx_job* jobs, int njobs, void* stream);
+/* msx_plan_check over every plan of the batch. */
+MSX_API int msx_batch_check(msx_batch* batch);
 
 /*
  * Autotuner: times every (row schedule, column schedule, group size) of the

@@ -17,6 +17,7 @@ MSX_ERR_INVALID = -1
 MSX_ERR_UNSUPPORTED = -2
 MSX_ERR_CUDA = -3
 MSX_ERR_ALLOC = -4
+MSX_ERR_TIMEOUT = -5
 
 # (name, restype, argtypes) for every entry point of include/msx.h
 _c = ctypes
@@ -37,15 +38,31 @@ SIGNATURES = [
     ('msx_plan_set_schedule', _c.c_int, [_vp, _c.c_int, _c.c_int, _c.c_int]),
     ('msx_plan_get_schedule', _c.c_int, [_vp, _c.POINTER(_c.c_int), _c.POINTER(_c.c_int), _c.POINTER(_c.c_int)]),
     ('msx_plan_set_graph', _c.c_int, [_vp, _c.c_int]),
+    ('msx_plan_set_tma', _c.c_int, [_vp, _c.c_int]),
+    ('msx_plan_check', _c.c_int, [_vp]),
     ('msx_multislice', _c.c_int, [_vp, _vp, _c.c_int, _vp, _vp, _vp, _c.c_int, _c.c_float, _c.c_double,
                                   _c.c_double, _c.c_float, _vp, _c.c_int, _c.c_int, _vp]),
     ('msx_multislice_noalloc', _c.c_int, [_vp, _c.c_int, _vp, _vp, _vp, _c.c_int, _c.c_int, _c.c_int, _c.c_float,
                                           _c.c_double, _c.c_double, _c.c_float, _vp, _c.c_int, _c.c_int, _vp]),
+    ('msx_batch_create', _c.c_int, [_c.c_int, _c.POINTER(_vp)]),
+    ('msx_batch_destroy', _c.c_int, [_vp]),
+    ('msx_batch_set_schedule', _c.c_int, [_vp, _c.c_int, _c.c_int, _c.c_int, _c.c_int, _c.c_int]),
+    ('msx_batch_run', _c.c_int, [_vp, _vp, _c.c_int, _vp]),
+    ('msx_batch_check', _c.c_int, [_vp]),
     ('msx_plan_autotune', _c.c_int, [_vp, _vp, _c.c_int, _vp, _vp, _vp, _c.c_int, _c.c_float, _c.c_double,
                                      _c.c_double, _c.c_float, _c.c_int, _c.c_size_t, _c.POINTER(_c.c_float), _vp]),
     ('msx_plan_profile', _c.c_int, [_vp, _vp, _c.c_int, _vp, _vp, _vp, _c.c_int, _c.c_float, _c.c_double,
                                     _c.c_double, _c.c_float, _c.c_int, _c.POINTER(_c.c_float), _vp]),
 ]
+
+
+class MsxJob(ctypes.Structure):
+    """ctypes mirror of msx_job (include/msx.h)."""
+    _fields_ = [('ny', ctypes.c_int), ('nx', ctypes.c_int), ('num_slices', ctypes.c_int), ('num_probes', ctypes.c_int),
+                ('crop_y', ctypes.c_int), ('crop_x', ctypes.c_int), ('kmax', ctypes.c_float), ('k_band', ctypes.c_float),
+                ('lambda_', ctypes.c_double), ('slice_t', ctypes.c_double), ('trans_dev', ctypes.c_void_p),
+                ('psi_k_dev', ctypes.c_void_p), ('normalization_dev', ctypes.c_void_p),
+                ('positions_dev', ctypes.c_void_p), ('cbed_out_dev', ctypes.c_void_p)]
 
 
 class MsxLibraryError(ImportError):

@@ -3,6 +3,9 @@
 #include "msx.h"
 #include "msx_internal.h"
 
+#include <algorithm>
+#include <array>
+#include <cmath>
 #include <cstdarg>
 #include <cstdint>
 #include <cstdio>
@@ -93,6 +96,14 @@ struct msx_plan {
   bool use_graph = true;
   cudaGraphExec_t gexec = nullptr;
   std::vector<unsigned char> gkey;
+  // persistent TMA-pipelined passes
+  bool use_tma = true;
+  int* err = nullptr;            // device error word of the bounded waits
+  float2* pyx = nullptr;         // py[ny] then px[nx]
+  int2* band = nullptr;          // mask band per column
+  CUtensorMap map{};             // workspace as (psi_waves*ny) x nx 8-byte elements, box col_c x col_boxr
+  bool map_ok = false;
+  int row_ctas = 0, col_ctas = 0;
 };
 
 namespace {
@@ -120,6 +131,47 @@ int ensure_workspace(msx_plan* p, size_t waves) {
   return MSX_OK;
 }
 
+using EncodeTiled = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                  const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+EncodeTiled encode_tiled() {
+  static EncodeTiled fn = nullptr;
+  if (!fn) {
+    void* f = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<EncodeTiled>(f);
+  }
+  return fn;
+}
+
+// Tensor map of the wave workspace for the column pass's tile loads, and the
+// persistent grid sizes of the current schedules.
+int prepare_tma(msx_plan* p) {
+  p->map_ok = false;
+  EncodeTiled enc = encode_tiled();
+  if (!enc) return fail(MSX_ERR_CUDA, "cuTensorMapEncodeTiled is unavailable");
+  const cuuint64_t dims[2] = {(cuuint64_t)p->nx, (cuuint64_t)p->psi_waves * p->ny};
+  const cuuint64_t strides[1] = {(cuuint64_t)p->nx * sizeof(float2)};
+  const cuuint32_t box[2] = {(cuuint32_t)p->col_ops->col_c, (cuuint32_t)p->col_ops->col_boxr};
+  const cuuint32_t estr[2] = {1, 1};
+  CUresult r = enc(&p->map, CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 2, p->psi, dims, strides, box, estr,
+                   CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                   CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) return fail(MSX_ERR_CUDA, "cuTensorMapEncodeTiled failed (%d)", (int)r);
+  int sms = 0, rr = 0, cr = 0, dummy = 0;
+  MSX_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, p->device), "SM count");
+  MSX_CUDA(p->row_ops->occupancy(&rr, &dummy), "occupancy");
+  MSX_CUDA(p->col_ops->occupancy(&dummy, &cr), "occupancy");
+  if (rr < 1 || cr < 1) return fail(MSX_ERR_CUDA, "persistent passes do not fit on an SM");
+  p->row_ctas = sms * rr;
+  p->col_ctas = sms * cr;
+  p->map_ok = true;
+  return MSX_OK;
+}
+
 void drop_graph(msx_plan* p) {
   if (p->gexec) cudaGraphExecDestroy(p->gexec);
   p->gexec = nullptr;
@@ -142,9 +194,29 @@ struct MsArgs {
   int group, row_sched, col_sched;
 };
 
+// One slice's row pass and (mid) column pass over a group of gn waves.
+int slice_passes(msx_plan* p, const float2* trans_s, int gn, const ColArgs& c, bool with_col, cudaStream_t st) {
+  if (p->use_tma && p->map_ok) {
+    TmaPassArgs ta{};
+    ta.psi = p->psi; ta.trans = trans_s; ta.tw = p->tw_row; ta.pyx = p->pyx; ta.band = p->band; ta.err = p->err;
+    ta.G = gn; ta.Ny = p->ny; ta.Nx = p->nx;
+    MSX_CUDA(p->row_ops->row_tma(ta, p->row_ctas, st), "row pass");
+    if (with_col) {
+      ta.tw = p->tw_col;
+      MSX_CUDA(p->col_ops->col_tma(p->map, ta, p->col_ctas, st), "column pass");
+    }
+  } else {
+    MSX_CUDA(p->row_ops->row(p->psi, trans_s, p->tw_row, gn, p->ny, st), "row pass");
+    if (with_col) MSX_CUDA(p->col_ops->col(COL_MID, c, st), "column pass");
+  }
+  return MSX_OK;
+}
+
 int enqueue_multislice(msx_plan* p, const MsArgs& a, cudaStream_t st) {
   const int ny = p->ny, nx = p->nx;
   MSX_CUDA(launch_ptab(ny, nx, a.kmax, a.lambda, a.slice_t, a.k_band, p->ptab, st), "propagator table");
+  if (p->use_tma && p->map_ok)
+    MSX_CUDA(launch_pfac(ny, nx, a.kmax, a.lambda, a.slice_t, a.k_band, p->pyx, p->band, st), "propagator factors");
   const size_t wave = (size_t)ny * nx;
   const int y0 = ny / 2 - a.crop_y / 2, x0 = nx / 2 - a.crop_x / 2;
   const float2* trans = reinterpret_cast<const float2*>(a.trans);
@@ -173,10 +245,9 @@ int enqueue_multislice(msx_plan* p, const MsArgs& a, cudaStream_t st) {
     c.ncols = nx;
     MSX_CUDA(p->col_ops->col(COL_INIT, c, st), "probe formation pass");
     for (int s = 0; s < a.num_slices; ++s) {
-      MSX_CUDA(p->row_ops->row(p->psi, trans + (size_t)s * wave, p->tw_row, gn, ny, st), "row pass");
-      if (s + 1 < a.num_slices) {
-        MSX_CUDA(p->col_ops->col(COL_MID, c, st), "column pass");
-      } else {
+      const int rc = slice_passes(p, trans + (size_t)s * wave, gn, c, s + 1 < a.num_slices, st);
+      if (rc != MSX_OK) return rc;
+      if (s + 1 == a.num_slices) {
         ColArgs f = c;
         f.x_begin = x0;
         f.ncols = a.crop_x;
@@ -228,7 +299,7 @@ int msx_atom_windows(const double* coeff_dev, int nspecies, int n0, int n1, int 
   if (nspecies <= 0 || oversample <= 0 || n0 < 2 || n1 < 2 || n0 % oversample || n1 % oversample)
     return fail(MSX_ERR_INVALID, "bad window grid %d x %d (oversample %d, %d species)", n0, n1, oversample, nspecies);
   if (!(potential_range > 0)) return fail(MSX_ERR_INVALID, "potential range must be positive");
-  if ((size_t)(n0 / oversample) * (n1 / oversample) > 24000)
+  if ((size_t)(n0 / oversample) * (n1 / oversample) > (size_t)65535 * 128)
     return fail(MSX_ERR_INVALID, "window %d x %d too large", n0 / oversample, n1 / oversample);
   MSX_CUDA(launch_atom_windows(coeff_dev, nspecies, n0, n1, oversample, potential_range, windows_out_dev,
                                (cudaStream_t)stream), "atom windows");
@@ -280,7 +351,11 @@ int msx_plan_create(int ny, int nx, int group, msx_plan** out) {
   int rc = msx_plan_set_schedule(p, 0, 0, group > 0 ? group : auto_group(ny, nx));
   if (rc == MSX_OK) {
     cudaError_t e = cudaMalloc(&p->ptab, sizeof(float2) * (size_t)ny * nx);
-    if (e != cudaSuccess) rc = fail(MSX_ERR_ALLOC, "propagator table allocation failed");
+    if (e == cudaSuccess) e = cudaMalloc(&p->pyx, sizeof(float2) * (size_t)(ny + nx));
+    if (e == cudaSuccess) e = cudaMalloc(&p->band, sizeof(int2) * (size_t)nx);
+    if (e == cudaSuccess) e = cudaMalloc(&p->err, sizeof(int));
+    if (e == cudaSuccess) e = cudaMemset(p->err, 0, sizeof(int));
+    if (e != cudaSuccess) rc = fail(MSX_ERR_ALLOC, "plan table allocation failed");
   }
   if (rc == MSX_OK) {
     cudaError_t e = cudaStreamCreateWithFlags(&p->work, cudaStreamNonBlocking);
@@ -301,6 +376,9 @@ int msx_plan_destroy(msx_plan* p) {
   drop_graph(p);
   if (p->psi) cudaFree(p->psi);
   if (p->ptab) cudaFree(p->ptab);
+  if (p->pyx) cudaFree(p->pyx);
+  if (p->band) cudaFree(p->band);
+  if (p->err) cudaFree(p->err);
   if (p->tw_row) cudaFree(p->tw_row);
   if (p->tw_col) cudaFree(p->tw_col);
   if (p->ev_in) cudaEventDestroy(p->ev_in);
@@ -334,7 +412,9 @@ int msx_plan_set_schedule(msx_plan* p, int row_schedule, int col_schedule, int g
   p->col_ops = &cops[col_schedule];
   if (group > 0) p->group = group;
   drop_graph(p);
-  return ensure_workspace(p, (size_t)p->group);
+  rc = ensure_workspace(p, (size_t)p->group);
+  if (rc != MSX_OK) return rc;
+  return prepare_tma(p);
 }
 
 int msx_plan_get_schedule(const msx_plan* p, int* row_schedule, int* col_schedule, int* group) {
@@ -342,6 +422,24 @@ int msx_plan_get_schedule(const msx_plan* p, int* row_schedule, int* col_schedul
   if (row_schedule) *row_schedule = p->row_sched;
   if (col_schedule) *col_schedule = p->col_sched;
   if (group) *group = p->group;
+  return MSX_OK;
+}
+
+int msx_plan_set_tma(msx_plan* p, int enable) {
+  if (!p) return fail(MSX_ERR_INVALID, "null plan");
+  p->use_tma = enable != 0;
+  drop_graph(p);
+  return MSX_OK;
+}
+
+int msx_plan_check(msx_plan* p) {
+  if (!p) return fail(MSX_ERR_INVALID, "null plan");
+  int h = 0;
+  MSX_CUDA(cudaMemcpy(&h, p->err, sizeof(int), cudaMemcpyDeviceToHost), "reading the plan error word");
+  if (h) {
+    MSX_CUDA(cudaMemset(p->err, 0, sizeof(int)), "clearing the plan error word");
+    return fail(MSX_ERR_TIMEOUT, "a pipelined pass gave up waiting for its tile copy (error word 0x%x)", h);
+  }
   return MSX_OK;
 }
 
@@ -425,6 +523,7 @@ int msx_plan_profile(msx_plan* p, const float* trans_dev, int num_slices, const 
   cudaEvent_t ev[4];
   for (auto& e : ev) MSX_CUDA(cudaEventCreate(&e), "cudaEventCreate");
   MSX_CUDA(launch_ptab(ny, nx, kmax, lambda, slice_t, k_band, p->ptab, st), "propagator table");
+  MSX_CUDA(launch_pfac(ny, nx, kmax, lambda, slice_t, k_band, p->pyx, p->band, st), "propagator factors");
   ColArgs c{};
   c.psi = p->psi; c.ptab = p->ptab; c.psik = reinterpret_cast<const float2*>(psi_k_dev); c.pos_yx = positions_dev;
   c.tw = p->tw_col; c.norm = normalization_dev; c.cbed = nullptr; c.G = gn; c.Nx = nx; c.kmax = kmax;
@@ -435,9 +534,17 @@ int msx_plan_profile(msx_plan* p, const float* trans_dev, int num_slices, const 
   for (int i = 0; i < iters; ++i) {
     const int s = i % num_slices;
     MSX_CUDA(cudaEventRecord(ev[0], st), "cudaEventRecord");
-    MSX_CUDA(p->row_ops->row(p->psi, trans + (size_t)s * wave, p->tw_row, gn, ny, st), "row pass");
+    int rc = slice_passes(p, trans + (size_t)s * wave, gn, c, false, st);
+    if (rc != MSX_OK) return rc;
     MSX_CUDA(cudaEventRecord(ev[1], st), "cudaEventRecord");
-    MSX_CUDA(p->col_ops->col(COL_MID, c, st), "column pass");
+    if (p->use_tma && p->map_ok) {
+      TmaPassArgs ta{};
+      ta.psi = p->psi; ta.tw = p->tw_col; ta.pyx = p->pyx; ta.band = p->band; ta.err = p->err;
+      ta.G = gn; ta.Ny = ny; ta.Nx = nx;
+      MSX_CUDA(p->col_ops->col_tma(p->map, ta, p->col_ctas, st), "column pass");
+    } else {
+      MSX_CUDA(p->col_ops->col(COL_MID, c, st), "column pass");
+    }
     MSX_CUDA(cudaEventRecord(ev[2], st), "cudaEventRecord");
     MSX_CUDA(cudaEventSynchronize(ev[2]), "cudaEventSynchronize");
     float a = 0, b = 0;
@@ -466,7 +573,7 @@ int msx_plan_autotune(msx_plan* p, const float* trans_dev, int num_slices, const
   if (max_workspace_bytes == 0) max_workspace_bytes = (size_t)1 << 30;
   // candidate groups: resident sets of 8 MiB .. 1 GiB, and every probe at once
   std::vector<int> groups;
-  for (size_t mb : {8, 16, 24, 32, 48, 64, 96, 128, 192, 256, 512, 1024}) {
+  for (size_t mb : {8, 16, 32, 48, 64, 128, 256, 512, 1024}) {
     size_t g = (mb << 20) / wave_bytes;
     if (g < 1) g = 1;
     if (g > (size_t)num_probes) g = (size_t)num_probes;
@@ -478,42 +585,290 @@ int msx_plan_autotune(msx_plan* p, const float* trans_dev, int num_slices, const
   cudaEvent_t e0, e1;
   MSX_CUDA(cudaEventCreate(&e0), "cudaEventCreate");
   MSX_CUDA(cudaEventCreate(&e1), "cudaEventCreate");
-  const int orig_r = p->row_sched, orig_c = p->col_sched, orig_g = p->group;
-  float best = 1e30f;
-  int br = orig_r, bc = orig_c, bg = orig_g;
   const float2* trans = reinterpret_cast<const float2*>(trans_dev);
   const size_t wave = (size_t)p->ny * p->nx;
+  // The row and column passes only share the group size, so for every group the
+  // best row schedule and the best column schedule are found separately.
+  float best = 1e30f;
+  int br = p->row_sched, bc = p->col_sched, bg = p->group;
   int rc = MSX_OK;
-  for (int r = 0; r < nr && rc == MSX_OK; ++r)
-    for (int cidx = 0; cidx < nc && rc == MSX_OK; ++cidx)
-      for (int g : groups) {
-        rc = msx_plan_set_schedule(p, r, cidx, g);
-        if (rc != MSX_OK) break;
-        MSX_CUDA(launch_ptab(p->ny, p->nx, kmax, lambda, slice_t, k_band, p->ptab, st), "propagator table");
-        ColArgs c{};
-        c.psi = p->psi; c.ptab = p->ptab; c.psik = reinterpret_cast<const float2*>(psi_k_dev); c.pos_yx = positions_dev;
-        c.tw = p->tw_col; c.norm = normalization_dev; c.G = g; c.Nx = p->nx; c.kmax = kmax; c.x_begin = 0; c.ncols = p->nx;
-        MSX_CUDA(p->col_ops->col(COL_INIT, c, st), "probe formation pass");
-        for (int pass = 0; pass < 2; ++pass) {  // pass 0 warms caches and clocks
-          MSX_CUDA(cudaEventRecord(e0, st), "cudaEventRecord");
-          for (int i = 0; i < iters; ++i) {
-            MSX_CUDA(p->row_ops->row(p->psi, trans + (size_t)(i % num_slices) * wave, p->tw_row, g, p->ny, st), "row pass");
-            MSX_CUDA(p->col_ops->col(COL_MID, c, st), "column pass");
-          }
-          MSX_CUDA(cudaEventRecord(e1, st), "cudaEventRecord");
+  auto time_loop = [&](bool row_pass, int g, float* ms) -> int {
+    ColArgs c{};
+    c.psi = p->psi; c.ptab = p->ptab; c.psik = reinterpret_cast<const float2*>(psi_k_dev); c.pos_yx = positions_dev;
+    c.tw = p->tw_col; c.norm = normalization_dev; c.G = g; c.Nx = p->nx; c.kmax = kmax; c.x_begin = 0; c.ncols = p->nx;
+    MSX_CUDA(p->col_ops->col(COL_INIT, c, st), "probe formation pass");
+    for (int pass = 0; pass < 2; ++pass) {  // pass 0 warms caches and clocks
+      MSX_CUDA(cudaEventRecord(e0, st), "cudaEventRecord");
+      for (int i = 0; i < iters; ++i) {
+        if (row_pass) {
+          const int r2 = slice_passes(p, trans + (size_t)(i % num_slices) * wave, g, c, false, st);
+          if (r2 != MSX_OK) return r2;
+        } else if (p->use_tma && p->map_ok) {
+          TmaPassArgs ta{};
+          ta.psi = p->psi; ta.tw = p->tw_col; ta.pyx = p->pyx; ta.band = p->band; ta.err = p->err;
+          ta.G = g; ta.Ny = p->ny; ta.Nx = p->nx;
+          MSX_CUDA(p->col_ops->col_tma(p->map, ta, p->col_ctas, st), "column pass");
+        } else {
+          MSX_CUDA(p->col_ops->col(COL_MID, c, st), "column pass");
         }
-        MSX_CUDA(cudaEventSynchronize(e1), "cudaEventSynchronize");
-        float ms = 0;
-        MSX_CUDA(cudaEventElapsedTime(&ms, e0, e1), "cudaEventElapsedTime");
-        const float ns = ms * 1e6f / ((float)iters * (float)g);
-        if (ns < best) { best = ns; br = r; bc = cidx; bg = g; }
       }
+      MSX_CUDA(cudaEventRecord(e1, st), "cudaEventRecord");
+    }
+    MSX_CUDA(cudaEventSynchronize(e1), "cudaEventSynchronize");
+    MSX_CUDA(cudaEventElapsedTime(ms, e0, e1), "cudaEventElapsedTime");
+    return MSX_OK;
+  };
+  for (int g : groups) {
+    float best_row = 1e30f, best_col = 1e30f;
+    int gr = 0, gc = 0;
+    for (int r = 0; r < nr && rc == MSX_OK; ++r) {
+      rc = msx_plan_set_schedule(p, r, 0, g);
+      if (rc != MSX_OK) break;
+      MSX_CUDA(launch_ptab(p->ny, p->nx, kmax, lambda, slice_t, k_band, p->ptab, st), "propagator table");
+      MSX_CUDA(launch_pfac(p->ny, p->nx, kmax, lambda, slice_t, k_band, p->pyx, p->band, st), "propagator factors");
+      float ms = 0;
+      rc = time_loop(true, g, &ms);
+      if (rc == MSX_OK && ms < best_row) { best_row = ms; gr = r; }
+    }
+    for (int cidx = 0; cidx < nc && rc == MSX_OK; ++cidx) {
+      rc = msx_plan_set_schedule(p, gr, cidx, g);
+      if (rc != MSX_OK) break;
+      MSX_CUDA(launch_ptab(p->ny, p->nx, kmax, lambda, slice_t, k_band, p->ptab, st), "propagator table");
+      MSX_CUDA(launch_pfac(p->ny, p->nx, kmax, lambda, slice_t, k_band, p->pyx, p->band, st), "propagator factors");
+      float ms = 0;
+      rc = time_loop(false, g, &ms);
+      if (rc == MSX_OK && ms < best_col) { best_col = ms; gc = cidx; }
+    }
+    if (rc != MSX_OK) break;
+    const float ns = (best_row + best_col) * 1e6f / ((float)iters * (float)g);
+    if (ns < best) { best = ns; br = gr; bc = gc; bg = g; }
+  }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   if (rc != MSX_OK) return rc;
   rc = msx_plan_set_schedule(p, br, bc, bg);
   if (best_ns_per_wave_slice) *best_ns_per_wave_slice = best;
   return rc;
+}
+
+}  // extern "C"
+
+// ============================================================================ uneven batches
+// A batch runs many independent jobs (crystals of different grid size,
+// thickness, voltage and probe count) as one CUDA graph: the jobs are spread
+// over `branches` parallel streams inside the capture (longest first onto the
+// least loaded branch), each branch owning one plan per grid size, so the GPU
+// overlaps jobs of different shapes.  The graph is replayed while the job list
+// repeats.
+struct msx_batch {
+  int branches = 4;
+  int device = 0;
+  std::vector<std::vector<std::pair<long long, msx_plan*>>> plans;  // per branch: (ny<<32|nx, plan)
+  std::vector<cudaStream_t> streams;
+  std::vector<cudaEvent_t> events;  // fork/join events, 2 per branch
+  cudaStream_t origin = nullptr;
+  cudaEvent_t ev_in = nullptr, ev_out = nullptr;
+  cudaGraphExec_t gexec = nullptr;
+  std::vector<unsigned char> gkey;
+  std::vector<std::pair<long long, std::array<int, 3>>> sched;  // (ny<<32|nx) -> row, col, group
+};
+
+namespace {
+
+msx_plan* batch_plan(msx_batch* b, int branch, int ny, int nx, int* rc) {
+  const long long key = ((long long)ny << 32) | (unsigned)nx;
+  for (auto& kv : b->plans[branch])
+    if (kv.first == key) return kv.second;
+  // resident group per branch: the branches share about 96 MiB of L2-resident waves
+  int group = (int)(((size_t)96 << 20) / ((size_t)b->branches * sizeof(float2) * ny * nx));
+  if (group < 2) group = 2;
+  int r = 0, c = 0;
+  for (auto& kv : b->sched)
+    if (kv.first == key) { r = kv.second[0]; c = kv.second[1]; if (kv.second[2] > 0) group = kv.second[2]; }
+  msx_plan* p = nullptr;
+  *rc = msx_plan_create(ny, nx, group, &p);
+  if (*rc != MSX_OK) return nullptr;
+  if (r || c) {
+    *rc = msx_plan_set_schedule(p, r, c, group);
+    if (*rc != MSX_OK) { msx_plan_destroy(p); return nullptr; }
+  }
+  b->plans[branch].push_back({key, p});
+  return p;
+}
+
+}  // namespace
+
+extern "C" {
+
+int msx_batch_create(int branches, msx_batch** out) {
+  if (!out) return fail(MSX_ERR_INVALID, "null batch pointer");
+  *out = nullptr;
+  if (branches < 0 || branches > 16) return fail(MSX_ERR_INVALID, "branches must be 0..16");
+  msx_batch* b = new msx_batch();
+  b->branches = branches ? branches : 4;
+  cudaError_t e = cudaGetDevice(&b->device);
+  b->plans.resize(b->branches);
+  b->streams.resize(b->branches, nullptr);
+  b->events.resize(2 * b->branches, nullptr);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&b->origin, cudaStreamNonBlocking);
+  for (int i = 0; i < b->branches && e == cudaSuccess; ++i) e = cudaStreamCreateWithFlags(&b->streams[i], cudaStreamNonBlocking);
+  for (auto& ev : b->events)
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ev, cudaEventDisableTiming);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->ev_in, cudaEventDisableTiming);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->ev_out, cudaEventDisableTiming);
+  if (e != cudaSuccess) {
+    msx_batch_destroy(b);
+    return cuda_fail(e, "batch streams/events");
+  }
+  *out = b;
+  return MSX_OK;
+}
+
+int msx_batch_destroy(msx_batch* b) {
+  if (!b) return MSX_OK;
+  if (b->gexec) cudaGraphExecDestroy(b->gexec);
+  for (auto& br : b->plans)
+    for (auto& kv : br) msx_plan_destroy(kv.second);
+  for (auto s : b->streams)
+    if (s) cudaStreamDestroy(s);
+  for (auto ev : b->events)
+    if (ev) cudaEventDestroy(ev);
+  if (b->ev_in) cudaEventDestroy(b->ev_in);
+  if (b->ev_out) cudaEventDestroy(b->ev_out);
+  if (b->origin) cudaStreamDestroy(b->origin);
+  delete b;
+  return MSX_OK;
+}
+
+int msx_batch_set_schedule(msx_batch* b, int ny, int nx, int row_schedule, int col_schedule, int group) {
+  if (!b) return fail(MSX_ERR_INVALID, "null batch");
+  if (!msx_supported_size(ny) || !msx_supported_size(nx)) return fail(MSX_ERR_UNSUPPORTED, "grid %d x %d", ny, nx);
+  if (row_schedule < 0 || row_schedule >= msx_num_schedules(nx) || col_schedule < 0 ||
+      col_schedule >= msx_num_schedules(ny) || group < 0)
+    return fail(MSX_ERR_INVALID, "schedule (%d, %d, group %d) out of range", row_schedule, col_schedule, group);
+  const long long key = ((long long)ny << 32) | (unsigned)nx;
+  bool found = false;
+  for (auto& kv : b->sched)
+    if (kv.first == key) { kv.second = {row_schedule, col_schedule, group}; found = true; }
+  if (!found) b->sched.push_back({key, {row_schedule, col_schedule, group}});
+  for (auto& br : b->plans)
+    for (auto& kv : br)
+      if (kv.first == key) {
+        const int rc = msx_plan_set_schedule(kv.second, row_schedule, col_schedule, group);
+        if (rc != MSX_OK) return rc;
+      }
+  if (b->gexec) cudaGraphExecDestroy(b->gexec);
+  b->gexec = nullptr;
+  b->gkey.clear();
+  return MSX_OK;
+}
+
+int msx_batch_run(msx_batch* b, const msx_job* jobs, int njobs, void* stream) {
+  if (!b) return fail(MSX_ERR_INVALID, "null batch");
+  if (njobs < 0 || (njobs > 0 && !jobs)) return fail(MSX_ERR_INVALID, "bad job list");
+  if (njobs == 0) return MSX_OK;
+  int dev = 0;
+  MSX_CUDA(cudaGetDevice(&dev), "cudaGetDevice");
+  if (dev != b->device) return fail(MSX_ERR_INVALID, "batch belongs to device %d, current device is %d", b->device, dev);
+  for (int i = 0; i < njobs; ++i) {
+    const msx_job& j = jobs[i];
+    if (!msx_supported_size(j.ny) || !msx_supported_size(j.nx))
+      return fail(MSX_ERR_UNSUPPORTED, "job %d: grid %d x %d", i, j.ny, j.nx);
+    if (j.num_probes < 0 || j.num_slices < 0 || j.crop_y <= 0 || j.crop_x <= 0 || j.crop_y > j.ny || j.crop_x > j.nx)
+      return fail(MSX_ERR_INVALID, "job %d: bad probe/slice count or crop", i);
+    if (j.num_probes > 0 && (!j.psi_k_dev || !j.normalization_dev || !j.positions_dev || !j.cbed_out_dev ||
+                             (j.num_slices > 0 && !j.trans_dev)))
+      return fail(MSX_ERR_INVALID, "job %d: null pointer", i);
+    if (!(j.kmax > 0) || !(j.lambda > 0) || !(j.slice_t >= 0) || !(j.k_band >= 0))
+      return fail(MSX_ERR_INVALID, "job %d: kmax, lambda must be positive", i);
+  }
+  cudaStream_t caller = (cudaStream_t)stream;
+  std::vector<unsigned char> key(sizeof(msx_job) * (size_t)njobs);
+  std::memcpy(key.data(), jobs, key.size());
+  if (!b->gexec || key != b->gkey) {
+    if (b->gexec) cudaGraphExecDestroy(b->gexec);
+    b->gexec = nullptr;
+    b->gkey.clear();
+    // longest job first onto the least loaded branch
+    std::vector<int> order(njobs);
+    for (int i = 0; i < njobs; ++i) order[i] = i;
+    auto cost = [&](int i) {
+      const msx_job& j = jobs[i];
+      const double n = (double)j.ny * j.nx;
+      return (double)j.num_probes * (j.num_slices + 1) * n * std::log2(n);
+    };
+    std::sort(order.begin(), order.end(), [&](int x, int y) { return cost(x) > cost(y); });
+    std::vector<double> load(b->branches, 0.0);
+    std::vector<std::vector<int>> assign(b->branches);
+    for (int i : order) {
+      int best = 0;
+      for (int k = 1; k < b->branches; ++k)
+        if (load[k] < load[best]) best = k;
+      load[best] += cost(i);
+      assign[best].push_back(i);
+    }
+    // plans are created (allocating) before the capture
+    for (int k = 0; k < b->branches; ++k)
+      for (int i : assign[k]) {
+        int rc = MSX_OK;
+        if (!batch_plan(b, k, jobs[i].ny, jobs[i].nx, &rc)) return rc;
+      }
+    cudaGraph_t graph = nullptr;
+    MSX_CUDA(cudaStreamBeginCapture(b->origin, cudaStreamCaptureModeThreadLocal), "cudaStreamBeginCapture");
+    int rc = MSX_OK;
+    for (int k = 0; k < b->branches && rc == MSX_OK; ++k) {
+      cudaError_t e = cudaEventRecord(b->events[2 * k], b->origin);
+      if (e == cudaSuccess) e = cudaStreamWaitEvent(b->streams[k], b->events[2 * k], 0);
+      if (e != cudaSuccess) rc = cuda_fail(e, "batch fork");
+      for (int i : assign[k]) {
+        if (rc != MSX_OK) break;
+        const msx_job& j = jobs[i];
+        if (j.num_probes == 0) continue;
+        msx_plan* p = batch_plan(b, k, j.ny, j.nx, &rc);
+        MsArgs a;
+        std::memset(&a, 0, sizeof(a));
+        a.trans = j.trans_dev; a.num_slices = j.num_slices; a.psik = j.psi_k_dev; a.norm = j.normalization_dev;
+        a.pos = j.positions_dev; a.num_probes = j.num_probes; a.kmax = j.kmax; a.lambda = j.lambda;
+        a.slice_t = j.slice_t; a.k_band = j.k_band; a.cbed = j.cbed_out_dev; a.crop_y = j.crop_y; a.crop_x = j.crop_x;
+        a.group = p->group; a.row_sched = p->row_sched; a.col_sched = p->col_sched;
+        rc = enqueue_multislice(p, a, b->streams[k]);
+      }
+      if (rc == MSX_OK) {
+        e = cudaEventRecord(b->events[2 * k + 1], b->streams[k]);
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(b->origin, b->events[2 * k + 1], 0);
+        if (e != cudaSuccess) rc = cuda_fail(e, "batch join");
+      }
+    }
+    cudaError_t e = cudaStreamEndCapture(b->origin, &graph);
+    if (rc != MSX_OK) {
+      if (graph) cudaGraphDestroy(graph);
+      return rc;
+    }
+    if (e != cudaSuccess) return cuda_fail(e, "cudaStreamEndCapture");
+    e = cudaGraphInstantiate(&b->gexec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (e != cudaSuccess) {
+      b->gexec = nullptr;
+      return cuda_fail(e, "cudaGraphInstantiate");
+    }
+    b->gkey = key;
+  }
+  MSX_CUDA(cudaEventRecord(b->ev_in, caller), "cudaEventRecord");
+  MSX_CUDA(cudaStreamWaitEvent(b->origin, b->ev_in, 0), "cudaStreamWaitEvent");
+  MSX_CUDA(cudaGraphLaunch(b->gexec, b->origin), "cudaGraphLaunch");
+  MSX_CUDA(cudaEventRecord(b->ev_out, b->origin), "cudaEventRecord");
+  MSX_CUDA(cudaStreamWaitEvent(caller, b->ev_out, 0), "cudaStreamWaitEvent");
+  return MSX_OK;
+}
+
+int msx_batch_check(msx_batch* b) {
+  if (!b) return fail(MSX_ERR_INVALID, "null batch");
+  for (auto& br : b->plans)
+    for (auto& kv : br) {
+      const int rc = msx_plan_check(kv.second);
+      if (rc != MSX_OK) return rc;
+    }
+  return MSX_OK;
 }
 
 }  // extern "C"

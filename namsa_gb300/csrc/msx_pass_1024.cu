@@ -1,5 +1,5 @@
-// Multislice pass schedules for lines of length 1024 (kernels in msx_passes.cuh).
-#include "msx_passes.cuh"
+// Multislice pass schedules for lines of length 1024 (kernels in msx_passes.cuh and msx_tma.cuh).
+#include "msx_sched.cuh"
 
 namespace msx {
 int schedules_1024(const SchedOps** out) {

@@ -24,27 +24,27 @@ namespace msx {
 // A schedule fixes the line transform (threads per line T, radices) and the
 // launch shape for one line length N.  Several schedules exist per N; the
 // autotuner in the host library picks one per grid size.  COL_C columns share
-// a column-pass CTA (COL_C * T = 256 threads); MINB is the minimum number of
-// resident CTAs requested from the register allocator.
-constexpr int kThreads = 256;
-constexpr int kWarps = kThreads / 32;
-
+// a column-pass CTA, whose COL_C * T threads (256 or 512) are also the CTA size
+// of the row pass; MINB is the minimum number of resident CTAs requested from
+// the register allocator.
 template <int N_, int T_, int COL_C_, int MINB_, int... Rs>
 struct Sched {
   static constexpr int N = N_;
   static constexpr int T = T_;
   static constexpr int C = COL_C_;
   static constexpr int MINB = MINB_;
+  static constexpr int THREADS = COL_C_ * T_;        // CTA size of every pass of the schedule
+  static constexpr int WARPS = THREADS / 32;
   using FFT = LineFFT<N_, T_, Radices<Rs...>>;
   static constexpr int E = FFT::E;
   static constexpr int TW = FFT::tw_words();
   static constexpr int TW_PAD = (TW + 31) / 32 * 32;
   static constexpr int LPW = 32 / T;                 // row lines per warp
-  static constexpr int ROW_LINES = LPW * kWarps;     // row lines per CTA
+  static constexpr int ROW_LINES = LPW * WARPS;      // row lines per CTA
   static constexpr int ROW_LINE_WORDS = PaddedLine::words(N);
   static constexpr size_t row_smem() { return sizeof(float2) * (TW_PAD + (size_t)ROW_LINES * ROW_LINE_WORDS); }
   static constexpr size_t col_smem() { return sizeof(float2) * (TW_PAD + (size_t)C * N); }
-  static_assert(C * T == kThreads, "column CTA shape");
+  static_assert(THREADS == 256 || THREADS == 512, "CTA of 256 or 512 threads");
   static_assert(T <= 32 && 32 % T == 0, "a row line must live inside one warp");
 };
 
@@ -58,7 +58,7 @@ __device__ __forceinline__ void load_twiddles(float2* dst, const float2* __restr
 // Lines are ordered (y, p) with the wave index fastest so the waves of one CTA
 // share the transmission row.
 template <class S>
-__global__ void __launch_bounds__(kThreads, S::MINB)
+__global__ void __launch_bounds__(S::THREADS, S::MINB)
 row_pass_kernel(float2* __restrict__ psi, const float2* __restrict__ trans, const float2* __restrict__ tw_g,
                 int G, int Ny) {
   constexpr int NX = S::N;
@@ -106,7 +106,7 @@ struct ColArgs {
 };
 
 template <class S, int MODE>
-__global__ void __launch_bounds__(kThreads, S::MINB) col_pass_kernel(ColArgs a) {
+__global__ void __launch_bounds__(S::THREADS, S::MINB) col_pass_kernel(ColArgs a) {
   constexpr int NY = S::N;
   extern __shared__ float2 smem[];
   float2* tw = smem;
@@ -181,61 +181,5 @@ __global__ void __launch_bounds__(kThreads, S::MINB) col_pass_kernel(ColArgs a) 
     }
   }
 }
-
-// ---------------------------------------------------------------- launchers
-// Type-erased entry points of one schedule, collected by the host library.
-struct SchedOps {
-  int n;                      // line length
-  const char* name;
-  int tw_words;
-  void (*host_twiddles)(float2*);
-  cudaError_t (*configure)();
-  cudaError_t (*row)(float2* psi, const float2* trans, const float2* tw, int G, int Ny, cudaStream_t st);
-  cudaError_t (*col)(int mode, const ColArgs& a, cudaStream_t st);
-};
-
-template <class S> struct SchedImpl {
-  static void host_twiddles(float2* tw) { S::FFT::host_twiddles(tw); }
-  static cudaError_t configure() {
-    cudaError_t e = cudaFuncSetAttribute(row_pass_kernel<S>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)S::row_smem());
-    const int cs = (int)S::col_smem();
-    if (e == cudaSuccess) e = cudaFuncSetAttribute(col_pass_kernel<S, COL_INIT>, cudaFuncAttributeMaxDynamicSharedMemorySize, cs);
-    if (e == cudaSuccess) e = cudaFuncSetAttribute(col_pass_kernel<S, COL_MID>, cudaFuncAttributeMaxDynamicSharedMemorySize, cs);
-    if (e == cudaSuccess) e = cudaFuncSetAttribute(col_pass_kernel<S, COL_FINAL>, cudaFuncAttributeMaxDynamicSharedMemorySize, cs);
-    if (e == cudaSuccess) e = cudaFuncSetAttribute(col_pass_kernel<S, COL_INIT_FINAL>, cudaFuncAttributeMaxDynamicSharedMemorySize, cs);
-    return e;
-  }
-  static cudaError_t row(float2* psi, const float2* trans, const float2* tw, int G, int Ny, cudaStream_t st) {
-    const int lines = G * Ny;
-    const int blocks = (lines + S::ROW_LINES - 1) / S::ROW_LINES;
-    row_pass_kernel<S><<<blocks, kThreads, S::row_smem(), st>>>(psi, trans, tw, G, Ny);
-    return cudaGetLastError();
-  }
-  static cudaError_t col(int mode, const ColArgs& a, cudaStream_t st) {
-    const int tiles = (a.ncols + S::C - 1) / S::C;
-    const dim3 grid(tiles * a.G);
-    const size_t sm = S::col_smem();
-    switch (mode) {
-      case COL_INIT: col_pass_kernel<S, COL_INIT><<<grid, kThreads, sm, st>>>(a); break;
-      case COL_MID: col_pass_kernel<S, COL_MID><<<grid, kThreads, sm, st>>>(a); break;
-      case COL_FINAL: col_pass_kernel<S, COL_FINAL><<<grid, kThreads, sm, st>>>(a); break;
-      default: col_pass_kernel<S, COL_INIT_FINAL><<<grid, kThreads, sm, st>>>(a); break;
-    }
-    return cudaGetLastError();
-  }
-  static SchedOps ops(const char* name) {
-    return SchedOps{S::N, name, S::TW, &host_twiddles, &configure, &row, &col};
-  }
-};
-
-// Schedules compiled for each line length (one translation unit per length).
-int schedules_64(const SchedOps** out);
-int schedules_128(const SchedOps** out);
-int schedules_256(const SchedOps** out);
-int schedules_384(const SchedOps** out);
-int schedules_512(const SchedOps** out);
-int schedules_768(const SchedOps** out);
-int schedules_1024(const SchedOps** out);
 
 }  // namespace msx

@@ -11,70 +11,72 @@ namespace msx {
 // K0(x) = int_0^inf exp(-x cosh u) du (x > 0).  The integrand is analytic and
 // decays double-exponentially in the strip |Im u| < pi/2, so the trapezoidal
 // rule with step h converges like exp(-pi^2 / h); h = 1/8 leaves an error far
-// below double rounding for the arguments used here (x >= 0.1).
+// below double rounding for the arguments used here (x >= 0.1).  The sum stops
+// once a term falls below 1e-18 of the running sum.
 __device__ double bessel_k0(double x) {
   const double h = 0.125;
   double sum = 0.5 * exp(-x);
   for (int k = 1; k < 400; ++k) {
-    const double e = x * cosh(k * h);
-    if (e > 745.0) break;
-    sum += exp(-e);
+    const double term = exp(-x * cosh(k * h));
+    sum += term;
+    if (term < 1e-18 * sum) break;
   }
   return h * sum;
 }
 
 // ------------------------------------------------------------------ atom windows
-// One CTA per species.  Follows _get_potential (namsa/msa.py:180-196) and
-// bin_2d_array (namsa/utils.py:101-108): oversampled inclusive grid
+// Follows _get_potential (namsa/msa.py:180-196) and bin_2d_array
+// (namsa/utils.py:101-108): oversampled inclusive grid
 // x_i = -range/2 + i*range/(n-1), Kirkland sum
 //   v = 4 pi^2 a0 e sum_i a_i K0(2 pi r sqrt(b_i) + 0.1) + 2 pi^2 a0 e sum_i c_i/d_i exp(-pi^2 r^2/d_i)
-// with a0 = 0.529, e = 14.4, then the 2x2 (oversample^2) mean, minus the
-// window minimum, rounded to float32.  All arithmetic is double.
-__global__ void atom_window_kernel(const double* __restrict__ coeff, int n0, int n1, int os, double range,
-                                   float* __restrict__ out) {
-  extern __shared__ double sh[];  // h0*h1 binned values + reduction scratch
-  const int h0 = n0 / os, h1 = n1 / os;
-  const double* c = coeff + 12 * blockIdx.x;
+// with a0 = 0.529, e = 14.4, the oversample x oversample mean, minus the window
+// minimum, rounded to float32.  All arithmetic is double.
+//
+// Every Kirkland coefficient is positive, so v decreases with r and the
+// window minimum is the corner bin (each of its samples lies farther out than
+// the matching sample of any other bin); every CTA evaluates the corner bins
+// itself, which needs no grid-wide reduction.  Grid: (species, bin blocks).
+__device__ double window_bin(const double* c, int i, int j, int os, double sx, double sy, double start) {
   const double pi = 3.14159265358979323846;
   const double pre = 4.0 * pi * pi * 0.529 * 14.4;
-  const double start = -range / 2, sx = range / (double)(n0 - 1), sy = range / (double)(n1 - 1);
-  double* vals = sh;
-  double* red = sh + h0 * h1;
-  double local_min = 1e300;
-  for (int o = threadIdx.x; o < h0 * h1; o += blockDim.x) {
-    const int i = o / h1, j = o % h1;
-    double acc0 = 0;  // mean over the os x os block, in numpy's order: mean(-1) then mean(-2)
-    for (int a = 0; a < os; ++a) {
-      double accr = 0;
-      for (int b = 0; b < os; ++b) {
-        const double gx = (double)(i * os + a) * sx + start;
-        const double gy = (double)(j * os + b) * sy + start;
-        const double r = sqrt(gx * gx + gy * gy);
-        double v = 0;
-        for (int k = 0; k < 3; ++k) {
-          const double ak = c[k], bk = c[3 + k], ck = c[6 + k], dk = c[9 + k];
-          const double term = pre * ak * bessel_k0(2 * pi * r * sqrt(bk) + 0.1)
-                            + pre / 2. * ck / dk * exp(-pi * pi * r * r / dk);
-          v = (k == 0) ? term : v + term;
-        }
-        accr = (b == 0) ? v : accr + v;
+  double acc0 = 0;  // numpy's order: mean over the last axis, then over the second-to-last
+  for (int a = 0; a < os; ++a) {
+    double accr = 0;
+    for (int b = 0; b < os; ++b) {
+      const double gx = (double)(i * os + a) * sx + start;
+      const double gy = (double)(j * os + b) * sy + start;
+      const double r = sqrt(gx * gx + gy * gy);
+      double v = 0;
+      for (int k = 0; k < 3; ++k) {
+        const double ak = c[k], bk = c[3 + k], ck = c[6 + k], dk = c[9 + k];
+        const double term = pre * ak * bessel_k0(2 * pi * r * sqrt(bk) + 0.1) + pre / 2. * ck / dk * exp(-pi * pi * r * r / dk);
+        v = (k == 0) ? term : v + term;
       }
-      accr /= os;
-      acc0 = (a == 0) ? accr : acc0 + accr;
+      accr = (b == 0) ? v : accr + v;
     }
-    acc0 /= os;
-    vals[o] = acc0;
-    local_min = fmin(local_min, acc0);
+    accr /= os;
+    acc0 = (a == 0) ? accr : acc0 + accr;
   }
-  red[threadIdx.x] = local_min;
+  return acc0 / os;
+}
+
+__global__ void atom_window_kernel(const double* __restrict__ coeff, int n0, int n1, int os, double range,
+                                   float* __restrict__ out) {
+  __shared__ double corner[4];
+  const int h0 = n0 / os, h1 = n1 / os;
+  const double* c = coeff + 12 * blockIdx.x;
+  const double start = -range / 2, sx = range / (double)(n0 - 1), sy = range / (double)(n1 - 1);
+  if (threadIdx.x < 4) {
+    const int ci = (threadIdx.x & 1) ? h0 - 1 : 0, cj = (threadIdx.x & 2) ? h1 - 1 : 0;
+    corner[threadIdx.x] = window_bin(c, ci, cj, os, sx, sy, start);
+  }
   __syncthreads();
-  for (int s = blockDim.x / 2; s > 0; s >>= 1) {
-    if (threadIdx.x < s) red[threadIdx.x] = fmin(red[threadIdx.x], red[threadIdx.x + s]);
-    __syncthreads();
+  const double vmin = fmin(fmin(corner[0], corner[1]), fmin(corner[2], corner[3]));
+  const int o = blockIdx.y * blockDim.x + threadIdx.x;
+  if (o < h0 * h1) {
+    const double v = window_bin(c, o / h1, o % h1, os, sx, sy, start);
+    out[(size_t)blockIdx.x * h0 * h1 + o] = (float)(v - vmin);
   }
-  const double vmin = red[0];
-  float* o_ = out + (size_t)blockIdx.x * h0 * h1;
-  for (int o = threadIdx.x; o < h0 * h1; o += blockDim.x) o_[o] = (float)(vals[o] - vmin);
 }
 
 // ------------------------------------------------------------------ transmission slices
@@ -236,15 +238,56 @@ __global__ void ptab_kernel(int Ny, int Nx, float kmax, double lambda, double sl
   ptab[(size_t)y * Nx + x] = v;
 }
 
+// Separable propagator factors for the persistent column pass:
+// py[y] = exp(-i pi lambda t ky^2), px[x] = exp(-i pi lambda t kx^2) / N, and per
+// column x the band [lo, hi] of rows whose float32 |k| passes the mask test
+// (the same comparison as ptab_kernel).  |k| is monotone in |ky|, so the rows
+// that pass form one interval.
+__global__ void pfac_kernel(int Ny, int Nx, float kmax, double lambda, double slice_t, float k_band,
+                            float2* __restrict__ pyx, int2* __restrict__ band) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const double km = (double)kmax;
+  if (i < Ny) {
+    const double ky = __dsub_rn(__ddiv_rn(__dmul_rn((double)i, km), (double)(Ny - 1)), __ddiv_rn(km, 2.0));
+    double f = 0.5 * lambda * slice_t * ky * ky;
+    f -= rint(f);
+    float sn, cs;
+    sincospif(2.0f * (float)f, &sn, &cs);
+    pyx[i] = make_float2(cs, -sn);
+  }
+  if (i < Nx) {
+    const double kx = __dsub_rn(__ddiv_rn(__dmul_rn((double)i, km), (double)(Nx - 1)), __ddiv_rn(km, 2.0));
+    double f = 0.5 * lambda * slice_t * kx * kx;
+    f -= rint(f);
+    float sn, cs;
+    sincospif(2.0f * (float)f, &sn, &cs);
+    const float inv_n = (float)(1.0 / ((double)Ny * (double)Nx));
+    pyx[Ny + i] = make_float2(cs * inv_n, -sn * inv_n);
+    int lo = 1, hi = 0;
+    bool found = false;
+    for (int y = 0; y < Ny; ++y) {
+      if ((float)krad_exact(i, y, Nx, Ny, kmax) < k_band) {
+        if (!found) { lo = y; found = true; }
+        hi = y;
+      }
+    }
+    band[i] = make_int2(lo, hi);
+  }
+}
+
+cudaError_t launch_pfac(int Ny, int Nx, float kmax, double lambda, double slice_t, float k_band, float2* pyx,
+                        int2* band, cudaStream_t st) {
+  const int n = Ny > Nx ? Ny : Nx;
+  pfac_kernel<<<(n + 127) / 128, 128, 0, st>>>(Ny, Nx, kmax, lambda, slice_t, k_band, pyx, band);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_atom_windows(const double* coeff, int nspecies, int n0, int n1, int os, double range, float* out,
                                 cudaStream_t st) {
   const int h0 = n0 / os, h1 = n1 / os;
-  const int threads = 256;
-  const size_t smem = sizeof(double) * ((size_t)h0 * h1 + threads);
-  if (smem > 200 * 1024) return cudaErrorInvalidValue;
-  cudaError_t e = cudaFuncSetAttribute(atom_window_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  if (e != cudaSuccess) return e;
-  atom_window_kernel<<<nspecies, threads, smem, st>>>(coeff, n0, n1, os, range, out);
+  const int threads = 128;
+  const dim3 grid(nspecies, (h0 * h1 + threads - 1) / threads);
+  atom_window_kernel<<<grid, threads, 0, st>>>(coeff, n0, n1, os, range, out);
   return cudaGetLastError();
 }
 

@@ -1,0 +1,258 @@
+// Persistent, TMA-pipelined versions of the two per-slice passes.
+//
+// Each CTA loops over tiles (a group of rows, or a group of columns of one
+// wave).  While it transforms tile i out of one shared-memory stage, the bulk
+// copy engine (cp.async.bulk for rows, cp.async.bulk.tensor for column tiles)
+// fills the other stage with tile i+1; one mbarrier per stage tracks the
+// bytes in flight.  Results go straight from registers to global memory.
+//
+// The row pass exchanges Stockham stages in place inside the staged rows, with
+// an XOR swizzle of the element index (bits [S, S+4) folded into bits [0, 4))
+// that keeps the per-stage scatters free of bank conflicts.  The column pass
+// exchanges in the staged tile itself (columns interleaved element by
+// element), and forms the propagator on the fly from separable factors:
+//   P(kx, ky) mask(kx, ky) / N = px[kx] * py[ky]  for  lo[kx] <= ky <= hi[kx],  else 0,
+// where [lo, hi] is the band of the float32 mask comparison in column kx.
+//
+// Waits: only thread 0 polls an mbarrier, with a clock64 limit of about one
+// second; it publishes the outcome through shared memory and a CTA barrier,
+// so the whole CTA leaves together.  On a timeout the kernel sets bit 0 of
+// *err, waits (again bounded) for the other stage's copy if one was issued,
+// and returns.
+#pragma once
+#include <cuda.h>
+#include <cuda_runtime.h>
+
+#include "msx_passes.cuh"
+
+namespace msx {
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void fence_mbar_init() { asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory"); }
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+// Bounded wait: gives up after ~2^31 cycles (about one second at GB300 clocks).
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity) {
+  const long long t0 = clock64();
+  while (!mbar_try_wait(bar, parity)) {
+    if (clock64() - t0 > (1LL << 31)) return false;
+  }
+  return true;
+}
+__device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                   smem_u32(dst)),
+               "l"(src), "r"(bytes), "r"(smem_u32(bar))
+               : "memory");
+}
+__device__ __forceinline__ void tma2d_g2s(void* dst, const CUtensorMap* map, int x, int y, uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::"r"(
+          smem_u32(dst)),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(smem_u32(bar))
+      : "memory");
+}
+
+// Row line inside a staged, densely packed row: element i lives at
+// i ^ ((i >> SH) & 15).  SH = log2(elements per thread) makes the first
+// Stockham scatter (stride E) and the gathers (stride T) conflict-free.
+template <int SH>
+struct SwizzledLine {
+  float2* base;
+  __host__ __device__ __forceinline__ float2& operator[](int i) const { return base[i ^ ((i >> SH) & 15)]; }
+};
+
+__host__ __device__ constexpr int ilog2(int v) { return v <= 1 ? 0 : 1 + ilog2(v / 2); }
+
+struct TmaPassArgs {
+  float2* psi;            // (Galloc, Ny, Nx) workspace
+  const float2* trans;    // (Ny, Nx) transmission slice (row pass)
+  const float2* tw;       // twiddles of the line schedule
+  const float2* pyx;      // py[Ny] then px[Nx] (column pass)
+  const int2* band;       // [lo, hi] ky band per column (column pass)
+  int* err;               // bit 0: a bounded wait gave up
+  int G, Ny, Nx;
+};
+
+// ----------------------------------------------------------------------------- row pass
+template <class S>
+struct RowTma {
+  static constexpr int NX = S::N;
+  static constexpr int L = S::ROW_LINES;
+  static constexpr int STAGE = (L + 1) * NX;  // float2 words: L rows + the transmission row
+  static constexpr size_t smem() { return 16 + sizeof(float2) * ((size_t)2 * STAGE + S::TW_PAD); }
+};
+
+template <class S>
+__global__ void __launch_bounds__(S::THREADS, S::MINB) row_pass_tma_kernel(TmaPassArgs a) {
+  constexpr int NX = S::N, T = S::T, E = S::E, L = S::ROW_LINES, STAGE = RowTma<S>::STAGE;
+  extern __shared__ __align__(1024) float2 smem[];
+  float2* stage = smem;                                   // 2 stages
+  float2* tw = smem + 2 * STAGE;
+  uint64_t* bar = reinterpret_cast<uint64_t*>(tw + S::TW_PAD);
+  __shared__ int ok_flag;
+  const int tid = threadIdx.x;
+  for (int i = tid; i < S::TW; i += blockDim.x) tw[i] = a.tw[i];
+  if (tid == 0) {
+    mbar_init(&bar[0], 1);
+    mbar_init(&bar[1], 1);
+    fence_mbar_init();
+  }
+  __syncthreads();
+  const int pchunks = (a.G + L - 1) / L;
+  const int ntiles = a.Ny * pchunks;
+
+  auto issue = [&](int tile, int s) {
+    const int y = tile / pchunks, pc = tile - y * pchunks;
+    const int p0 = pc * L;
+    const int nl = min(L, a.G - p0);
+    float2* dst = stage + s * STAGE;
+    mbar_expect_tx(&bar[s], (uint32_t)((nl + 1) * NX * sizeof(float2)));
+    for (int i = 0; i < nl; ++i)
+      bulk_g2s(dst + i * NX, a.psi + ((size_t)(p0 + i) * a.Ny + y) * NX, NX * sizeof(float2), &bar[s]);
+    bulk_g2s(dst + L * NX, a.trans + (size_t)y * NX, NX * sizeof(float2), &bar[s]);
+  };
+
+  const int warp = tid >> 5, lane = tid & 31;
+  const int lw = lane / T, t = lane % T;
+  const int slot = warp * S::LPW + lw;  // line slot within a tile
+  int it = 0;
+  int pending = -1;  // stage of a load issued but not yet waited for
+  if (tid == 0 && blockIdx.x < ntiles) { issue(blockIdx.x, 0); pending = 0; }
+  for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x, ++it) {
+    const int s = it & 1;
+    const int next = tile + gridDim.x;
+    if (tid == 0) {
+      if (next < ntiles) { issue(next, s ^ 1); pending = s ^ 1; }
+      ok_flag = mbar_wait_bounded(&bar[s], (it >> 1) & 1) ? 1 : 0;
+      if (pending == s) pending = -1;
+      if (!ok_flag) {
+        atomicOr(a.err, 1);
+        if (pending >= 0) mbar_wait_bounded(&bar[pending], ((it + 1) >> 1) & 1);
+      }
+    }
+    __syncthreads();
+    if (!ok_flag) return;
+    const int y = tile / pchunks, pc = tile - y * pchunks;
+    const int p0 = pc * L;
+    const int nl = min(L, a.G - p0);
+    float2* line = stage + s * STAGE + slot * NX;
+    const float2* trow = stage + s * STAGE + L * NX;
+    SwizzledLine<ilog2(E)> buf{line};
+    float2 v[E];
+#pragma unroll
+    for (int m = 0; m < E; ++m) v[m] = line[t + T * m];
+    S::FFT::template run<true, false>(v, buf, tw, t);
+#pragma unroll
+    for (int m = 0; m < E; ++m) v[m] = cmul(v[m], trow[t + T * m]);
+    S::FFT::template run<false, false>(v, buf, tw, t);
+    if (slot < nl) {
+      float2* out = a.psi + ((size_t)(p0 + slot) * a.Ny + y) * NX;
+#pragma unroll
+      for (int m = 0; m < E; ++m) out[t + T * m] = v[m];
+    }
+    fence_proxy_async();  // this stage is refilled by the copy engine two tiles later
+    __syncthreads();
+  }
+}
+
+// ----------------------------------------------------------------------------- column pass
+template <class S>
+struct ColTma {
+  static constexpr int NY = S::N;
+  static constexpr int C = S::C;
+  static constexpr int BOXR = NY < 128 ? NY : 128;  // rows per tensor-map box
+  static constexpr int NBOX = NY / BOXR;
+  static constexpr int STAGE = C * NY;
+  static constexpr size_t smem() { return 16 + sizeof(float2) * ((size_t)2 * STAGE + S::TW_PAD + NY); }
+};
+
+template <class S>
+__global__ void __launch_bounds__(S::THREADS, S::MINB) col_mid_tma_kernel(const __grid_constant__ CUtensorMap map,
+                                                                        TmaPassArgs a) {
+  constexpr int NY = S::N, T = S::T, E = S::E, C = S::C;
+  constexpr int BOXR = ColTma<S>::BOXR, NBOX = ColTma<S>::NBOX, STAGE = ColTma<S>::STAGE;
+  extern __shared__ __align__(1024) float2 smem[];
+  float2* stage = smem;
+  float2* tw = smem + 2 * STAGE;
+  float2* py = tw + S::TW_PAD;
+  uint64_t* bar = reinterpret_cast<uint64_t*>(py + NY);
+  __shared__ int ok_flag;
+  const int tid = threadIdx.x;
+  for (int i = tid; i < S::TW; i += blockDim.x) tw[i] = a.tw[i];
+  for (int i = tid; i < NY; i += blockDim.x) py[i] = a.pyx[i];
+  if (tid == 0) {
+    mbar_init(&bar[0], 1);
+    mbar_init(&bar[1], 1);
+    fence_mbar_init();
+  }
+  __syncthreads();
+  const int tiles_x = a.Nx / C;
+  const int ntiles = tiles_x * a.G;
+
+  auto issue = [&](int tile, int s) {
+    const int p = tile % a.G, xt = tile / a.G;
+    float2* dst = stage + s * STAGE;
+    mbar_expect_tx(&bar[s], (uint32_t)(STAGE * sizeof(float2)));
+#pragma unroll
+    for (int b = 0; b < NBOX; ++b) tma2d_g2s(dst + b * BOXR * C, &map, xt * C, p * NY + b * BOXR, &bar[s]);
+  };
+
+  const int c = tid % C, t = tid / C;
+  int it = 0;
+  int pending = -1;
+  if (tid == 0 && blockIdx.x < ntiles) { issue(blockIdx.x, 0); pending = 0; }
+  for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x, ++it) {
+    const int s = it & 1;
+    const int next = tile + gridDim.x;
+    if (tid == 0) {
+      if (next < ntiles) { issue(next, s ^ 1); pending = s ^ 1; }
+      ok_flag = mbar_wait_bounded(&bar[s], (it >> 1) & 1) ? 1 : 0;
+      if (pending == s) pending = -1;
+      if (!ok_flag) {
+        atomicOr(a.err, 1);
+        if (pending >= 0) mbar_wait_bounded(&bar[pending], ((it + 1) >> 1) & 1);
+      }
+    }
+    __syncthreads();
+    if (!ok_flag) return;
+    const int p = tile % a.G, xt = tile / a.G;
+    const int x = xt * C + c;
+    const float2 px = __ldg(a.pyx + NY + x);  // issued early: consumed after the forward transform
+    const int2 bd = __ldg(a.band + x);
+    InterleavedLine<C> buf{stage + s * STAGE + c};
+    float2 v[E];
+#pragma unroll
+    for (int m = 0; m < E; ++m) v[m] = buf[t + T * m];
+    S::FFT::template run<false, true>(v, buf, tw, t);
+#pragma unroll
+    for (int m = 0; m < E; ++m) {
+      const int ky = t + T * m;
+      const float2 f = (ky >= bd.x && ky <= bd.y) ? cmul(px, py[ky]) : make_float2(0.f, 0.f);
+      v[m] = cmul(v[m], f);
+    }
+    S::FFT::template run<true, true>(v, buf, tw, t);
+    float2* col = a.psi + (size_t)p * NY * a.Nx + x;
+#pragma unroll
+    for (int m = 0; m < E; ++m) col[(t + T * m) * a.Nx] = v[m];
+    fence_proxy_async();
+    __syncthreads();
+  }
+}
+
+}  // namespace msx

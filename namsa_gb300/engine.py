@@ -142,6 +142,14 @@ class Plan:
     def set_graph(self, enable):
         _lib.check(lib().msx_plan_set_graph(self.handle, int(bool(enable))))
 
+    def set_tma(self, enable):
+        """Persistent TMA-pipelined passes (default) or the plain one-CTA-per-tile passes."""
+        _lib.check(lib().msx_plan_set_tma(self.handle, int(bool(enable))))
+
+    def check(self):
+        """Synchronise and raise MsxError(MSX_ERR_TIMEOUT) if a pipelined pass gave up waiting."""
+        _lib.check(lib().msx_plan_check(self.handle))
+
     def multislice(self, trans, psik, norm, positions, kmax, lam, slice_t, k_band, crop=None, out=None):
         """CBED stack (P, crop_y, crop_x) float32 for positions (P, 2) [y, x] float32.
 
@@ -190,3 +198,51 @@ class Plan:
                                            float(k_band), int(iters), int(max_workspace_bytes), ctypes.byref(best),
                                            _stream()))
         return self.schedule, float(best.value)
+
+
+class Batch:
+    """Uneven batch of multislice jobs run as one CUDA graph over parallel branches."""
+
+    def __init__(self, branches=0):
+        h = _vp()
+        _lib.check(lib().msx_batch_create(int(branches), ctypes.byref(h)))
+        self._h = h
+        self._keep = []
+
+    def close(self):
+        if getattr(self, '_h', None) is not None:
+            lib().msx_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_schedule(self, ny, nx, row, col, group=0):
+        _lib.check(lib().msx_batch_set_schedule(self._h, int(ny), int(nx), int(row), int(col), int(group)))
+
+    def run(self, jobs):
+        """jobs: list of dicts with keys trans, psik, norm, positions, kmax, lam, slice_t,
+        k_band, out (CUDA tensors / numbers as for Plan.multislice).  Returns the outs."""
+        arr = (_lib.MsxJob * len(jobs))()
+        for j, d in zip(arr, jobs):
+            _need(d['trans'], torch.complex64, 'trans', 3)
+            _need(d['psik'], torch.complex64, 'psi_k', 2)
+            _need(d['norm'], torch.float64, 'normalization', 1)
+            _need(d['positions'], torch.float32, 'positions', 2)
+            _need(d['out'], torch.float32, 'out', 3)
+            S, ny, nx = d['trans'].shape
+            j.ny, j.nx, j.num_slices, j.num_probes = ny, nx, S, d['positions'].shape[0]
+            j.crop_y, j.crop_x = d['out'].shape[1], d['out'].shape[2]
+            j.kmax, j.k_band, j.lambda_, j.slice_t = float(d['kmax']), float(d['k_band']), float(d['lam']), float(d['slice_t'])
+            j.trans_dev, j.psi_k_dev = d['trans'].data_ptr(), d['psik'].data_ptr()
+            j.normalization_dev, j.positions_dev = d['norm'].data_ptr(), d['positions'].data_ptr()
+            j.cbed_out_dev = d['out'].data_ptr()
+        _lib.check(lib().msx_batch_run(self._h, ctypes.cast(arr, _vp), len(jobs), _stream()))
+        self._keep = jobs  # the graph refers to these buffers until the next run
+        return [d['out'] for d in jobs]
+
+    def check(self):
+        _lib.check(lib().msx_batch_check(self._h))

@@ -30,17 +30,20 @@ def crystal_geom(sc, energy, semi, n):
     return O.Geometry(xyz, sc['atomic_number'], energy, semi, n)
 
 
-def engine_cbed(trans, psik, norm, pos, kmax, lam, slice_t, bandwidth, crop=None, group=0, sched=(0, 0), graph=True):
+def engine_cbed(trans, psik, norm, pos, kmax, lam, slice_t, bandwidth, crop=None, group=0, sched=(0, 0), graph=True,
+                tma=True):
     ny, nx = psik.shape
     plan = engine.Plan(ny, nx, group)
     plan.set_schedule(sched[0], sched[1])
     plan.set_graph(graph)
+    plan.set_tma(tma)
     out = plan.multislice(torch.from_numpy(np.ascontiguousarray(trans.astype(np.complex64))).to(DEV),
                           torch.from_numpy(np.ascontiguousarray(psik.astype(np.complex64))).to(DEV),
                           torch.tensor([norm], dtype=torch.float64, device=DEV),
                           torch.from_numpy(np.ascontiguousarray(pos.astype(np.float32))).to(DEV),
                           np.float32(kmax), lam, slice_t, np.float32(bandwidth * kmax), crop=crop)
     res = out.cpu().numpy()
+    plan.check()
     plan.close()
     return res
 
@@ -120,9 +123,10 @@ def test_multislice_every_size_and_schedule(n):
     g, trans, psik, norm, pos, kmax, lam, st = random_case(n, n, S=3, P=3, seed=n)
     ref = oracle_cbed(g, trans, psik, norm, pos, st, 1 / 3)
     for k in range(len(engine.schedules(n))):
-        got = engine_cbed(trans, psik, norm, pos, kmax, lam, st, 1 / 3, sched=(k, k))
-        err = O.rel_l2(got, ref)
-        assert err.max() < 2e-5, (n, k, err)
+        for tma in (True, False):
+            got = engine_cbed(trans, psik, norm, pos, kmax, lam, st, 1 / 3, sched=(k, k), tma=tma)
+            err = O.rel_l2(got, ref)
+            assert err.max() < 2e-5, (n, k, tma, err)
 
 
 @pytest.mark.parametrize('ny,nx', [(256, 512), (384, 768), (128, 64)])
@@ -139,10 +143,13 @@ def test_groups_crop_graph_determinism():
     a = engine_cbed(trans, psik, norm, pos, kmax, lam, st, 0.4, crop=64, group=3)
     b = engine_cbed(trans, psik, norm, pos, kmax, lam, st, 0.4, crop=64, group=3, graph=False)
     c = engine_cbed(trans, psik, norm, pos, kmax, lam, st, 0.4, crop=64, group=7)
+    d = engine_cbed(trans, psik, norm, pos, kmax, lam, st, 0.4, crop=64, group=7, tma=False)
+    e = engine_cbed(trans, psik, norm, pos, kmax, lam, st, 0.4, crop=64, group=3, tma=False)
     assert a.shape == (7, 64, 64)
-    assert O.rel_l2(a, ref).max() < 2e-5
+    assert O.rel_l2(a, ref).max() < 2e-5 and O.rel_l2(d, ref).max() < 2e-5
     np.testing.assert_array_equal(a, b)
     np.testing.assert_array_equal(a, c)
+    np.testing.assert_array_equal(d, e)
 
 
 def test_zero_slices_and_single_probe():
