@@ -175,6 +175,20 @@ MSX_API int msx_multislice(msx_plan* plan, const float* trans_dev, int num_slice
                    void* stream);
 
 /*
+ * Annular (or any) detector signals fused into the last pass instead of CBED
+ * stacks: signals_out[p][d] = sum_k I_p(k) w_d(k), with I_p the CBED pattern of
+ * msx_multislice (full grid, natural FFT order) and w_d the weights
+ * detectors_dev[d] (num_detectors, ny, nx) float32, 1 <= num_detectors <= 8.
+ * Replaces MSA.integrate_cbed (namsa/msa.py:426-439), which integrates an
+ * already stored CBED stack on the host.  num_slices must be >= 1.
+ * Launched directly (no graph).
+ */
+MSX_API int msx_multislice_detect(msx_plan* plan, const float* trans_dev, int num_slices, const float* psi_k_dev,
+                                  const double* normalization_dev, const float* positions_dev, int num_probes,
+                                  float kmax, double lambda, double slice_t, float k_band, const float* detectors_dev,
+                                  int num_detectors, float* signals_out_dev, void* stream);
+
+/*
  * msx_multislice without any device allocation, for callers that cannot call
  * cudaMalloc: applications whose device memory is entirely owned by their own
  * pool or allocator, plugin hosts that forbid allocation inside their callbacks,

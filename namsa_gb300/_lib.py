@@ -42,6 +42,8 @@ SIGNATURES = [
     ('msx_plan_check', _c.c_int, [_vp]),
     ('msx_multislice', _c.c_int, [_vp, _vp, _c.c_int, _vp, _vp, _vp, _c.c_int, _c.c_float, _c.c_double,
                                   _c.c_double, _c.c_float, _vp, _c.c_int, _c.c_int, _vp]),
+    ('msx_multislice_detect', _c.c_int, [_vp, _vp, _c.c_int, _vp, _vp, _vp, _c.c_int, _c.c_float, _c.c_double,
+                                         _c.c_double, _c.c_float, _vp, _c.c_int, _vp, _vp]),
     ('msx_multislice_noalloc', _c.c_int, [_vp, _c.c_int, _vp, _vp, _vp, _c.c_int, _c.c_int, _c.c_int, _c.c_float,
                                           _c.c_double, _c.c_double, _c.c_float, _vp, _c.c_int, _c.c_int, _vp]),
     ('msx_batch_create', _c.c_int, [_c.c_int, _c.POINTER(_vp)]),

@@ -104,6 +104,8 @@ struct msx_plan {
   CUtensorMap map{};             // workspace as (psi_waves*ny) x nx 8-byte elements, box col_c x col_boxr
   bool map_ok = false;
   int row_ctas = 0, col_ctas = 0;
+  float* partial = nullptr;      // detector partial sums
+  size_t partial_words = 0;
 };
 
 namespace {
@@ -192,6 +194,7 @@ struct MsArgs {
   const float* trans; int num_slices; const float* psik; const double* norm; const float* pos; int num_probes;
   float kmax; double lambda, slice_t; float k_band; float* cbed; int crop_y, crop_x;
   int group, row_sched, col_sched;
+  const float* det; int ndet; float* signals;  // detector mode (det != nullptr): signals (P, ndet) instead of cbed
 };
 
 // One slice's row pass and (mid) column pass over a group of gn waves.
@@ -249,9 +252,18 @@ int enqueue_multislice(msx_plan* p, const MsArgs& a, cudaStream_t st) {
       if (rc != MSX_OK) return rc;
       if (s + 1 == a.num_slices) {
         ColArgs f = c;
-        f.x_begin = x0;
-        f.ncols = a.crop_x;
-        MSX_CUDA(p->col_ops->col(COL_FINAL, f, st), "final column pass");
+        if (a.det) {
+          f.det = a.det;
+          f.ndet = a.ndet;
+          f.partial = p->partial;
+          MSX_CUDA(p->col_ops->col(COL_DETECT, f, st), "detector pass");
+          MSX_CUDA(launch_detect_reduce(p->partial, gn, nx / p->col_ops->col_c, a.ndet,
+                                        a.signals + (size_t)g0 * a.ndet, st), "detector reduction");
+        } else {
+          f.x_begin = x0;
+          f.ncols = a.crop_x;
+          MSX_CUDA(p->col_ops->col(COL_FINAL, f, st), "final column pass");
+        }
       }
     }
   }
@@ -379,6 +391,7 @@ int msx_plan_destroy(msx_plan* p) {
   if (p->pyx) cudaFree(p->pyx);
   if (p->band) cudaFree(p->band);
   if (p->err) cudaFree(p->err);
+  if (p->partial) cudaFree(p->partial);
   if (p->tw_row) cudaFree(p->tw_row);
   if (p->tw_col) cudaFree(p->tw_col);
   if (p->ev_in) cudaEventDestroy(p->ev_in);
@@ -508,6 +521,38 @@ int msx_multislice(msx_plan* p, const float* trans_dev, int num_slices, const fl
   MSX_CUDA(cudaEventRecord(p->ev_out, p->work), "cudaEventRecord");
   MSX_CUDA(cudaStreamWaitEvent(caller, p->ev_out, 0), "cudaStreamWaitEvent");
   return MSX_OK;
+}
+
+int msx_multislice_detect(msx_plan* p, const float* trans_dev, int num_slices, const float* psi_k_dev,
+                          const double* normalization_dev, const float* positions_dev, int num_probes, float kmax,
+                          double lambda, double slice_t, float k_band, const float* detectors_dev, int num_detectors,
+                          float* signals_out_dev, void* stream) {
+  if (!p) return fail(MSX_ERR_INVALID, "null plan");
+  if (num_probes < 0 || num_slices < 1) return fail(MSX_ERR_INVALID, "detector mode needs num_slices >= 1");
+  if (num_probes == 0) return MSX_OK;
+  if (num_detectors < 1 || num_detectors > kMaxDetectors)
+    return fail(MSX_ERR_INVALID, "1..%d detectors supported, got %d", kMaxDetectors, num_detectors);
+  if (!trans_dev || !psi_k_dev || !normalization_dev || !positions_dev || !detectors_dev || !signals_out_dev)
+    return fail(MSX_ERR_INVALID, "null pointer");
+  if (!(kmax > 0) || !(lambda > 0) || !(slice_t >= 0) || !(k_band >= 0))
+    return fail(MSX_ERR_INVALID, "kmax, lambda must be positive; slice thickness and k_band non-negative");
+  const size_t need = (size_t)p->group * (p->nx / p->col_ops->col_c) * num_detectors;
+  if (need > p->partial_words) {
+    if (p->partial) cudaFree(p->partial);
+    p->partial = nullptr;
+    p->partial_words = 0;
+    if (cudaMalloc(&p->partial, need * sizeof(float)) != cudaSuccess)
+      return fail(MSX_ERR_ALLOC, "detector partial sums allocation failed");
+    p->partial_words = need;
+  }
+  MsArgs a;
+  std::memset(&a, 0, sizeof(a));
+  a.trans = trans_dev; a.num_slices = num_slices; a.psik = psi_k_dev; a.norm = normalization_dev;
+  a.pos = positions_dev; a.num_probes = num_probes; a.kmax = kmax; a.lambda = lambda; a.slice_t = slice_t;
+  a.k_band = k_band; a.crop_y = p->ny; a.crop_x = p->nx; a.group = p->group; a.row_sched = p->row_sched;
+  a.col_sched = p->col_sched; a.det = detectors_dev; a.ndet = num_detectors; a.signals = signals_out_dev;
+  drop_graph(p);  // the detector sequence is launched directly
+  return enqueue_multislice(p, a, (cudaStream_t)stream);
 }
 
 int msx_plan_profile(msx_plan* p, const float* trans_dev, int num_slices, const float* psi_k_dev,
@@ -679,8 +724,9 @@ msx_plan* batch_plan(msx_batch* b, int branch, int ny, int nx, int* rc) {
   const long long key = ((long long)ny << 32) | (unsigned)nx;
   for (auto& kv : b->plans[branch])
     if (kv.first == key) return kv.second;
-  // resident group per branch: the branches share about 96 MiB of L2-resident waves
-  int group = (int)(((size_t)96 << 20) / ((size_t)b->branches * sizeof(float2) * ny * nx));
+  // Persistent passes amortise their start-up over large groups: up to 512 MiB
+  // of waves per branch (the jobs of a branch run one after another).
+  int group = (int)(((size_t)512 << 20) / (sizeof(float2) * (size_t)ny * nx));
   if (group < 2) group = 2;
   int r = 0, c = 0;
   for (auto& kv : b->sched)

@@ -15,6 +15,7 @@ cudaError_t launch_probe(int Ny, int Nx, float kmax, double lambda, float k_semi
 // Sets the message returned by msx_last_error for the calling thread.
 void set_last_error(const char* msg);
 
+cudaError_t launch_detect_reduce(const float* partial, int G, int tiles, int ndet, float* out, cudaStream_t st);
 cudaError_t launch_pfac(int Ny, int Nx, float kmax, double lambda, double slice_t, float k_band, float2* pyx,
                         int2* band, cudaStream_t st);
 cudaError_t launch_ptab(int Ny, int Nx, float kmax, double lambda, double slice_t, float k_band, float2* ptab,

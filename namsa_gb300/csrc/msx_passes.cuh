@@ -89,7 +89,8 @@ row_pass_kernel(float2* __restrict__ psi, const float2* __restrict__ trans, cons
 }
 
 // ---------------------------------------------------------------- column passes
-enum ColMode { COL_INIT = 0, COL_MID = 1, COL_FINAL = 2, COL_INIT_FINAL = 3 };
+enum ColMode { COL_INIT = 0, COL_MID = 1, COL_FINAL = 2, COL_INIT_FINAL = 3, COL_DETECT = 4 };
+constexpr int kMaxDetectors = 8;
 
 struct ColArgs {
   float2* psi;             // (G, Ny, Nx) group workspace
@@ -103,6 +104,9 @@ struct ColArgs {
   int x_begin, ncols;      // columns handled: x_begin .. x_begin + ncols - 1
   int y0, crop_y;          // output rows y0 .. y0 + crop_y - 1 (final)
   float kmax;              // k-grid extent (float32 like the reference)
+  const float* det;        // (ndet, Ny, Nx) detector weights over the CBED grid (detect)
+  int ndet;
+  float* partial;          // (G, Nx / C, ndet) per-tile detector sums (detect)
 };
 
 template <class S, int MODE>
@@ -155,14 +159,44 @@ __global__ void __launch_bounds__(S::THREADS, S::MINB) col_pass_kernel(ColArgs a
 #pragma unroll
     for (int m = 0; m < S::E; ++m) v[m] = cmul(v[m], __ldg(pcol + (t + S::T * m) * Nx));
     S::FFT::template run<true, true>(v, buf, tw, t);
-  } else if constexpr (MODE == COL_FINAL) {
+  } else if constexpr (MODE == COL_FINAL || MODE == COL_DETECT) {
     S::FFT::template run<false, true>(v, buf, tw, t);
 #pragma unroll
     for (int m = 0; m < S::E; ++m) v[m] = cmul(v[m], __ldg(pcol + (t + S::T * m) * Nx));
   }
   // COL_INIT_FINAL (no slices): fft2(ifft2_u(Y)) = N*Y, so v already holds Y.
 
-  if constexpr (MODE == COL_FINAL || MODE == COL_INIT_FINAL) {
+  if constexpr (MODE == COL_DETECT) {
+    // Integrated detector signals (MSA.integrate_cbed, namsa/msa.py:426-439) of
+    // this CTA's columns: sum_k I(k) w_d(k), reduced in a fixed order.
+    const double ntot = (double)NY * (double)a.Nx;
+    const float scale = (float)(ntot / *a.norm);
+    float acc[kMaxDetectors];
+#pragma unroll
+    for (int d = 0; d < kMaxDetectors; ++d) acc[d] = 0.f;
+#pragma unroll
+    for (int m = 0; m < S::E; ++m) {
+      const float inten = fmaf(v[m].x, v[m].x, v[m].y * v[m].y) * scale;
+      const int ky = t + S::T * m;
+#pragma unroll
+      for (int d = 0; d < kMaxDetectors; ++d)
+        if (d < a.ndet && valid) acc[d] = fmaf(inten, __ldg(a.det + ((size_t)d * NY + ky) * Nx + x), acc[d]);
+    }
+    __syncthreads();  // the exchange buffer is reused for the reduction
+    float* red = reinterpret_cast<float*>(smem + S::TW_PAD);
+#pragma unroll
+    for (int d = 0; d < kMaxDetectors; ++d) {
+      if (d >= a.ndet) break;
+      red[threadIdx.x] = acc[d];
+      __syncthreads();
+      for (int sh = S::THREADS / 2; sh > 0; sh >>= 1) {
+        if ((int)threadIdx.x < sh) red[threadIdx.x] += red[threadIdx.x + sh];
+        __syncthreads();
+      }
+      if (threadIdx.x == 0) a.partial[((size_t)p * (a.ncols / S::C) + tile) * a.ndet + d] = red[0];
+      __syncthreads();
+    }
+  } else if constexpr (MODE == COL_FINAL || MODE == COL_INIT_FINAL) {
     const double ntot = (double)NY * (double)a.Nx;
     // COL_FINAL: I = N |P/N * fft2_u(psi t)|^2 / norm ; COL_INIT_FINAL: I = N |Y|^2 / norm
     const float scale = (float)(ntot / *a.norm);

@@ -36,6 +36,7 @@ template <class S> struct SchedImpl {
     if (e == cudaSuccess) e = cudaFuncSetAttribute(col_pass_kernel<S, COL_MID>, cudaFuncAttributeMaxDynamicSharedMemorySize, cs);
     if (e == cudaSuccess) e = cudaFuncSetAttribute(col_pass_kernel<S, COL_FINAL>, cudaFuncAttributeMaxDynamicSharedMemorySize, cs);
     if (e == cudaSuccess) e = cudaFuncSetAttribute(col_pass_kernel<S, COL_INIT_FINAL>, cudaFuncAttributeMaxDynamicSharedMemorySize, cs);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(col_pass_kernel<S, COL_DETECT>, cudaFuncAttributeMaxDynamicSharedMemorySize, cs);
     if (e == cudaSuccess) e = cudaFuncSetAttribute(row_pass_tma_kernel<S>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)RowTma<S>::smem());
     if (e == cudaSuccess) e = cudaFuncSetAttribute(col_mid_tma_kernel<S>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ColTma<S>::smem());
     return e;
@@ -54,6 +55,7 @@ template <class S> struct SchedImpl {
       case COL_INIT: col_pass_kernel<S, COL_INIT><<<grid, S::THREADS, sm, st>>>(a); break;
       case COL_MID: col_pass_kernel<S, COL_MID><<<grid, S::THREADS, sm, st>>>(a); break;
       case COL_FINAL: col_pass_kernel<S, COL_FINAL><<<grid, S::THREADS, sm, st>>>(a); break;
+      case COL_DETECT: col_pass_kernel<S, COL_DETECT><<<grid, S::THREADS, sm, st>>>(a); break;
       default: col_pass_kernel<S, COL_INIT_FINAL><<<grid, S::THREADS, sm, st>>>(a); break;
     }
     return cudaGetLastError();

@@ -282,6 +282,24 @@ cudaError_t launch_pfac(int Ny, int Nx, float kmax, double lambda, double slice_
   return cudaGetLastError();
 }
 
+// Detector signals: out[p][d] = sum over column tiles of partial[p][tile][d],
+// in tile order (deterministic).
+__global__ void detect_reduce_kernel(const float* __restrict__ partial, int G, int tiles, int ndet,
+                                     float* __restrict__ out) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= G * ndet) return;
+  const int p = i / ndet, d = i % ndet;
+  float s = 0.f;
+  for (int k = 0; k < tiles; ++k) s += partial[((size_t)p * tiles + k) * ndet + d];
+  out[i] = s;
+}
+
+cudaError_t launch_detect_reduce(const float* partial, int G, int tiles, int ndet, float* out, cudaStream_t st) {
+  const int n = G * ndet;
+  detect_reduce_kernel<<<(n + 127) / 128, 128, 0, st>>>(partial, G, tiles, ndet, out);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_atom_windows(const double* coeff, int nspecies, int n0, int n1, int os, double range, float* out,
                                 cudaStream_t st) {
   const int h0 = n0 / os, h1 = n1 / os;

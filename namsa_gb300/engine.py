@@ -177,6 +177,20 @@ class Plan:
                                         int(cy), int(cx), _stream()))
         return out
 
+    def detect(self, trans, psik, norm, positions, kmax, lam, slice_t, k_band, detectors, out=None):
+        """Detector signals (P, ndet) float32: sum over each CBED pattern weighted by
+        detectors (ndet, ny, nx) float32, fused into the last pass."""
+        _need(trans, torch.complex64, 'trans', 3)
+        _need(detectors, torch.float32, 'detectors', 3)
+        P = positions.shape[0]
+        nd = detectors.shape[0]
+        if out is None:
+            out = torch.empty((P, nd), dtype=torch.float32, device=trans.device)
+        _lib.check(lib().msx_multislice_detect(self.handle, _ptr(trans), trans.shape[0], _ptr(psik), _ptr(norm),
+                                               _ptr(positions), P, float(kmax), float(lam), float(slice_t),
+                                               float(k_band), _ptr(detectors), nd, _ptr(out), _stream()))
+        return out
+
     def profile(self, trans, psik, norm, positions, kmax, lam, slice_t, k_band, iters=20):
         """Mean duration (ms) of one row pass and one column pass over the plan's
         first group, timed with CUDA events on the current stream; also returns

@@ -240,3 +240,20 @@ def test_config2_scan_sampled_vs_fp64():
     ref = O.multislice_gpu(tr, psik, P, sim.probe_positions[pick], norm, geom, crop=256)
     err = O.rel_l2(got[pick], ref)
     assert err.max() < 1e-4, err
+
+
+def test_detector_signals_match_cbed_sums():
+    """Fused detector epilogue (msx_multislice_detect) against the CBED stack
+    summed with the same weights in float64 (MSA.integrate_cbed, msa.py:426-439)."""
+    g, trans, psik, norm, pos, kmax, lam, st = random_case(256, 256, S=4, P=5, seed=21)
+    cbed = engine_cbed(trans, psik, norm, pos, kmax, lam, st, 0.45)
+    det = np.stack([M.annular_detector(np.array([256, 256]), np.array([kmax, kmax]) / 256, lam, a, b)
+                    for a, b in [(0.02, 0.05), (0.05, 0.09), (0.0, 0.02)]]).astype(np.float32)
+    ref = np.einsum('pyx,dyx->pd', cbed.astype(np.float64), det.astype(np.float64))
+    plan = engine.Plan(256, 256, 2)
+    sig = plan.detect(torch.from_numpy(trans).to(DEV), torch.from_numpy(psik).to(DEV),
+                      torch.tensor([norm], dtype=torch.float64, device=DEV), torch.from_numpy(pos).to(DEV),
+                      np.float32(kmax), lam, st, np.float32(0.45 * kmax), torch.from_numpy(det).to(DEV)).cpu().numpy()
+    plan.close()
+    assert sig.shape == (5, 3)
+    assert np.abs(sig - ref).max() <= 2e-5 * np.abs(ref).max()
