@@ -215,6 +215,40 @@ MSX_API int msx_multislice_noalloc(const float* trans_dev, int num_slices, const
                                    float* cbed_out_dev, int crop_y, int crop_x, void* stream);
 
 /*
+ * Dataset post-processing of the reference's production runs
+ * (scripts/summit_scripts/utils.py:74-118), on the device.
+ *
+ * msx_process_cbed: out[p] = (cbed[p] - mean_p) / std_p (population std) as
+ * IEEE float16, for num_patterns patterns of height x width float32
+ * (process_cbed, utils.py:102-118).
+ *
+ * msx_process_potential: the projected-potential label of a transmission stack
+ * (num_slices, ny, nx) complex64: mean over slices of Im t, Gaussian filter
+ * (sigma 1.2, 11 taps, half-sample reflecting borders, like
+ * scipy.ndimage.gaussian_filter), the central crop rows and columns
+ * [ny/4, 3*nx/4) (the reference applies one slice to both axes), then
+ * (x - mean) / max(std, 1/sqrt(size)) as float16 (process_potential,
+ * utils.py:74-100).  work_dev: 2*ny*nx + 22 floats of caller scratch (8-byte
+ * aligned).  out: (3*nx/4 - ny/4)^2 halves.
+ */
+MSX_API int msx_process_cbed(const float* cbed_dev, int num_patterns, int height, int width, void* out_fp16_dev,
+                             void* stream);
+MSX_API int msx_process_potential(const float* trans_dev, int num_slices, int ny, int nx, float* work_dev,
+                                  void* out_fp16_dev, void* stream);
+
+/*
+ * Transmission slices from a sampled 3-D potential (ab-initio input) instead
+ * of Kirkland sites.  Replaces MSA/MSAGPU.integrate_potential_slices
+ * (namsa/msa.py:373-424, 568-578): pot_dev (nz, ld_y, ld_x) float32 with the
+ * z sample coordinates z_dev (nz) float64; slice s integrates its d = nz /
+ * num_slices samples by the trapezoidal rule (samples past num_slices * d are
+ * dropped, intervals between slices are not integrated, as in the reference),
+ * V = -integral, t = exp(i sigma V) over the leading ny x nx window.
+ */
+MSX_API int msx_integrate_potential(const float* pot_dev, const double* z_dev, int nz, int ld_y, int ld_x, int ny,
+                                    int nx, int num_slices, float sigma, float* trans_out_dev, void* stream);
+
+/*
  * Uneven batches.  Replaces the reference's fan-out over materials and probe
  * blocks (MPI ranks with one crystal each, scripts/sim_batch.py:201,
  * namsa/msa.py:1014-1081) by one CUDA graph on one GPU: jobs of different grid

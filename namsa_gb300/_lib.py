@@ -46,6 +46,10 @@ SIGNATURES = [
                                          _c.c_double, _c.c_float, _vp, _c.c_int, _vp, _vp]),
     ('msx_multislice_noalloc', _c.c_int, [_vp, _c.c_int, _vp, _vp, _vp, _c.c_int, _c.c_int, _c.c_int, _c.c_float,
                                           _c.c_double, _c.c_double, _c.c_float, _vp, _c.c_int, _c.c_int, _vp]),
+    ('msx_process_cbed', _c.c_int, [_vp, _c.c_int, _c.c_int, _c.c_int, _vp, _vp]),
+    ('msx_process_potential', _c.c_int, [_vp, _c.c_int, _c.c_int, _c.c_int, _vp, _vp, _vp]),
+    ('msx_integrate_potential', _c.c_int, [_vp, _vp, _c.c_int, _c.c_int, _c.c_int, _c.c_int, _c.c_int, _c.c_int,
+                                           _c.c_float, _vp, _vp]),
     ('msx_batch_create', _c.c_int, [_c.c_int, _c.POINTER(_vp)]),
     ('msx_batch_destroy', _c.c_int, [_vp]),
     ('msx_batch_set_schedule', _c.c_int, [_vp, _c.c_int, _c.c_int, _c.c_int, _c.c_int, _c.c_int]),

@@ -102,6 +102,38 @@ def build_probe(ny, nx, kmax, lam, k_semi, c1, c3, c5, smooth, device=None):
     return psik, ap, norm
 
 
+def process_cbed(cbed):
+    """Per-pattern z-scored float16 copy of a (P, H, W) float32 CBED stack."""
+    _need(cbed, torch.float32, 'cbed', 3)
+    out = torch.empty(cbed.shape, dtype=torch.float16, device=cbed.device)
+    _lib.check(lib().msx_process_cbed(_ptr(cbed), cbed.shape[0], cbed.shape[1], cbed.shape[2], _ptr(out), _stream()))
+    return out
+
+
+def process_potential(trans):
+    """Projected-potential label (1, w, w) float16 of a transmission stack (S, ny, nx)."""
+    _need(trans, torch.complex64, 'trans', 3)
+    S, ny, nx = trans.shape
+    r0, r1 = ny // 4, 3 * nx // 4
+    work = torch.empty(2 * ny * nx + 22, dtype=torch.float32, device=trans.device)
+    out = torch.empty((1, r1 - r0, r1 - r0), dtype=torch.float16, device=trans.device)
+    _lib.check(lib().msx_process_potential(_ptr(trans), S, ny, nx, _ptr(work), _ptr(out), _stream()))
+    return out
+
+
+def integrate_potential(pot, z, num_slices, sigma):
+    """Transmission slices (num_slices, n, n) complex64 from a potential (nz, ny, nx)
+    float32 sampled at z (nz,) float64, over the leading square n = min(ny, nx)."""
+    _need(pot, torch.float32, 'pot', 3)
+    _need(z, torch.float64, 'z', 1)
+    nz, ly, lx = pot.shape
+    n = min(ly, lx)
+    out = torch.empty((num_slices, n, n), dtype=torch.complex64, device=pot.device)
+    _lib.check(lib().msx_integrate_potential(_ptr(pot), _ptr(z), nz, ly, lx, n, n, int(num_slices), float(sigma),
+                                             _ptr(out), _stream()))
+    return out
+
+
 class Plan:
     """A multislice plan: resident wave workspace, schedules and graph cache."""
 

@@ -250,6 +250,45 @@ class MSAGPU:
             np.float32(self.sigma), want_potential=keep_potential)
         self.print_verbose('Built %d potential slices with shape:%s pixels' % (self.num_slices, self.sampling))
 
+    def integrate_potential_slices(self, pot, grid, slice_thickness, output=False):
+        """Transmission slices from a sampled 3-D potential (namsa/msa.py:373-424, 568-578).
+
+        ``pot`` is (nz, ny, nx) in the reference's units, ``grid`` the (z, y, x)
+        coordinate arrays.  The geometry is updated like the reference: square
+        crop to min(ny, nx), dims from the coordinate maxima, sampling from the
+        slice shape (or from ``max_angle``)."""
+        dev = self._dev()
+        z, y, x = [np.asarray(g, np.float64) for g in grid]
+        self.slice_t = slice_thickness
+        S = int((z[-1] - z[0]) // slice_thickness)
+        n = min(x.size, y.size)
+        self.num_slices = S
+        self.dims = np.array([x.max(), y.max(), z.max()])
+        if self.max_angle is None:
+            self.sampling = np.array([n, n])
+            self.kmax = np.min(self.sampling / self.dims[:2])
+            self.max_ang = self.kmax * self.Lambda
+        else:
+            self.max_ang = self.max_angle
+            self.kmax = self.max_ang / self.Lambda
+            self.sampling = np.floor(self.kmax * self.dims[:2]).astype(int)[::-1]
+        self.pix_size = self.dims[:2][::-1] / self.sampling
+        self.kpix_size = self.kmax / self.sampling
+        p = torch.as_tensor(np.ascontiguousarray(pot, np.float32), device=dev)
+        zt = torch.as_tensor(z, device=dev)
+        self.trans = engine.integrate_potential(p, zt, S, np.float32(self.sigma))
+        self.potential = None
+        if output:
+            return self.trans
+
+    def process_cbed(self):
+        """Per-pattern z-scored float16 CBED stack (scripts/summit_scripts/utils.py:102-118)."""
+        return engine.process_cbed(self.cbed)
+
+    def process_potential(self):
+        """Projected-potential label, float16 (scripts/summit_scripts/utils.py:74-100)."""
+        return engine.process_potential(self.trans)
+
     @property
     def potential_slices(self):
         """Host copy of the transmission slices (the reference keeps them pinned on the host, msa.py:616-638)."""

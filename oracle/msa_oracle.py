@@ -442,3 +442,40 @@ def _tile(basis, zs, n, a):
     arr['x'], arr['y'], arr['z'] = pos[:, 0], pos[:, 1], pos[:, 2]
     arr['occ'] = 1
     return arr
+
+
+# --------------------------------------------------------------------------- dataset post-processing
+def process_cbed(cbed):
+    """Per-pattern z-score to float16 (scripts/summit_scripts/utils.py:102-118)."""
+    cbed = np.asarray(cbed)
+    return ((cbed - np.mean(cbed, axis=(1, -1), keepdims=True)) / np.std(cbed, axis=(1, -1), keepdims=True)).astype(np.float16)
+
+
+def process_potential(trans):
+    """Projected-potential label (scripts/summit_scripts/utils.py:74-100): mean of Im t over
+    slices, Gaussian filter sigma 1.2 (scipy, reflecting borders), the central crop
+    [ny//4, 3*nx//4) on both axes, z-score with std floored at 1/sqrt(size), float16."""
+    from scipy.ndimage import gaussian_filter
+    proj = np.imag(trans).mean(0)
+    proj = gaussian_filter(proj, 1.2)
+    snap = slice(int(proj.shape[0] // 4), int(3 * proj.shape[1] // 4))
+    proj = proj[snap, snap]
+    proj = (proj - proj.mean()) / max(proj.std(), 1. / np.sqrt(proj.size))
+    return np.expand_dims(proj, 0).astype(np.float16)
+
+
+def integrate_potential_slices(pot, z, slice_t):
+    """Slices of a sampled 3-D potential (namsa/msa.py:373-406): ``int(z_dim // t)``
+    slices of ``nz // S`` samples each (trailing samples dropped), square crop to
+    min(ny, nx), trapezoidal rule along z within each slice, negated."""
+    z = np.asarray(z, np.float64)
+    S = int((z[-1] - z[0]) // slice_t)
+    n = min(pot.shape[1], pot.shape[2])
+    pot = pot[:, :n, :n]
+    d = pot.shape[0] // S
+    out = []
+    for s in range(S):
+        p = pot[s * d:(s + 1) * d].astype(np.float64)
+        zz = z[s * d:(s + 1) * d]
+        out.append(-(np.diff(zz)[:, None, None] * (p[1:] + p[:-1]) * 0.5).sum(0))
+    return np.array(out)

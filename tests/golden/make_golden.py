@@ -17,6 +17,12 @@ Fixtures written (all ``.npz``):
 * ``si_config1.npz``  -- Si 4x4x20 cells at 256^2, 80 slices, 100 keV, 20 mrad,
                          probe at the origin: window, slice checksums and exit wave.
 * ``positions.npz``   -- ``generate_probe_positions`` for both of its branches.
+* ``postproc.npz``    -- ``process_cbed`` / ``process_potential``
+                         (scripts/summit_scripts/utils.py:74-118) on seeded inputs.
+* ``integrated.npz``  -- ``MSA.integrate_potential_slices`` (namsa/msa.py:373-424)
+                         on a seeded 3-D potential.  SciPy 1.14 removed
+                         ``integrate.trapz``; it is aliased to ``trapezoid``
+                         (the same rule) for this call.
 """
 import os
 import sys
@@ -51,6 +57,14 @@ def import_reference(ref_root):
     import namsa.msa as msa
     import namsa.optics as optics
     return msa, optics
+
+
+def import_reference_utils(ref_root):
+    for name in ['skimage', 'skimage.transform']:
+        sys.modules.setdefault(name, _Stub(name))
+    sys.path.insert(0, os.path.join(ref_root, 'scripts', 'summit_scripts'))
+    import utils as ref_utils
+    return ref_utils
 
 
 def main(ref_root='/root/reference'):
@@ -109,6 +123,26 @@ def main(ref_root='/root/reference'):
         res[name + '_range'] = m2.grid_range
     res['dims'] = m2.dims
     np.savez_compressed(os.path.join(HERE, 'positions.npz'), **res)
+
+    # dataset post-processing
+    ru = import_reference_utils(ref_root)
+    rng = np.random.default_rng(7)
+    cbed = rng.gamma(0.7, 1e-4, size=(3, 32, 40)).astype(np.float32)
+    trans = np.exp(1j * rng.uniform(0, 0.4, size=(4, 64, 64))).astype(np.complex64)
+    np.savez_compressed(os.path.join(HERE, 'postproc.npz'), cbed=cbed, cbed_out=ru.process_cbed(cbed),
+                        trans=trans, pot_out=ru.process_potential(trans))
+
+    # integrated potential slices
+    import scipy.integrate as si
+    si.trapz = si.trapezoid
+    m3 = msa.MSA(200, 20e-3, si_supercell(1, 1, 1), sampling=np.array([48, 48]), debye_waller=False)
+    pot = rng.uniform(0, 2, size=(31, 50, 48)).astype(np.float32)
+    zc = np.linspace(0, 12.0, 31)
+    yc = np.linspace(0, 9.0, 50)
+    xc = np.linspace(0, 8.5, 48)
+    out = m3.integrate_potential_slices(pot, (zc, yc, xc), 2.5, output=True)
+    np.savez_compressed(os.path.join(HERE, 'integrated.npz'), pot=pot, z=zc, y=yc, x=xc, slice_t=2.5,
+                        slices=out, sigma=m3.sigma, sampling=m3.sampling, dims=m3.dims)
     print('golden fixtures written to', HERE)
 
 

@@ -97,3 +97,16 @@ def test_gpu_conventions_self_consistency(kirk):
     pd = dict(PD_SMALL, scherzer=True)
     psik, ap, norm = O.probe_gpu(geom, pd)
     assert abs(norm - 64 * 64 * np.sum(np.abs(psik) ** 2)) < 1e-9 * norm
+
+
+def test_postprocessing_matches_reference():
+    g = np.load(os.path.join(G, 'postproc.npz'))
+    np.testing.assert_array_equal(O.process_cbed(g['cbed']), g['cbed_out'])
+    np.testing.assert_array_equal(O.process_potential(g['trans']), g['pot_out'])
+
+
+def test_integrated_potential_matches_reference():
+    g = np.load(os.path.join(G, 'integrated.npz'))
+    out = O.integrate_potential_slices(g['pot'], g['z'], float(g['slice_t']))
+    assert out.shape == g['slices'].shape
+    np.testing.assert_allclose(out, g['slices'], rtol=2e-6, atol=2e-6)
