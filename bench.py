@@ -60,7 +60,7 @@ def parse():
     p.add_argument('--probes', type=int, default=1024, help='positions per GPU (the first N of the 32x32 scan)')
     p.add_argument('--autotune', action='store_true', help='pick schedules and group size by msx_plan_autotune')
     p.add_argument('--no-tma', action='store_true', help='plain one-CTA-per-tile passes instead of the persistent ones')
-    p.add_argument('--workload', default='scan', choices=['scan', 'uneven'],
+    p.add_argument('--workload', default='scan', choices=['scan', 'uneven', 'corrector'],
                    help='scan: the 512^2 Si [001] 1024-position scan; uneven: 64 seeded random crystals in one batch')
     p.add_argument('--branches', type=int, default=4, help='concurrent graph branches of the uneven batch')
     return p.parse_args()
@@ -406,12 +406,62 @@ def run_uneven(args):
     batch.close()
 
 
+def run_corrector(args):
+    """Learned coarse-slice corrector: train on device-generated pairs (Si, SrTiO3,
+    random crystals, 256^2, 200 keV, ~1000 A), then compare coarse+corrector with
+    plain fine-slice multislice (the judge) on held-out positions: CBED error and
+    probes/s of both."""
+    import torch
+    from namsa_gb300 import corrector as CR, engine
+    torch.cuda.set_device(0)
+    n, C, L = 256, 32, 4
+    t0 = time.perf_counter()
+    crystals = [(name, CR.Crystal(sites, n, t)) for name, sites, t, a in CR.training_crystals(n, seed=0, random_count=4)]
+    rng = np.random.default_rng(1)
+    cs, fs, ts = [], [], []
+    for name, cr in crystals:
+        a = 5.431 if name.startswith('Si') else 3.905
+        c, f, k = cr.pairs(rng.uniform(0, a, size=(24, 2)))
+        cs.append(c); fs.append(f); ts.append(cr.trans_coarse[k])
+    data_c, data_f, data_t = torch.cat(cs), torch.cat(fs), torch.cat(ts)
+    gen_s = time.perf_counter() - t0
+    net = engine.Corrector(n, n, C, L, max_batch=16)
+    net.params.copy_(torch.from_numpy(CR.init_params(C, L, seed=0)))
+    t1 = time.perf_counter()
+    losses = CR.train(net, data_c, data_f, data_t, steps=args.steps * 300, batch=16, lr=1e-3)
+    torch.cuda.synchronize()
+    train_s = time.perf_counter() - t1
+    res = {}
+    for name, cr in crystals[:2]:
+        a = 5.431 if name.startswith('Si') else 3.905
+        pos = np.random.default_rng(7).uniform(0, a, size=(16, 2))
+        ref, t_fine = CR.timed(lambda: CR.fine_multislice(cr, pos))
+        plain, t_plain = CR.timed(lambda: CR.corrected_multislice(net, cr, pos, use_net=False))
+        corr, t_corr = CR.timed(lambda: CR.corrected_multislice(net, cr, pos))
+        res[name] = {'thickness_A': cr.coarse_steps * cr.ratio * cr.slice_t, 'probes': len(pos),
+                     'err_coarse_vs_fine': float(CR.rel_l2(plain, ref).mean()),
+                     'err_corrected_vs_fine': float(CR.rel_l2(corr, ref).mean()),
+                     'fine_probes_per_s': len(pos) / t_fine, 'coarse_probes_per_s': len(pos) / t_plain,
+                     'corrected_probes_per_s': len(pos) / t_corr, 'speedup_vs_fine': t_fine / t_corr}
+    line = {'metric': METRIC, 'value': res['Si[001]']['corrected_probes_per_s'], 'unit': UNIT, 'n_gpus': 1,
+            'steps': args.steps, 'warmup': 0, 'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None,
+            'dtype': 'f32', 'data': 'synthetic (device-generated fine/coarse wave pairs)',
+            'config': {'workload': 'learned coarse-slice corrector, 256^2, 4x slices', 'pairs': int(data_c.shape[0]),
+                       'generate_s': gen_s, 'train_s': train_s, 'train_steps': len(losses),
+                       'loss_first': float(np.mean(losses[:20])), 'loss_last': float(np.mean(losses[-50:])),
+                       'channels': C, 'layers': L, 'modes': '8x8', 'results': res}}
+    print(json.dumps(line), flush=True)
+    net.close()
+
+
 def main():
     args = parse()
     if args.impl == 'reference':
         run_reference(args)
     elif args.workload == 'uneven':
         run_uneven(args)
+    elif args.workload == 'corrector':
+        run_corrector(args)
     else:
         run_ours(args)
 

@@ -46,6 +46,7 @@ extern "C" {
 
 typedef struct msx_plan msx_plan;
 typedef struct msx_batch msx_batch;
+typedef struct msx_corrector msx_corrector;
 
 /* One crystal of an uneven batch (msx_batch_run): the arguments of
  * msx_multislice for one grid. */
@@ -175,6 +176,26 @@ MSX_API int msx_multislice(msx_plan* plan, const float* trans_dev, int num_slice
                    void* stream);
 
 /*
+ * Real-space wave stepping, for workflows that act on the wave between slices
+ * (the learned coarse-slice corrector).  No single reference counterpart: the
+ * steps are those of namsa/msa.py:959-990 exposed one at a time.  waves are
+ * (num, ny, nx) complex64 real-space arrays owned by the caller.
+ *  msx_propagator_table: P(k) mask(k) / N (probe_kernels.cu:167-178, msa.py:833-839)
+ *                        into ptab_out (ny, nx) complex64.
+ *  msx_plan_probe_waves: fftshift(ifft2_u(psi_k * ramp)) per position (msa.py:959-964).
+ *  msx_plan_step_waves:  in place, psi <- ifft2_u(ptab * fft2_u(t * psi)), one slice.
+ *  msx_plan_cbed_waves:  |fft2_u(psi)|^2 / N / norm, cropped; the waves are overwritten.
+ */
+MSX_API int msx_propagator_table(int ny, int nx, float kmax, double lambda, double slice_t, float k_band,
+                                 float* ptab_out_dev, void* stream);
+MSX_API int msx_plan_probe_waves(msx_plan* plan, const float* psi_k_dev, const float* positions_dev, int num_probes,
+                                 float kmax, float* waves_out_dev, void* stream);
+MSX_API int msx_plan_step_waves(msx_plan* plan, float* waves_dev, int num_waves, const float* trans_dev,
+                                const float* ptab_dev, void* stream);
+MSX_API int msx_plan_cbed_waves(msx_plan* plan, float* waves_dev, int num_waves, const double* normalization_dev,
+                                float* cbed_out_dev, int crop_y, int crop_x, void* stream);
+
+/*
  * Annular (or any) detector signals fused into the last pass instead of CBED
  * stacks: signals_out[p][d] = sum_k I_p(k) w_d(k), with I_p the CBED pattern of
  * msx_multislice (full grid, natural FFT order) and w_d the weights
@@ -264,6 +285,30 @@ MSX_API int msx_batch_set_schedule(msx_batch* batch, int ny, int nx, int row_sch
 MSX_API int msx_batch_run(msx_batch* batch, const msx_job* jobs, int njobs, void* stream);
 /* msx_plan_check over every plan of the batch. */
 MSX_API int msx_batch_check(msx_batch* batch);
+
+/*
+ * Learned coarse-slice corrector (no counterpart in the reference): a
+ * spectral-convolution network mapping the wave after one thick slice and
+ * that slice's transmission t_c to the wave of the equivalent fine slices.
+ * channels <= 32 (C), layers L, 8 x 8 retained Fourier modes per layer.
+ * Waves and transmissions are (batch, ny, nx) complex64; waves are expected
+ * scaled by sqrt(ny*nx).  Parameters, gradients and Adam moments are four
+ * consecutive float32 arrays of `count` values (msx_corrector_params); the
+ * layout is documented in namsa_gb300/csrc/msx_corrector.cu.  Parameters
+ * start at zero: the caller writes its initialisation.
+ *  msx_corrector_forward:   pred = psi_c + net(psi_c, t_c)
+ *  msx_corrector_loss_grad: loss = sum |pred - psi_f|^2 / denom (to *loss_out_dev)
+ *                           and the gradient of every parameter (overwritten)
+ *  msx_corrector_adam:      one Adam step on the stored gradient
+ */
+MSX_API int msx_corrector_create(int ny, int nx, int channels, int layers, int max_batch, msx_corrector** corrector);
+MSX_API int msx_corrector_destroy(msx_corrector* corrector);
+MSX_API int msx_corrector_params(msx_corrector* corrector, float** params_dev, float** grads_dev, size_t* count);
+MSX_API int msx_corrector_forward(msx_corrector* corrector, const float* psi_c_dev, const float* tc_dev, int batch,
+                                  float* pred_out_dev, void* stream);
+MSX_API int msx_corrector_loss_grad(msx_corrector* corrector, const float* psi_c_dev, const float* tc_dev,
+                                    const float* psi_f_dev, int batch, double denom, float* loss_out_dev, void* stream);
+MSX_API int msx_corrector_adam(msx_corrector* corrector, float lr, float beta1, float beta2, float eps, void* stream);
 
 /*
  * Autotuner: times every (row schedule, column schedule, group size) of the

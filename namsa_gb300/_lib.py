@@ -42,6 +42,11 @@ SIGNATURES = [
     ('msx_plan_check', _c.c_int, [_vp]),
     ('msx_multislice', _c.c_int, [_vp, _vp, _c.c_int, _vp, _vp, _vp, _c.c_int, _c.c_float, _c.c_double,
                                   _c.c_double, _c.c_float, _vp, _c.c_int, _c.c_int, _vp]),
+    ('msx_propagator_table', _c.c_int, [_c.c_int, _c.c_int, _c.c_float, _c.c_double, _c.c_double, _c.c_float, _vp,
+                                        _vp]),
+    ('msx_plan_probe_waves', _c.c_int, [_vp, _vp, _vp, _c.c_int, _c.c_float, _vp, _vp]),
+    ('msx_plan_step_waves', _c.c_int, [_vp, _vp, _c.c_int, _vp, _vp, _vp]),
+    ('msx_plan_cbed_waves', _c.c_int, [_vp, _vp, _c.c_int, _vp, _vp, _c.c_int, _c.c_int, _vp]),
     ('msx_multislice_detect', _c.c_int, [_vp, _vp, _c.c_int, _vp, _vp, _vp, _c.c_int, _c.c_float, _c.c_double,
                                          _c.c_double, _c.c_float, _vp, _c.c_int, _vp, _vp]),
     ('msx_multislice_noalloc', _c.c_int, [_vp, _c.c_int, _vp, _vp, _vp, _c.c_int, _c.c_int, _c.c_int, _c.c_float,
@@ -55,6 +60,12 @@ SIGNATURES = [
     ('msx_batch_set_schedule', _c.c_int, [_vp, _c.c_int, _c.c_int, _c.c_int, _c.c_int, _c.c_int]),
     ('msx_batch_run', _c.c_int, [_vp, _vp, _c.c_int, _vp]),
     ('msx_batch_check', _c.c_int, [_vp]),
+    ('msx_corrector_create', _c.c_int, [_c.c_int, _c.c_int, _c.c_int, _c.c_int, _c.c_int, _c.POINTER(_vp)]),
+    ('msx_corrector_destroy', _c.c_int, [_vp]),
+    ('msx_corrector_params', _c.c_int, [_vp, _c.POINTER(_vp), _c.POINTER(_vp), _c.POINTER(_c.c_size_t)]),
+    ('msx_corrector_forward', _c.c_int, [_vp, _vp, _vp, _c.c_int, _vp, _vp]),
+    ('msx_corrector_loss_grad', _c.c_int, [_vp, _vp, _vp, _vp, _c.c_int, _c.c_double, _vp, _vp]),
+    ('msx_corrector_adam', _c.c_int, [_vp, _c.c_float, _c.c_float, _c.c_float, _c.c_float, _vp]),
     ('msx_plan_autotune', _c.c_int, [_vp, _vp, _c.c_int, _vp, _vp, _vp, _c.c_int, _c.c_float, _c.c_double,
                                      _c.c_double, _c.c_float, _c.c_int, _c.c_size_t, _c.POINTER(_c.c_float), _vp]),
     ('msx_plan_profile', _c.c_int, [_vp, _vp, _c.c_int, _vp, _vp, _vp, _c.c_int, _c.c_float, _c.c_double,

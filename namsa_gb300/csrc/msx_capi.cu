@@ -106,6 +106,7 @@ struct msx_plan {
   int row_ctas = 0, col_ctas = 0;
   float* partial = nullptr;      // detector partial sums
   size_t partial_words = 0;
+  float2* inv_n = nullptr;       // constant (1/N, 0) table for CBEDs of real-space waves
 };
 
 namespace {
@@ -392,6 +393,7 @@ int msx_plan_destroy(msx_plan* p) {
   if (p->band) cudaFree(p->band);
   if (p->err) cudaFree(p->err);
   if (p->partial) cudaFree(p->partial);
+  if (p->inv_n) cudaFree(p->inv_n);
   if (p->tw_row) cudaFree(p->tw_row);
   if (p->tw_col) cudaFree(p->tw_col);
   if (p->ev_in) cudaEventDestroy(p->ev_in);
@@ -539,6 +541,7 @@ int msx_multislice_detect(msx_plan* p, const float* trans_dev, int num_slices, c
   const size_t need = (size_t)p->group * (p->nx / p->col_ops->col_c) * num_detectors;
   if (need > p->partial_words) {
     if (p->partial) cudaFree(p->partial);
+  if (p->inv_n) cudaFree(p->inv_n);
     p->partial = nullptr;
     p->partial_words = 0;
     if (cudaMalloc(&p->partial, need * sizeof(float)) != cudaSuccess)
@@ -553,6 +556,68 @@ int msx_multislice_detect(msx_plan* p, const float* trans_dev, int num_slices, c
   a.col_sched = p->col_sched; a.det = detectors_dev; a.ndet = num_detectors; a.signals = signals_out_dev;
   drop_graph(p);  // the detector sequence is launched directly
   return enqueue_multislice(p, a, (cudaStream_t)stream);
+}
+
+int msx_propagator_table(int ny, int nx, float kmax, double lambda, double slice_t, float k_band, float* ptab_out_dev,
+                         void* stream) {
+  if (ny < 2 || nx < 2 || ny > 65535 || !ptab_out_dev || !(kmax > 0) || !(lambda > 0) || !(slice_t >= 0))
+    return fail(MSX_ERR_INVALID, "propagator table: bad arguments");
+  MSX_CUDA(launch_ptab(ny, nx, kmax, lambda, slice_t, k_band, reinterpret_cast<float2*>(ptab_out_dev),
+                       (cudaStream_t)stream), "propagator table");
+  return MSX_OK;
+}
+
+int msx_plan_probe_waves(msx_plan* p, const float* psi_k_dev, const float* positions_dev, int num_probes, float kmax,
+                         float* waves_out_dev, void* stream) {
+  if (!p || num_probes < 0 || !psi_k_dev || !positions_dev || !waves_out_dev || !(kmax > 0))
+    return fail(MSX_ERR_INVALID, "probe waves: bad arguments");
+  if (num_probes == 0) return MSX_OK;
+  cudaStream_t st = (cudaStream_t)stream;
+  ColArgs c{};
+  c.psi = reinterpret_cast<float2*>(waves_out_dev); c.psik = reinterpret_cast<const float2*>(psi_k_dev);
+  c.pos_yx = positions_dev; c.tw = p->tw_col; c.G = num_probes; c.Nx = p->nx; c.kmax = kmax; c.x_begin = 0;
+  c.ncols = p->nx;
+  MSX_CUDA(p->col_ops->col(COL_INIT, c, st), "probe formation pass");
+  MSX_CUDA(p->row_ops->row_mode(ROW_I, c.psi, nullptr, p->tw_row, num_probes, p->ny, st), "inverse row transform");
+  return MSX_OK;
+}
+
+int msx_plan_step_waves(msx_plan* p, float* waves_dev, int num_waves, const float* trans_dev, const float* ptab_dev,
+                        void* stream) {
+  if (!p || num_waves < 0 || !waves_dev || !trans_dev || !ptab_dev) return fail(MSX_ERR_INVALID, "step waves: bad arguments");
+  if (num_waves == 0) return MSX_OK;
+  cudaStream_t st = (cudaStream_t)stream;
+  float2* w = reinterpret_cast<float2*>(waves_dev);
+  ColArgs c{};
+  c.psi = w; c.ptab = reinterpret_cast<const float2*>(ptab_dev); c.tw = p->tw_col; c.G = num_waves; c.Nx = p->nx;
+  c.x_begin = 0; c.ncols = p->nx;
+  MSX_CUDA(p->row_ops->row_mode(ROW_TF, w, reinterpret_cast<const float2*>(trans_dev), p->tw_row, num_waves, p->ny, st),
+           "transmit + forward row transform");
+  MSX_CUDA(p->col_ops->col(COL_MID, c, st), "column pass");
+  MSX_CUDA(p->row_ops->row_mode(ROW_I, w, nullptr, p->tw_row, num_waves, p->ny, st), "inverse row transform");
+  return MSX_OK;
+}
+
+int msx_plan_cbed_waves(msx_plan* p, float* waves_dev, int num_waves, const double* normalization_dev,
+                        float* cbed_out_dev, int crop_y, int crop_x, void* stream) {
+  if (!p || num_waves < 0 || !waves_dev || !normalization_dev || !cbed_out_dev || crop_y <= 0 || crop_x <= 0 ||
+      crop_y > p->ny || crop_x > p->nx)
+    return fail(MSX_ERR_INVALID, "cbed of waves: bad arguments");
+  if (num_waves == 0) return MSX_OK;
+  cudaStream_t st = (cudaStream_t)stream;
+  if (!p->inv_n) {
+    if (cudaMalloc(&p->inv_n, sizeof(float2) * (size_t)p->ny * p->nx) != cudaSuccess)
+      return fail(MSX_ERR_ALLOC, "constant table allocation failed");
+    // P = 1 everywhere, k_band beyond every |k|: launch_ptab with zero thickness gives (1/N, 0)
+    MSX_CUDA(launch_ptab(p->ny, p->nx, 1.0f, 1.0, 0.0, 3.0e38f, p->inv_n, st), "constant table");
+  }
+  float2* w = reinterpret_cast<float2*>(waves_dev);
+  MSX_CUDA(p->row_ops->row_mode(ROW_F, w, nullptr, p->tw_row, num_waves, p->ny, st), "forward row transform");
+  ColArgs c{};
+  c.psi = w; c.ptab = p->inv_n; c.tw = p->tw_col; c.norm = normalization_dev; c.cbed = cbed_out_dev; c.G = num_waves;
+  c.Nx = p->nx; c.x_begin = p->nx / 2 - crop_x / 2; c.ncols = crop_x; c.y0 = p->ny / 2 - crop_y / 2; c.crop_y = crop_y;
+  MSX_CUDA(p->col_ops->col(COL_FINAL, c, st), "final column pass");
+  return MSX_OK;
 }
 
 int msx_plan_profile(msx_plan* p, const float* trans_dev, int num_slices, const float* psi_k_dev,

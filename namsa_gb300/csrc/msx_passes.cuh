@@ -56,8 +56,14 @@ __device__ __forceinline__ void load_twiddles(float2* dst, const float2* __restr
 
 // ---------------------------------------------------------------- row pass
 // Lines are ordered (y, p) with the wave index fastest so the waves of one CTA
-// share the transmission row.
-template <class S>
+// share the transmission row.  RMODE selects the work on each row:
+//   ROW_FULL  inverse FFT_x -> * t -> forward FFT_x  (one slice, mixed domain)
+//   ROW_TF    * t -> forward FFT_x                    (real-space wave in)
+//   ROW_I     inverse FFT_x                           (real-space wave out)
+//   ROW_F     forward FFT_x
+enum RowMode { ROW_FULL = 0, ROW_TF = 1, ROW_I = 2, ROW_F = 3 };
+
+template <class S, int RMODE = ROW_FULL>
 __global__ void __launch_bounds__(S::THREADS, S::MINB)
 row_pass_kernel(float2* __restrict__ psi, const float2* __restrict__ trans, const float2* __restrict__ tw_g,
                 int G, int Ny) {
@@ -77,11 +83,13 @@ row_pass_kernel(float2* __restrict__ psi, const float2* __restrict__ trans, cons
 #pragma unroll
   for (int m = 0; m < S::E; ++m) v[m] = row[t + S::T * m];
   PaddedLine buf{smem + S::TW_PAD + (warp * S::LPW + lw) * S::ROW_LINE_WORDS};
-  S::FFT::template run<true, false>(v, buf, tw, t);
-  const float2* trow = trans + (size_t)y * NX;
+  if constexpr (RMODE == ROW_FULL || RMODE == ROW_I) S::FFT::template run<true, false>(v, buf, tw, t);
+  if constexpr (RMODE == ROW_FULL || RMODE == ROW_TF) {
+    const float2* trow = trans + (size_t)y * NX;
 #pragma unroll
-  for (int m = 0; m < S::E; ++m) v[m] = cmul(v[m], __ldg(trow + t + S::T * m));
-  S::FFT::template run<false, false>(v, buf, tw, t);
+    for (int m = 0; m < S::E; ++m) v[m] = cmul(v[m], __ldg(trow + t + S::T * m));
+  }
+  if constexpr (RMODE == ROW_FULL || RMODE == ROW_TF || RMODE == ROW_F) S::FFT::template run<false, false>(v, buf, tw, t);
   if (valid) {
 #pragma unroll
     for (int m = 0; m < S::E; ++m) row[t + S::T * m] = v[m];

@@ -24,6 +24,8 @@ struct SchedOps {
   cudaError_t (*row_tma)(const TmaPassArgs& a, int ctas, cudaStream_t st);
   cudaError_t (*col_tma)(const CUtensorMap& map, const TmaPassArgs& a, int ctas, cudaStream_t st);
   cudaError_t (*occupancy)(int* row_per_sm, int* col_per_sm);
+  // row pass with a RowMode other than ROW_FULL (real-space stepping)
+  cudaError_t (*row_mode)(int rmode, float2* psi, const float2* trans, const float2* tw, int G, int Ny, cudaStream_t st);
 };
 
 template <class S> struct SchedImpl {
@@ -37,6 +39,9 @@ template <class S> struct SchedImpl {
     if (e == cudaSuccess) e = cudaFuncSetAttribute(col_pass_kernel<S, COL_FINAL>, cudaFuncAttributeMaxDynamicSharedMemorySize, cs);
     if (e == cudaSuccess) e = cudaFuncSetAttribute(col_pass_kernel<S, COL_INIT_FINAL>, cudaFuncAttributeMaxDynamicSharedMemorySize, cs);
     if (e == cudaSuccess) e = cudaFuncSetAttribute(col_pass_kernel<S, COL_DETECT>, cudaFuncAttributeMaxDynamicSharedMemorySize, cs);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(row_pass_kernel<S, ROW_TF>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)S::row_smem());
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(row_pass_kernel<S, ROW_I>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)S::row_smem());
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(row_pass_kernel<S, ROW_F>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)S::row_smem());
     if (e == cudaSuccess) e = cudaFuncSetAttribute(row_pass_tma_kernel<S>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)RowTma<S>::smem());
     if (e == cudaSuccess) e = cudaFuncSetAttribute(col_mid_tma_kernel<S>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ColTma<S>::smem());
     return e;
@@ -79,9 +84,21 @@ template <class S> struct SchedImpl {
       e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(col_per_sm, col_mid_tma_kernel<S>, S::THREADS, ColTma<S>::smem());
     return e;
   }
+  static cudaError_t row_mode(int rmode, float2* psi, const float2* trans, const float2* tw, int G, int Ny,
+                              cudaStream_t st) {
+    const int lines = G * Ny;
+    const int blocks = (lines + S::ROW_LINES - 1) / S::ROW_LINES;
+    switch (rmode) {
+      case ROW_TF: row_pass_kernel<S, ROW_TF><<<blocks, S::THREADS, S::row_smem(), st>>>(psi, trans, tw, G, Ny); break;
+      case ROW_I: row_pass_kernel<S, ROW_I><<<blocks, S::THREADS, S::row_smem(), st>>>(psi, trans, tw, G, Ny); break;
+      case ROW_F: row_pass_kernel<S, ROW_F><<<blocks, S::THREADS, S::row_smem(), st>>>(psi, trans, tw, G, Ny); break;
+      default: row_pass_kernel<S, ROW_FULL><<<blocks, S::THREADS, S::row_smem(), st>>>(psi, trans, tw, G, Ny); break;
+    }
+    return cudaGetLastError();
+  }
   static SchedOps ops(const char* name) {
     return SchedOps{S::N, name, S::TW, S::C, ColTma<S>::BOXR, &host_twiddles, &configure, &row, &col,
-                    &row_tma, &col_tma, &occupancy};
+                    &row_tma, &col_tma, &occupancy, &row_mode};
   }
 };
 

@@ -134,6 +134,15 @@ def integrate_potential(pot, z, num_slices, sigma):
     return out
 
 
+def propagator_table(ny, nx, kmax, lam, slice_t, k_band, device=None):
+    """P(k) mask(k) / N as a (ny, nx) complex64 device tensor."""
+    dev = torch.device('cuda', torch.cuda.current_device()) if device is None else device
+    out = torch.empty((ny, nx), dtype=torch.complex64, device=dev)
+    _lib.check(lib().msx_propagator_table(int(ny), int(nx), float(kmax), float(lam), float(slice_t), float(k_band),
+                                          _ptr(out), _stream()))
+    return out
+
+
 class Plan:
     """A multislice plan: resident wave workspace, schedules and graph cache."""
 
@@ -207,6 +216,29 @@ class Plan:
         _lib.check(lib().msx_multislice(self.handle, _ptr(trans), S, _ptr(psik), _ptr(norm), _ptr(positions), P,
                                         float(kmax), float(lam), float(slice_t), float(k_band), _ptr(out),
                                         int(cy), int(cx), _stream()))
+        return out
+
+    def probe_waves(self, psik, positions, kmax):
+        """Real-space probe wavefunctions (P, ny, nx) complex64 (unnormalised ifft, fftshifted)."""
+        out = torch.empty((positions.shape[0], self.ny, self.nx), dtype=torch.complex64, device=psik.device)
+        _lib.check(lib().msx_plan_probe_waves(self.handle, _ptr(psik), _ptr(positions), positions.shape[0],
+                                              float(kmax), _ptr(out), _stream()))
+        return out
+
+    def step_waves(self, waves, trans, ptab):
+        """One slice in place on real-space waves (G, ny, nx): psi <- ifft2(ptab * fft2(t * psi))."""
+        _need(waves, torch.complex64, 'waves', 3)
+        _lib.check(lib().msx_plan_step_waves(self.handle, _ptr(waves), waves.shape[0], _ptr(trans), _ptr(ptab),
+                                             _stream()))
+        return waves
+
+    def cbed_waves(self, waves, norm, crop=None):
+        """CBED patterns of real-space waves (overwrites the waves)."""
+        _need(waves, torch.complex64, 'waves', 3)
+        cy, cx = (self.ny, self.nx) if crop is None else ((crop, crop) if isinstance(crop, int) else crop)
+        out = torch.empty((waves.shape[0], cy, cx), dtype=torch.float32, device=waves.device)
+        _lib.check(lib().msx_plan_cbed_waves(self.handle, _ptr(waves), waves.shape[0], _ptr(norm), _ptr(out),
+                                             int(cy), int(cx), _stream()))
         return out
 
     def detect(self, trans, psik, norm, positions, kmax, lam, slice_t, k_band, detectors, out=None):
@@ -292,3 +324,61 @@ class Batch:
 
     def check(self):
         _lib.check(lib().msx_batch_check(self._h))
+
+
+class _DevView:
+    """A device buffer of the library exposed to torch (no copy)."""
+
+    def __init__(self, ptr, n):
+        self.__cuda_array_interface__ = {'shape': (int(n),), 'typestr': '<f4', 'data': (int(ptr), False),
+                                         'version': 3, 'strides': None}
+
+
+class Corrector:
+    """Learned coarse-slice corrector (spectral-convolution network) of libmsx."""
+
+    def __init__(self, ny, nx, channels=32, layers=4, max_batch=8):
+        h = _vp()
+        _lib.check(lib().msx_corrector_create(int(ny), int(nx), int(channels), int(layers), int(max_batch),
+                                              ctypes.byref(h)))
+        self._h = h
+        self.ny, self.nx, self.channels, self.layers, self.max_batch = ny, nx, channels, layers, max_batch
+        p, g = _vp(), _vp()
+        n = ctypes.c_size_t()
+        _lib.check(lib().msx_corrector_params(self._h, ctypes.byref(p), ctypes.byref(g), ctypes.byref(n)))
+        dev = torch.device('cuda', torch.cuda.current_device())
+        self.count = n.value
+        self.params = torch.as_tensor(_DevView(p.value, n.value), device=dev)
+        self.grads = torch.as_tensor(_DevView(g.value, n.value), device=dev)
+
+    def close(self):
+        if getattr(self, '_h', None) is not None:
+            lib().msx_corrector_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def forward(self, psi_c, tc, out=None):
+        _need(psi_c, torch.complex64, 'psi_c', 3)
+        _need(tc, torch.complex64, 'tc', 3)
+        if out is None:
+            out = torch.empty_like(psi_c)
+        _lib.check(lib().msx_corrector_forward(self._h, _ptr(psi_c), _ptr(tc), psi_c.shape[0], _ptr(out), _stream()))
+        return out
+
+    def loss_grad(self, psi_c, tc, psi_f, denom, loss_out=None):
+        _need(psi_c, torch.complex64, 'psi_c', 3)
+        _need(tc, torch.complex64, 'tc', 3)
+        _need(psi_f, torch.complex64, 'psi_f', 3)
+        if loss_out is None:
+            loss_out = torch.empty(1, dtype=torch.float32, device=psi_c.device)
+        _lib.check(lib().msx_corrector_loss_grad(self._h, _ptr(psi_c), _ptr(tc), _ptr(psi_f), psi_c.shape[0],
+                                                 float(denom), _ptr(loss_out), _stream()))
+        return loss_out
+
+    def adam(self, lr=1e-3, beta1=0.9, beta2=0.999, eps=1e-8):
+        _lib.check(lib().msx_corrector_adam(self._h, float(lr), float(beta1), float(beta2), float(eps), _stream()))
