@@ -135,12 +135,14 @@ def corrected_multislice(net, crystal, positions, steps=None, use_net=True):
 
 
 def fine_multislice(crystal, positions, steps=None):
-    """CBED of plain fine-slice multislice through the same thickness."""
+    """CBED of plain fine-slice multislice (the fused engine path) through the
+    same thickness as `steps` coarse steps."""
     steps = crystal.coarse_steps if steps is None else steps
-    w = crystal.waves(positions)
-    for j in range(crystal.ratio * steps):
-        crystal.plan.step_waves(w, crystal.trans_fine[j], crystal.ptab_fine)
-    return crystal.plan.cbed_waves(w, crystal.sim.norm_dev)
+    sim = crystal.sim
+    pos = torch.as_tensor(np.asarray(positions, np.float32), device=crystal.trans_fine.device)
+    trans = crystal.trans_fine[:crystal.ratio * steps].contiguous()
+    return crystal.plan.multislice(trans, sim.psi_k_dev, sim.norm_dev, pos, crystal.kmax, sim.Lambda,
+                                   crystal.slice_t, np.float32(sim.kmax / 3))
 
 
 def rel_l2(a, b):
