@@ -60,7 +60,7 @@ def parse():
     p.add_argument('--probes', type=int, default=1024, help='positions per GPU (the first N of the 32x32 scan)')
     p.add_argument('--autotune', action='store_true', help='pick schedules and group size by msx_plan_autotune')
     p.add_argument('--no-tma', action='store_true', help='plain one-CTA-per-tile passes instead of the persistent ones')
-    p.add_argument('--workload', default='scan', choices=['scan', 'uneven', 'corrector'],
+    p.add_argument('--workload', default='scan', choices=['scan', 'uneven', 'corrector', 'precision'],
                    help='scan: the 512^2 Si [001] 1024-position scan; uneven: 64 seeded random crystals in one batch')
     p.add_argument('--branches', type=int, default=4, help='concurrent graph branches of the uneven batch')
     return p.parse_args()
@@ -454,6 +454,59 @@ def run_corrector(args):
     net.close()
 
 
+def run_precision(args):
+    """SrTiO3 [001], 400 A thick, t = a/2, 300 keV, 25 mrad: CBED error against the
+    FP64 oracle of (a) the FP32 FFT engine at 1024^2 (64 cells, 64 positions) and,
+    on 512^2 sub-runs (32 cells), (b) the FP32 engine and (c) the split-BF16
+    tensor-core DFT stages.  The FP64 oracle runs on the host for a sample of
+    positions."""
+    import torch
+    from namsa_gb300 import corrector as CR, engine, structures
+    from oracle import msa_oracle as O
+    torch.cuda.set_device(0)
+    a = 3.905
+    rng = np.random.default_rng(0)
+    out = {}
+    for n, cells, forms in [(512, 32, ('fp32_fft', 'bf16x3_tensor_core')), (1024, 64, ('fp32_fft',))]:
+        sc = structures.srtio3((cells, cells, int(np.ceil(400 / a))))
+        cr = CR.Crystal(sc, n, a / 2, kv=300, semi_angle=25e-3, ratio=1)
+        pos = rng.uniform(0, a, size=(64, 2)).astype(np.float32)
+        sample = np.arange(0, 64, 32) if n == 1024 else np.arange(0, 64, 16)
+        xyz = np.column_stack([sc['x'], sc['y'], sc['z']]).astype(np.float32)
+        geom = O.Geometry(xyz, sc['atomic_number'], 300., 25e-3, [n, n])
+        P, _ = O.propagator_gpu(geom, a / 2, 1 / 3)
+        psik, _, norm = O.probe_gpu(geom, CR.PROBE)
+        t0 = time.perf_counter()
+        ref = O.multislice_gpu(cr.trans_fine.cpu().numpy().astype(np.complex128), psik, P, pos[sample], norm, geom)
+        oracle_s = time.perf_counter() - t0
+        res = {'slices': int(cr.trans_fine.shape[0]), 'positions': 64, 'oracle_positions': len(sample),
+               'oracle_s': oracle_s}
+        for form in forms:
+            torch.cuda.synchronize()
+            t1 = time.perf_counter()
+            if form == 'fp32_fft':
+                got = CR.fine_multislice(cr, pos)
+            else:
+                w = cr.waves(pos)
+                for s in range(cr.trans_fine.shape[0]):
+                    engine.step_waves_tc(w, cr.trans_fine[s], cr.ptab_fine)
+                got = cr.plan.cbed_waves(w, cr.sim.norm_dev)
+                engine.tc_check()
+            torch.cuda.synchronize()
+            dt = time.perf_counter() - t1
+            g = got.cpu().numpy()[sample]
+            e = O.rel_l2(g, ref)
+            res[form] = {'rel_l2_mean': float(e.mean()), 'rel_l2_max': float(e.max()),
+                         'max_abs': float(np.abs(g - ref).max()), 'max_ref': float(np.abs(ref).max()),
+                         'probes_per_s': 64 / dt}
+        out[f'{n}x{n}'] = res
+    line = {'metric': METRIC, 'value': out['1024x1024']['fp32_fft']['probes_per_s'], 'unit': UNIT, 'n_gpus': 1,
+            'steps': 1, 'warmup': 0, 'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None,
+            'dtype': 'c64', 'data': 'synthetic (generated SrTiO3 supercell)',
+            'config': {'workload': 'precision study SrTiO3[001] 400 A, 300 keV, 25 mrad', 'results': out}}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
     if args.impl == 'reference':
@@ -462,6 +515,8 @@ def main():
         run_uneven(args)
     elif args.workload == 'corrector':
         run_corrector(args)
+    elif args.workload == 'precision':
+        run_precision(args)
     else:
         run_ours(args)
 

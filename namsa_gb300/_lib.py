@@ -60,6 +60,9 @@ SIGNATURES = [
     ('msx_batch_set_schedule', _c.c_int, [_vp, _c.c_int, _c.c_int, _c.c_int, _c.c_int, _c.c_int]),
     ('msx_batch_run', _c.c_int, [_vp, _vp, _c.c_int, _vp]),
     ('msx_batch_check', _c.c_int, [_vp]),
+    ('msx_tc_dft', _c.c_int, [_vp, _c.c_int, _c.c_int, _c.c_int, _vp, _vp]),
+    ('msx_step_waves_tc', _c.c_int, [_vp, _c.c_int, _c.c_int, _vp, _vp, _vp]),
+    ('msx_tc_check', _c.c_int, []),
     ('msx_corrector_create', _c.c_int, [_c.c_int, _c.c_int, _c.c_int, _c.c_int, _c.c_int, _c.POINTER(_vp)]),
     ('msx_corrector_destroy', _c.c_int, [_vp]),
     ('msx_corrector_params', _c.c_int, [_vp, _c.POINTER(_vp), _c.POINTER(_vp), _c.POINTER(_c.c_size_t)]),

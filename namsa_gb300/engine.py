@@ -143,6 +143,26 @@ def propagator_table(ny, nx, kmax, lam, slice_t, k_band, device=None):
     return out
 
 
+def tc_dft(x, sign):
+    """Tensor-core split-BF16 DFT along the last axis of (lines, n) complex64, n in {256, 512}."""
+    _need(x, torch.complex64, 'x', 2)
+    z = torch.empty_like(x)
+    _lib.check(lib().msx_tc_dft(_ptr(x), x.shape[0], x.shape[1], int(sign), _ptr(z), _stream()))
+    return z
+
+
+def step_waves_tc(waves, trans, ptab):
+    """One slice on real-space waves (G, n, n) with the four 1-D DFTs on the tensor cores."""
+    _need(waves, torch.complex64, 'waves', 3)
+    _lib.check(lib().msx_step_waves_tc(_ptr(waves), waves.shape[0], waves.shape[1], _ptr(trans), _ptr(ptab),
+                                       _stream()))
+    return waves
+
+
+def tc_check():
+    _lib.check(lib().msx_tc_check())
+
+
 class Plan:
     """A multislice plan: resident wave workspace, schedules and graph cache."""
 

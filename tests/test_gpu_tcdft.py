@@ -1,0 +1,66 @@
+"""Split-BF16 tensor-core DFT stages (tcgen05) against NumPy FFTs in float64,
+and the tensor-core slice step against the FP32 FFT step."""
+import numpy as np
+import pytest
+import torch
+
+from namsa_gb300 import engine
+
+pytestmark = pytest.mark.gpu
+DEV = 'cuda'
+
+
+@pytest.mark.parametrize('n,lines', [(256, 128), (512, 256)])
+def test_tc_dft_matches_fft(n, lines):
+    rng = np.random.default_rng(n)
+    x = (rng.standard_normal((lines, n)) + 1j * rng.standard_normal((lines, n))).astype(np.complex64)
+    xd = torch.from_numpy(x).to(DEV)
+    for sign in (-1, 1):
+        z = engine.tc_dft(xd, sign).cpu().numpy()
+        ref = np.fft.fft(x.astype(np.complex128), axis=1) if sign < 0 else np.fft.ifft(x.astype(np.complex128), axis=1) * n
+        err = np.linalg.norm(z - ref) / np.linalg.norm(ref)
+        assert err < 5e-5, (sign, err)
+    engine.tc_check()
+
+
+def test_tc_step_matches_fp32_step():
+    rng = np.random.default_rng(1)
+    n, G = 256, 3
+    w = (rng.standard_normal((G, n, n)) + 1j * rng.standard_normal((G, n, n))).astype(np.complex64)
+    t = np.exp(0.3j * rng.standard_normal((n, n))).astype(np.complex64)
+    ptab = engine.propagator_table(n, n, np.float32(12.0), 0.025, 1.5, np.float32(4.0))
+    a = torch.from_numpy(w).to(DEV)
+    b = a.clone()
+    td = torch.from_numpy(t).to(DEV)
+    plan = engine.Plan(n, n)
+    plan.step_waves(a, td, ptab)
+    engine.step_waves_tc(b, td, ptab)
+    torch.cuda.synchronize()
+    engine.tc_check()
+    err = (torch.linalg.vector_norm(a - b) / torch.linalg.vector_norm(a)).item()
+    assert err < 1e-4, err
+    plan.close()
+
+
+def test_tc_multislice_cbed_vs_fp64():
+    """A 256^2 SrTiO3 [001] run with every per-slice DFT on the tensor cores
+    stays within the 1e-3 CBED bar against the FP64 oracle."""
+    from namsa_gb300 import corrector as CR, structures
+    from oracle import msa_oracle as O
+    torch.cuda.set_device(0)
+    sc = structures.srtio3((16, 16, 8))
+    cr = CR.Crystal(sc, 256, 3.905 / 2, kv=300, semi_angle=25e-3, ratio=1)
+    pos = np.array([[0., 0.], [1.0, 1.9]], np.float32)
+    w = cr.waves(pos)
+    S = cr.trans_fine.shape[0]
+    for s in range(S):
+        engine.step_waves_tc(w, cr.trans_fine[s], cr.ptab_fine)
+    got = cr.plan.cbed_waves(w, cr.sim.norm_dev).cpu().numpy()
+    engine.tc_check()
+    xyz = np.column_stack([sc['x'], sc['y'], sc['z']]).astype(np.float32)
+    geom = O.Geometry(xyz, sc['atomic_number'], 300., 25e-3, [256, 256])
+    P, _ = O.propagator_gpu(geom, 3.905 / 2, 1 / 3)
+    psik, _, norm = O.probe_gpu(geom, CR.PROBE)
+    ref = O.multislice_gpu(cr.trans_fine.cpu().numpy().astype(np.complex128), psik, P, pos, norm, geom)
+    err = O.rel_l2(got, ref)
+    assert err.max() < 1e-3, err
