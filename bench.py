@@ -58,7 +58,8 @@ def parse():
     p.add_argument('--no-cpu-baseline', action='store_true')
     p.add_argument('--cpu-sample', type=int, default=0, help='probes per CPU-baseline sample (0 = number of cores)')
     p.add_argument('--probes', type=int, default=1024, help='positions per GPU (the first N of the 32x32 scan)')
-    p.add_argument('--autotune', action='store_true', help='pick schedules and group size by msx_plan_autotune')
+    p.add_argument('--no-autotune', dest='autotune', action='store_false',
+                   help='keep the library default schedule instead of msx_plan_autotune')
     p.add_argument('--no-tma', action='store_true', help='plain one-CTA-per-tile passes instead of the persistent ones')
     p.add_argument('--workload', default='scan', choices=['scan', 'uneven', 'corrector', 'precision'],
                    help='scan: the 512^2 Si [001] 1024-position scan; uneven: 64 seeded random crystals in one batch')
@@ -429,6 +430,12 @@ def run_corrector(args):
     net.params.copy_(torch.from_numpy(CR.init_params(C, L, seed=0)))
     t1 = time.perf_counter()
     losses = CR.train(net, data_c, data_f, data_t, steps=args.steps * 300, batch=16, lr=1e-3)
+    # second phase: add pairs taken along the corrector's own trajectories
+    for name, cr in crystals:
+        a = 5.431 if name.startswith('Si') else 3.905
+        c, f, k = CR.rollout_pairs(net, cr, rng.uniform(0, a, size=(8, 2)))
+        data_c, data_f, data_t = torch.cat([data_c, c]), torch.cat([data_f, f]), torch.cat([data_t, cr.trans_coarse[k]])
+    losses += CR.train(net, data_c, data_f, data_t, steps=args.steps * 150, batch=16, lr=3e-4, seed=1)
     torch.cuda.synchronize()
     train_s = time.perf_counter() - t1
     res = {}

@@ -313,7 +313,8 @@ MSX_API int msx_tc_check(void);
  * layout is documented in namsa_gb300/csrc/msx_corrector.cu.  Parameters
  * start at zero: the caller writes its initialisation.
  *  msx_corrector_forward:   pred = psi_c + net(psi_c, t_c)
- *  msx_corrector_loss_grad: loss = sum |pred - psi_f|^2 / denom (to *loss_out_dev)
+ *  msx_corrector_loss_grad: loss = sum_b w_b sum |pred_b - psi_f_b|^2 / denom (to
+ *                           *loss_out_dev; w_b = sample_weights_dev[b], or 1 when NULL)
  *                           and the gradient of every parameter (overwritten)
  *  msx_corrector_adam:      one Adam step on the stored gradient
  */
@@ -323,7 +324,8 @@ MSX_API int msx_corrector_params(msx_corrector* corrector, float** params_dev, f
 MSX_API int msx_corrector_forward(msx_corrector* corrector, const float* psi_c_dev, const float* tc_dev, int batch,
                                   float* pred_out_dev, void* stream);
 MSX_API int msx_corrector_loss_grad(msx_corrector* corrector, const float* psi_c_dev, const float* tc_dev,
-                                    const float* psi_f_dev, int batch, double denom, float* loss_out_dev, void* stream);
+                                    const float* psi_f_dev, int batch, double denom, const float* sample_weights_dev,
+                                    float* loss_out_dev, void* stream);
 MSX_API int msx_corrector_adam(msx_corrector* corrector, float lr, float beta1, float beta2, float eps, void* stream);
 
 /*

@@ -67,7 +67,7 @@ SIGNATURES = [
     ('msx_corrector_destroy', _c.c_int, [_vp]),
     ('msx_corrector_params', _c.c_int, [_vp, _c.POINTER(_vp), _c.POINTER(_vp), _c.POINTER(_c.c_size_t)]),
     ('msx_corrector_forward', _c.c_int, [_vp, _vp, _vp, _c.c_int, _vp, _vp]),
-    ('msx_corrector_loss_grad', _c.c_int, [_vp, _vp, _vp, _vp, _c.c_int, _c.c_double, _vp, _vp]),
+    ('msx_corrector_loss_grad', _c.c_int, [_vp, _vp, _vp, _vp, _c.c_int, _c.c_double, _vp, _vp, _vp]),
     ('msx_corrector_adam', _c.c_int, [_vp, _c.c_float, _c.c_float, _c.c_float, _c.c_float, _vp]),
     ('msx_plan_autotune', _c.c_int, [_vp, _vp, _c.c_int, _vp, _vp, _vp, _c.c_int, _c.c_float, _c.c_double,
                                      _c.c_double, _c.c_float, _c.c_int, _c.c_size_t, _c.POINTER(_c.c_float), _vp]),

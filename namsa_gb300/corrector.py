@@ -29,15 +29,15 @@ PROBE = {'smooth_apert': True, 'apert_smooth': 50, 'spherical_phase': True,
 
 def init_params(C, L, seed=0, K=8):
     """Seeded initial parameters in the library's layout: fan-in scaled linear
-    maps, spectral weights ~ 1/C, and a near-zero output layer (the untrained
-    network returns the coarse wave)."""
+    maps, spectral weights ~ 1/C, and a zero output layer (the untrained
+    network returns the coarse wave exactly)."""
     rng = np.random.default_rng(seed)
     parts = [rng.standard_normal((C, 4)) / 2.0, np.zeros(C)]
     for _ in range(L):
         parts += [rng.standard_normal((K, K, C, C)) / C, rng.standard_normal((K, K, C, C)) / C,
                   rng.standard_normal((C, C)) / math.sqrt(C), np.zeros(C)]
     parts += [rng.standard_normal((C, C)) / math.sqrt(C), np.zeros(C),
-              1e-2 * rng.standard_normal((2, C)) / math.sqrt(C), np.zeros(2)]
+              np.zeros((2, C)), np.zeros(2)]
     return np.concatenate([p.ravel() for p in parts]).astype(np.float32)
 
 
@@ -102,20 +102,49 @@ def training_crystals(n=256, seed=0, random_count=6):
 
 
 def train(net, data_c, data_f, data_t, steps, batch, lr=1e-3, seed=0, log=None):
-    """Adam on random batches of pairs; returns the per-step normalised losses."""
+    """Adam on random batches of pairs; every pair is weighted by the inverse of its
+    own coarse error, so the loss is the mean ratio (corrected error / coarse error)
+    and 1 means no gain.  Returns the per-step losses."""
     g = torch.Generator(device='cpu').manual_seed(seed)
     n = data_c.shape[0]
     losses = []
     for s in range(steps):
         idx = torch.randint(0, n, (batch,), generator=g).to(data_c.device)
         c, f, t = data_c[idx].contiguous(), data_f[idx].contiguous(), data_t[idx].contiguous()
-        denom = float((f - c).abs().pow(2).sum().item())
-        loss = net.loss_grad(c, t, f, denom)
+        w = 1.0 / (f - c).abs().pow(2).sum((1, 2)).clamp_min(1e-20).float()
+        loss = net.loss_grad(c, t, f, float(batch), weights=w.contiguous())
         net.adam(lr=lr * (0.5 * (1 + math.cos(math.pi * s / steps))))
         losses.append(float(loss.item()))
         if log and s % 100 == 0:
             log(f'step {s} loss {losses[-1]:.4f}')
     return losses
+
+
+def rollout_pairs(net, crystal, positions, steps=None):
+    """Pairs taken along the corrector's own trajectory: at every coarse step the
+    target is four fine steps from the current corrected wave.  Training on them
+    teaches the network the states it meets when it is applied repeatedly."""
+    w = crystal.waves(positions)
+    steps = crystal.coarse_steps if steps is None else min(steps, crystal.coarse_steps)
+    out_c, out_f, idx = [], [], []
+    B = w.shape[0]
+    for k in range(steps):
+        c = w.clone()
+        crystal.plan.step_waves(c, crystal.trans_coarse[k], crystal.ptab_coarse)
+        f = w.clone()
+        for j in range(crystal.ratio * k, crystal.ratio * (k + 1)):
+            crystal.plan.step_waves(f, crystal.trans_fine[j], crystal.ptab_fine)
+        cs, fs = c * crystal.scale, f * crystal.scale
+        out_c.append(cs)
+        out_f.append(fs)
+        idx.append(torch.full((B,), k, dtype=torch.long, device=w.device))
+        nxt = torch.empty_like(cs)
+        for b0 in range(0, B, net.max_batch):
+            chunk = cs[b0:b0 + net.max_batch].contiguous()
+            tc = crystal.trans_coarse[k].expand(chunk.shape[0], -1, -1).contiguous()
+            nxt[b0:b0 + net.max_batch] = net.forward(chunk, tc)
+        w = (nxt / crystal.scale).contiguous()
+    return torch.cat(out_c), torch.cat(out_f), torch.cat(idx)
 
 
 def corrected_multislice(net, crystal, positions, steps=None, use_net=True):
@@ -151,6 +180,7 @@ def rel_l2(a, b):
 
 
 def timed(fn, reps=3):
+    fn()  # first call outside the timing (lazy set-up)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     for _ in range(reps):

@@ -12,7 +12,8 @@
 //   h  = gelu(P1 a_L + c1);  o = P2 h + c2                          (2 channels)
 //   psi_pred = psi_c + (o_0 + i o_1)
 // Waves are scaled by sqrt(H W) by the caller so that they are O(1).
-// Loss: sum |psi_pred - psi_f|^2 / denom.  gelu is the tanh form.
+// Loss: sum_b w_b sum |psi_pred - psi_f|^2 / denom (w_b = 1 without sample
+// weights).  gelu is the tanh form.
 // All arithmetic is FP32; reductions over pixels are two-stage and ordered.
 #include "msx.h"
 #include "msx_internal.h"
@@ -326,8 +327,8 @@ __global__ void mix_bwd_data_kernel(const float* __restrict__ Rr, const float* _
 
 // psi_pred = psi_c + (o0 + i o1); with a target: dO = 2 (psi_pred - psi_f) / denom and per-block sums of |r|^2
 __global__ void output_kernel(const float* __restrict__ o, const float2* __restrict__ psi_c, const float2* __restrict__ psi_f,
-                              int HW, int B, float inv_denom, float2* __restrict__ pred, float* __restrict__ dO,
-                              double* __restrict__ block_sums) {
+                              int HW, int B, float inv_denom, const float* __restrict__ sample_w, float2* __restrict__ pred,
+                              float* __restrict__ dO, double* __restrict__ block_sums) {
   __shared__ double red[256];
   const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   double sq = 0;
@@ -340,9 +341,10 @@ __global__ void output_kernel(const float* __restrict__ o, const float2* __restr
     if (psi_f) {
       const float2 f = psi_f[i];
       const float rx = w.x - f.x, ry = w.y - f.y;
-      sq = (double)rx * rx + (double)ry * ry;
-      dO[((size_t)b * 2) * HW + p] = 2.f * rx * inv_denom;
-      dO[((size_t)b * 2 + 1) * HW + p] = 2.f * ry * inv_denom;
+      const float wt = sample_w ? sample_w[b] * inv_denom : inv_denom;
+      sq = ((double)rx * rx + (double)ry * ry) * (double)wt;
+      dO[((size_t)b * 2) * HW + p] = 2.f * rx * wt;
+      dO[((size_t)b * 2 + 1) * HW + p] = 2.f * ry * wt;
     }
   }
   if (!block_sums) return;
@@ -589,13 +591,14 @@ int msx_corrector_forward(msx_corrector* k, const float* psi_c_dev, const float*
   if (rc) return rc;
   const long long nb = (long long)batch * k->H * k->W;
   output_kernel<<<blocks_for(nb, 256), 256, 0, st>>>(k->o, reinterpret_cast<const float2*>(psi_c_dev), nullptr, k->H * k->W,
-                                                     batch, 0.f, reinterpret_cast<float2*>(pred_out_dev), nullptr, nullptr);
+                                                     batch, 0.f, nullptr, reinterpret_cast<float2*>(pred_out_dev), nullptr,
+                                                     nullptr);
   NN_CUDA(cudaGetLastError());
   return MSX_OK;
 }
 
 int msx_corrector_loss_grad(msx_corrector* k, const float* psi_c_dev, const float* tc_dev, const float* psi_f_dev,
-                            int batch, double denom, float* loss_out_dev, void* stream) {
+                            int batch, double denom, const float* sample_weights_dev, float* loss_out_dev, void* stream) {
   if (!k || !psi_c_dev || !tc_dev || !psi_f_dev || batch < 1 || batch > k->maxB || !(denom > 0))
     return cfail(MSX_ERR_INVALID, "corrector loss: bad arguments");
   cudaStream_t st = (cudaStream_t)stream;
@@ -605,8 +608,8 @@ int msx_corrector_loss_grad(msx_corrector* k, const float* psi_c_dev, const floa
   const unsigned nblk = blocks_for(nb, 256);
   output_kernel<<<nblk, 256, 0, st>>>(k->o, reinterpret_cast<const float2*>(psi_c_dev),
                                        reinterpret_cast<const float2*>(psi_f_dev), k->H * k->W, batch,
-                                       (float)(1.0 / denom), nullptr, k->dO, k->sums);
-  sum_blocks_kernel<<<1, 32, 0, st>>>(k->sums, (int)nblk, 1.0 / denom, loss_out_dev ? loss_out_dev : k->loss);
+                                       (float)(1.0 / denom), sample_weights_dev, nullptr, k->dO, k->sums);
+  sum_blocks_kernel<<<1, 32, 0, st>>>(k->sums, (int)nblk, 1.0, loss_out_dev ? loss_out_dev : k->loss);
   rc = backward(k, batch, st);
   return rc;
 }

@@ -390,14 +390,17 @@ class Corrector:
         _lib.check(lib().msx_corrector_forward(self._h, _ptr(psi_c), _ptr(tc), psi_c.shape[0], _ptr(out), _stream()))
         return out
 
-    def loss_grad(self, psi_c, tc, psi_f, denom, loss_out=None):
+    def loss_grad(self, psi_c, tc, psi_f, denom, weights=None, loss_out=None):
+        """Loss sum_b w_b |pred_b - psi_f_b|^2 / denom and the parameter gradients."""
         _need(psi_c, torch.complex64, 'psi_c', 3)
         _need(tc, torch.complex64, 'tc', 3)
         _need(psi_f, torch.complex64, 'psi_f', 3)
+        if weights is not None:
+            _need(weights, torch.float32, 'weights', 1)
         if loss_out is None:
             loss_out = torch.empty(1, dtype=torch.float32, device=psi_c.device)
         _lib.check(lib().msx_corrector_loss_grad(self._h, _ptr(psi_c), _ptr(tc), _ptr(psi_f), psi_c.shape[0],
-                                                 float(denom), _ptr(loss_out), _stream()))
+                                                 float(denom), _ptr(weights), _ptr(loss_out), _stream()))
         return loss_out
 
     def adam(self, lr=1e-3, beta1=0.9, beta2=0.999, eps=1e-8):
