@@ -289,9 +289,8 @@ MSX_API int msx_batch_check(msx_batch* batch);
 /*
  * Split-BF16 tensor-core DFT stages (precision study; no reference
  * counterpart).  A length-n DFT of complex lines as a 2n x 2n real GEMM on
- * tcgen05 with bfloat16 operand splits and FP32 accumulation: the data in two
- * parts, the DFT matrix in three, five products (x_hi b_hi + x_hi b_mid +
- * x_lo b_hi + x_hi b_lo + x_lo b_mid).  n = 256 or 512.
+ * tcgen05 with bfloat16 hi/lo operand splits (hi.hi + hi.lo + lo.hi, FP32
+ * accumulation).  n = 256 or 512.
  *  msx_tc_dft:        z (lines, n) = sum_m x[m] e^{sign 2 pi i m k / n}, lines % 128 == 0
  *  msx_step_waves_tc: the msx_plan_step_waves slice with all four 1-D DFTs on the
  *                     tensor cores (square n x n grids)

@@ -2,21 +2,17 @@
 //
 // A length-N complex DFT of L lines is the real GEMM
 //   [Zr | Zi] (L x 2N) = [Xr | Xi] (L x 2N) . B^T,  B (2N x 2N) built from cos/sin,
-// run on bfloat16 operand splits accumulated in FP32 in tensor memory.  The
-// data X is split in two (x = x_hi + x_lo, ~16 significant bits) and the
-// constant DFT matrix in three (b = b_hi + b_mid + b_lo, ~24 bits): the five
-// products x_hi b_hi + x_hi b_mid + x_lo b_hi + x_hi b_lo + x_lo b_mid keep the
-// matrix at FP32 accuracy, so its (otherwise systematic, repeated every slice)
-// representation error does not accumulate over hundreds of slices; the
-// remaining error of the data split is random from slice to slice.  This is
-// the precision-study form of the multislice step for grids up to 512^2; the
-// FP32 FFT passes remain the production path.
+// run with both operands split into bfloat16 pairs x = hi + lo and the three
+// products hi.hi + hi.lo + lo.hi accumulated in FP32 in tensor memory (the
+// lo.lo term, below FP32 rounding of the sum, is dropped).  This is the
+// precision-study form of the multislice step for grids up to 512^2; the FP32
+// FFT passes remain the production path.
 //
-// GEMM kernel: one CTA computes a 128 x 128 tile of Z.  Operand tiles are
+// GEMM kernel: one CTA computes a 128 x 256 tile of Z.  Operand tiles are
 // stored in global memory already in the tensor-core shared-memory layout
 // (K-major, 128-byte swizzle: 8-row atoms of 128 B, 16-byte chunk c of row r
-// at chunk c ^ (r mod 8)), so each K block (64 bf16) of A_hi, A_lo, B_hi,
-// B_mid, B_lo arrives with five 1-D bulk copies.  Warp 0 lane 0 produces (double-buffered,
+// at chunk c ^ (r mod 8)), so each K block (64 bf16) of A_hi, A_lo, B_hi, B_lo
+// arrives with four 1-D bulk copies.  Warp 0 lane 0 produces (double-buffered,
 // mbarrier full/empty), warp 1 lane 0 issues tcgen05.mma (M=128, N=256, K=16)
 // and commits to the stage's empty barrier; all four warps then read the
 // accumulator with tcgen05.ld and write FP32 results.  Every mbarrier wait is
@@ -34,11 +30,11 @@
 namespace msx {
 namespace tc {
 
-constexpr int BM = 128, BN = 128, BK = 64, STAGES = 2;
+constexpr int BM = 128, BN = 256, BK = 64, STAGES = 2;
 constexpr int A_BYTES = BM * BK * 2;                     // 16 KB
-constexpr int B_BYTES = BN * BK * 2;                     // 16 KB
-constexpr int STAGE_BYTES = 2 * A_BYTES + 3 * B_BYTES;   // 80 KB
-constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 1024;  // 160 KB + alignment slack (dynamic)
+constexpr int B_BYTES = BN * BK * 2;                     // 32 KB
+constexpr int STAGE_BYTES = 2 * A_BYTES + 2 * B_BYTES;   // 96 KB
+constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 1024;  // 192 KB + alignment slack (dynamic)
 
 // byte offset of element (row, k) (k in [0, 64)) inside a 128B-swizzled K-major block
 __host__ __device__ __forceinline__ uint32_t sw128_offset(int row, int k) {
@@ -70,8 +66,8 @@ __device__ __forceinline__ void mma_commit(uint64_t* bar) {
 
 __global__ void __launch_bounds__(128, 1)
 tc_gemm_kernel(const uint8_t* __restrict__ a_hi, const uint8_t* __restrict__ a_lo, const uint8_t* __restrict__ b_hi,
-               const uint8_t* __restrict__ b_mid, const uint8_t* __restrict__ b_lo, int kblocks, int ntiles_n, int N,
-               float* __restrict__ Z, int* __restrict__ err) {
+               const uint8_t* __restrict__ b_lo, int kblocks, int ntiles_n, int N, float* __restrict__ Z,
+               int* __restrict__ err) {
   extern __shared__ __align__(1024) uint8_t smem_raw[];
   // the 128-byte swizzle is anchored to 1024-byte boundaries: align the stages explicitly
   uint8_t* smem = smem_raw + ((1024u - (smem_u32(smem_raw) & 1023u)) & 1023u);
@@ -112,8 +108,7 @@ tc_gemm_kernel(const uint8_t* __restrict__ a_hi, const uint8_t* __restrict__ a_l
       bulk_g2s(st, a_hi + a_tile + (size_t)kb * A_BYTES, A_BYTES, &full[s]);
       bulk_g2s(st + A_BYTES, a_lo + a_tile + (size_t)kb * A_BYTES, A_BYTES, &full[s]);
       bulk_g2s(st + 2 * A_BYTES, b_hi + b_tile + (size_t)kb * B_BYTES, B_BYTES, &full[s]);
-      bulk_g2s(st + 2 * A_BYTES + B_BYTES, b_mid + b_tile + (size_t)kb * B_BYTES, B_BYTES, &full[s]);
-      bulk_g2s(st + 2 * A_BYTES + 2 * B_BYTES, b_lo + b_tile + (size_t)kb * B_BYTES, B_BYTES, &full[s]);
+      bulk_g2s(st + 2 * A_BYTES + B_BYTES, b_lo + b_tile + (size_t)kb * B_BYTES, B_BYTES, &full[s]);
     }
   } else if (threadIdx.x == 32) {  // MMA issuer
     for (int kb = 0; kb < kblocks; ++kb) {
@@ -124,16 +119,14 @@ tc_gemm_kernel(const uint8_t* __restrict__ a_hi, const uint8_t* __restrict__ a_l
       }
       asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
       const uint32_t st = smem_u32(smem + s * STAGE_BYTES);
-      const uint32_t ahi = st, alo = st + A_BYTES, bhi = st + 2 * A_BYTES, bmid = bhi + B_BYTES, blo = bmid + B_BYTES;
+      const uint32_t ahi = st, alo = st + A_BYTES, bhi = st + 2 * A_BYTES, blo = st + 2 * A_BYTES + B_BYTES;
 #pragma unroll
       for (int j = 0; j < BK / 16; ++j) {  // K = 16 per MMA: 32 bytes along the swizzled row
         const uint32_t off = (uint32_t)j * 32u;
         const uint32_t acc0 = (kb > 0 || j > 0) ? 1u : 0u;
         mma_bf16(tmem, smem_desc(ahi + off), smem_desc(bhi + off), acc0);
-        mma_bf16(tmem, smem_desc(ahi + off), smem_desc(bmid + off), 1u);
-        mma_bf16(tmem, smem_desc(alo + off), smem_desc(bhi + off), 1u);
         mma_bf16(tmem, smem_desc(ahi + off), smem_desc(blo + off), 1u);
-        mma_bf16(tmem, smem_desc(alo + off), smem_desc(bmid + off), 1u);
+        mma_bf16(tmem, smem_desc(alo + off), smem_desc(bhi + off), 1u);
       }
       mma_commit(&empty[s]);  // the stage is free once these MMAs have read it
     }
@@ -222,12 +215,10 @@ int tfail(int code, const char* msg) {
 }
 
 // B (2N x 2N) of a DFT of sign s (e^{s 2 pi i n k / N}) in 128B-swizzled K-major
-// tiles of BN rows x 64 columns, split into bf16 hi, mid and lo (from the double values).
-void build_dft_tiles(int N, int sign, std::vector<__nv_bfloat16>& hi, std::vector<__nv_bfloat16>& mid,
-                     std::vector<__nv_bfloat16>& lo) {
+// tiles of 256 rows x 64 columns, split into bf16 hi and lo.
+void build_dft_tiles(int N, int sign, std::vector<__nv_bfloat16>& hi, std::vector<__nv_bfloat16>& lo) {
   const int K = 2 * N, NO = 2 * N, kblocks = K / BK, ntiles = NO / BN;
   hi.assign((size_t)NO * K, __float2bfloat16(0.f));
-  mid.assign((size_t)NO * K, __float2bfloat16(0.f));
   lo.assign((size_t)NO * K, __float2bfloat16(0.f));
   const double two_pi = 6.283185307179586476925286766559;
   for (int j = 0; j < NO; ++j)
@@ -238,14 +229,12 @@ void build_dft_tiles(int N, int sign, std::vector<__nv_bfloat16>& hi, std::vecto
       double v;
       if (j < N) v = kk < N ? c : -sign * s;   // Zr = Xr cos - s Xi sin
       else v = kk < N ? sign * s : c;           // Zi = s Xr sin + Xi cos
-      const __nv_bfloat16 h = __float2bfloat16_rn((float)v);
-      const double r1 = v - (double)__bfloat162float(h);
-      const __nv_bfloat16 m = __float2bfloat16_rn((float)r1);
-      const __nv_bfloat16 l = __float2bfloat16_rn((float)(r1 - (double)__bfloat162float(m)));
+      const float f = (float)v;
+      const __nv_bfloat16 h = __float2bfloat16_rn(f);
+      const __nv_bfloat16 l = __float2bfloat16_rn(f - __bfloat162float(h));
       const int nt = j / BN, r = j % BN, kb = kk / BK;
       const size_t byte = ((size_t)nt * kblocks + kb) * B_BYTES + sw128_offset(r, kk % BK);
       hi[byte / 2] = h;
-      mid[byte / 2] = m;
       lo[byte / 2] = l;
     }
   (void)ntiles;
@@ -253,8 +242,7 @@ void build_dft_tiles(int N, int sign, std::vector<__nv_bfloat16>& hi, std::vecto
 
 struct TcState {
   int N = 0;
-  __nv_bfloat16 *fwd_hi = nullptr, *fwd_mid = nullptr, *fwd_lo = nullptr;
-  __nv_bfloat16 *inv_hi = nullptr, *inv_mid = nullptr, *inv_lo = nullptr;
+  __nv_bfloat16 *fwd_hi = nullptr, *fwd_lo = nullptr, *inv_hi = nullptr, *inv_lo = nullptr;
   __nv_bfloat16 *a_hi = nullptr, *a_lo = nullptr;
   float2 *z0 = nullptr, *z1 = nullptr, *ptab_t = nullptr;
   int* err = nullptr;
@@ -266,21 +254,18 @@ thread_local TcState g_tc;  // one per host thread; sized by the largest call
 int tc_prepare(int N, size_t lines) {
   TcState& s = g_tc;
   if (s.N != N) {
-    for (void* p : {(void*)s.fwd_hi, (void*)s.fwd_mid, (void*)s.fwd_lo, (void*)s.inv_hi, (void*)s.inv_mid,
-                    (void*)s.inv_lo})
+    for (void* p : {(void*)s.fwd_hi, (void*)s.fwd_lo, (void*)s.inv_hi, (void*)s.inv_lo})
       if (p) cudaFree(p);
-    std::vector<__nv_bfloat16> h, m, l;
+    std::vector<__nv_bfloat16> h, l;
     const size_t bytes = sizeof(__nv_bfloat16) * 4 * (size_t)N * N;
-    if (cudaMalloc(&s.fwd_hi, bytes) || cudaMalloc(&s.fwd_mid, bytes) || cudaMalloc(&s.fwd_lo, bytes) ||
-        cudaMalloc(&s.inv_hi, bytes) || cudaMalloc(&s.inv_mid, bytes) || cudaMalloc(&s.inv_lo, bytes))
+    if (cudaMalloc(&s.fwd_hi, bytes) || cudaMalloc(&s.fwd_lo, bytes) || cudaMalloc(&s.inv_hi, bytes) ||
+        cudaMalloc(&s.inv_lo, bytes))
       return tfail(MSX_ERR_ALLOC, "tensor-core DFT matrices: allocation failed");
-    build_dft_tiles(N, -1, h, m, l);
+    build_dft_tiles(N, -1, h, l);
     cudaMemcpy(s.fwd_hi, h.data(), bytes, cudaMemcpyHostToDevice);
-    cudaMemcpy(s.fwd_mid, m.data(), bytes, cudaMemcpyHostToDevice);
     cudaMemcpy(s.fwd_lo, l.data(), bytes, cudaMemcpyHostToDevice);
-    build_dft_tiles(N, +1, h, m, l);
+    build_dft_tiles(N, +1, h, l);
     cudaMemcpy(s.inv_hi, h.data(), bytes, cudaMemcpyHostToDevice);
-    cudaMemcpy(s.inv_mid, m.data(), bytes, cudaMemcpyHostToDevice);
     cudaMemcpy(s.inv_lo, l.data(), bytes, cudaMemcpyHostToDevice);
     s.N = N;
     s.lines_cap = 0;
@@ -315,7 +300,6 @@ int tc_dft(const float2* X, size_t lines, int N, const float2* mult, int lm, int
   tc_gemm_kernel<<<grid, 128, SMEM_BYTES, st>>>(reinterpret_cast<const uint8_t*>(s.a_hi),
                                                  reinterpret_cast<const uint8_t*>(s.a_lo),
                                                  reinterpret_cast<const uint8_t*>(sign < 0 ? s.fwd_hi : s.inv_hi),
-                                                 reinterpret_cast<const uint8_t*>(sign < 0 ? s.fwd_mid : s.inv_mid),
                                                  reinterpret_cast<const uint8_t*>(sign < 0 ? s.fwd_lo : s.inv_lo),
                                                  kblocks, ntn, N, reinterpret_cast<float*>(Z), s.err);
   const cudaError_t e = cudaGetLastError();
