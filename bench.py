@@ -40,9 +40,13 @@ METRIC = 'STEM probe-positions/sec at ≤1e-3 CBED rel. error vs FP64; learned v
 UNIT = 'probe-positions/s'
 A_SI = 5.431
 WORKLOAD = 'Si[001] 8x8x50 cells, 512x512 c64, 199 slices (t=a/4), 200 keV, 30 mrad, Cs=1um, 32x32 positions, crop 256'
-# DRAM bytes per launch of the dominant pass, from the ncu capture summarised in
-# profiles/ (keyed by line length, schedule index, waves per launch); None until captured.
-NCU_TRAFFIC = {}
+# DRAM bytes (read + write) per launch of a pass, from the ncu --set full capture
+# summarised in profiles/row_col_tma_passes_si512_g512.md, keyed by (pass, line
+# length, schedule index, waves per launch); other keys report null.
+NCU_TRAFFIC = {
+    ('row', 512, 1, 512): 1.076813e9 + 1.012529e9,   # row_pass_tma_kernel t32_r16x16x2
+    ('col', 512, 0, 512): 1.198959e9 + 1.012810e9,   # col_mid_tma_kernel t16_r32x16
+}
 
 
 def parse():
@@ -328,7 +332,7 @@ def run_ours(args):
     sm_clock = (clk.get('sm_mhz') or 1900.0)
     fp32_peak = 152 * 128 * 2 * sm_clock * 1e6 / 1e12
     roof = {'bound': 'hbm', 'achieved': achieved, 'peak': hbm_peak, 'unit': 'GB/s', 'frac': achieved / hbm_peak,
-            'traffic': NCU_TRAFFIC.get((512, plan.schedule[0] if dom == 'row' else plan.schedule[1], gw)),
+            'traffic': NCU_TRAFFIC.get((dom, 512, plan.schedule[0] if dom == 'row' else plan.schedule[1], gw)),
             'kernel': f'{dom}_pass_kernel (512, {gw} waves per launch)', 'peak_source': f'{peak_src} hbm_gbs',
             'launch_ms': dom_ms, 'row_pass_ms': row_ms, 'col_pass_ms': col_ms,
             'fp32': {'achieved_tflops': alg_flops / (dom_ms / 1e3) / 1e12, 'peak_tflops': fp32_peak,
@@ -503,9 +507,12 @@ def run_precision(args):
             dt = time.perf_counter() - t1
             g = got.cpu().numpy()[sample]
             e = O.rel_l2(g, ref)
+            # total-intensity ratio: a value below 1 is a systematic loss of norm
+            # (rounding towards zero), not random rounding noise
+            ratio = g.reshape(len(sample), -1).sum(1) / ref.reshape(len(sample), -1).sum(1)
             res[form] = {'rel_l2_mean': float(e.mean()), 'rel_l2_max': float(e.max()),
                          'max_abs': float(np.abs(g - ref).max()), 'max_ref': float(np.abs(ref).max()),
-                         'probes_per_s': 64 / dt}
+                         'intensity_ratio': float(ratio.mean()), 'probes_per_s': 64 / dt}
         out[f'{n}x{n}'] = res
     line = {'metric': METRIC, 'value': out['1024x1024']['fp32_fft']['probes_per_s'], 'unit': UNIT, 'n_gpus': 1,
             'steps': 1, 'warmup': 0, 'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None,
