@@ -211,7 +211,75 @@ def run_reference(args):
                              'sample': f'{nprobe} of the 1024 positions per step, 199 slices, 512^2, '
                                        f'process pool of {procs} (reference CPU MSA path restated in oracle/)'},
             'e2e': {'value': value, 'unit': UNIT, 'h2d_bytes_per_step': 0, 'd2h_bytes_per_step': 0}}
+    line['reference_gpu'] = reference_gpu_leg(args)
     print(json.dumps(line), flush=True)
+
+
+def reference_gpu_leg(args):
+    """The reference's own GPU path on this GPU: its rendered kernels and cuFFT in
+    MSAGPU.multislice's order (oracle/refgpu_harness.cu), on the same 1024-position
+    Si 512^2 scan.  `value` times the device work of one multislice call (probe
+    stack, 199 x [t/N, FFT, P, IFFT], final FFT and |.|^2) with CUDA events; `call_ms`
+    adds what the reference's call also does each time: the batched cuFFT plan,
+    the propagator, the D2H copy of the complex stack and the host-side division
+    by the normalisation (namsa/msa.py:767-924)."""
+    try:
+        import torch
+        if not torch.cuda.is_available():
+            return {'unavailable': 'no GPU on this host'}
+        from oracle import msa_oracle as O
+        from oracle import refgpu as R
+        ref = R.RefGPU('c2')
+    except Exception as e:  # harness not rendered/built here
+        return {'unavailable': f'reference GPU harness not available: {e}'.splitlines()[0]}
+    torch.cuda.set_device(0)
+    meta = ref.meta
+    sc = O.si_supercell(*meta['cells'])
+    geom = O.Geometry(np.column_stack([sc['x'], sc['y'], sc['z']]), sc['atomic_number'], meta['kv'], meta['semi'],
+                      [512, 512])
+    _, win = O.atom_windows(geom, np.load(os.path.join(ROOT, 'namsa_gb300', 'data', 'kirkland_params.npy')))
+    trans = ref.build_potential(geom, meta['slice_t'], win)
+    kmax = np.float32(geom.kmax)
+    ab = PROBE['aberration_dict']
+    psik, _, _, norm = ref.build_probe(kmax, np.float32(geom.semi_ang / geom.lam), geom.lam, ab['C1'], ab['C3'],
+                                       ab['C5'], PROBE['smooth_apert'])
+    pos = torch.from_numpy(scan_positions(0)).cuda()
+    P = int(pos.shape[0])
+    psi = torch.empty((P, 512, 512), dtype=torch.complex64, device='cuda')
+    host = torch.empty((P, 512, 512), dtype=torch.complex64, pin_memory=True)
+    ctx = ref.context(P)
+    try:
+        ref.propagator(ctx, kmax, np.float32(geom.kmax / 3), meta['slice_t'], geom.lam)
+        for _ in range(max(1, args.warmup)):
+            ref.propagate(ctx, trans, psik, pos, kmax, psi)
+        st = torch.cuda.current_stream()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record(st)
+        for _ in range(args.steps):
+            ref.propagate(ctx, trans, psik, pos, kmax, psi)
+        e1.record(st)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / args.steps
+    finally:
+        ref.destroy(ctx)
+    # one whole call as the reference makes it (plan, propagator, beams, D2H, host scaling)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    ctx = ref.context(P)
+    try:
+        ref.propagator(ctx, kmax, np.float32(geom.kmax / 3), meta['slice_t'], geom.lam)
+        ref.propagate(ctx, trans, psik, pos, kmax, psi)
+        host.copy_(psi)
+        out = (host.numpy() / norm).real.astype(np.float32)
+    finally:
+        ref.destroy(ctx)
+    call_ms = (time.perf_counter() - t0) * 1e3
+    del out
+    return {'value': P / (ms / 1e3), 'unit': UNIT, 'ms_per_step': ms, 'call_ms': call_ms,
+            'call_value': P / (call_ms / 1e3), 'positions': P, 'slices': int(trans.shape[0]),
+            'kind': 'reference kernels (rendered from namsa/probe_kernels.cu, potential_kernels.cu) + cuFFT, '
+                    'MSAGPU call order, one batch of 1024'}
 
 
 def run_ours(args):

@@ -15,7 +15,7 @@ Two convention sets exist in the reference and both are restated here:
   order (reversed, msa.py:337,346), aperture smoothing (``apert_smooth``
   instead of the kernel's fixed 80, probe_kernels.cu:203-204), window
   placement (``int()`` truncation, msa.py:169-171, instead of ``rintf`` around
-  an integer centre, potential_kernels.cu:331-337), the bandwidth mask
+  an integer centre, potential_kernels.cu:30-33), the bandwidth mask
   (pixel-radius ``N*bw`` around ``N/2``, msa.py:245-251, instead of
   ``k < bw*kmax``, msa.py:833), and the Scherzer rule (only when C3 > 1,
   optics.py:84-88).  The CPU conventions are pinned against the reference
@@ -27,7 +27,7 @@ Two convention sets exist in the reference and both are restated here:
 Precision: ``dtype=np.float64`` evaluates everything in FP64 (the accuracy
 oracle).  ``potential_slices_gpu(..., mode="f32")`` reproduces the kernel's
 sequential float32 accumulation bit for bit (one thread per pixel adds the
-sites of its slice in site order, potential_kernels.cu:325-347).
+sites of its slice in site order, potential_kernels.cu:25-41).
 """
 from __future__ import annotations
 
@@ -171,7 +171,7 @@ def potential_slices_gpu(sites, windows, sampling, mode="f64"):
 
 
 def transmission(V, sigma, mode="f64"):
-    """t = exp(i sigma V) (potential_kernels.cu:352-362; msa.py:334 for the CPU path)."""
+    """t = exp(i sigma V) (potential_kernels.cu:48-57; msa.py:334 for the CPU path)."""
     if mode == "f32":
         arg = V.astype(np.float32) * np.float32(sigma)
         t = np.empty(V.shape, np.complex64)

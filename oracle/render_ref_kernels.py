@@ -1,0 +1,92 @@
+"""Render the reference's CUDA kernel templates for the reference-GPU harness -- TEST INFRASTRUCTURE ONLY.
+
+The reference compiles its kernels at run time: jinja2 fills the grid size (and,
+for the potential kernel, the window shape, the padded site-list length and the
+slice count) into namsa/probe_kernels.cu and namsa/potential_kernels.cu, and
+pycuda's SourceModule compiles the result (namsa/cuda_kernels.py:8-57).  This
+script performs the same rendering, with the same template variables, for the
+two Si [001] workloads the parity tests use, and writes the rendered sources
+into ``oracle/_ref/`` (git-ignored, never part of the product):
+
+  c1  Si 4x4x20 cells (face-inclusive), 256^2, 100 keV, t = a/4 (80 slices)
+  c2  Si 8x8x50 cells (face-inclusive), 512^2, 200 keV, t = a/4 (199 slices)
+
+plus ``oracle/_ref/workloads.json`` with the rendered parameters.  The sources
+are then compiled against the stand-in header ``oracle/pycuda-complex.hpp`` and
+the harness ``oracle/refgpu_harness.cu`` by ``oracle/build_ref.py``.
+
+The rendering needs the reference checkout (``/root/reference`` by default, or
+the ``NAMSA_REFERENCE`` environment variable); machines without it use the
+rendered files already present in ``oracle/_ref/``.
+"""
+from __future__ import annotations
+
+import json
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(HERE)
+OUT = os.path.join(HERE, '_ref')
+REFERENCE = os.environ.get('NAMSA_REFERENCE', '/root/reference')
+
+A_SI = 5.431
+WORKLOADS = {
+    'c1': dict(cells=(4, 4, 20), n=256, kv=100.0, semi=20e-3),
+    'c2': dict(cells=(8, 8, 50), n=512, kv=200.0, semi=30e-3),
+}
+
+
+def workload_params(tag):
+    """Grid, window shape, slice count and padded site-list length of a workload,
+    computed with the oracle's restatement of the reference's set-up."""
+    sys.path.insert(0, ROOT)
+    from oracle import msa_oracle as O
+    w = WORKLOADS[tag]
+    sc = O.si_supercell(*w['cells'])
+    xyz = np.column_stack([sc['x'], sc['y'], sc['z']]).astype(np.float32)
+    geom = O.Geometry(xyz, sc['atomic_number'], w['kv'], w['semi'], [w['n'], w['n']])
+    kirk = np.load(os.path.join(ROOT, 'namsa_gb300', 'data', 'kirkland_params.npy'))
+    _, win = O.atom_windows(geom, kirk)
+    t = A_SI / 4
+    sites = O.slice_sites_gpu(geom, t)
+    max_sites = max(len(s) for s in sites)
+    return dict(tag=tag, ny=w['n'], nx=w['n'], pot_y=int(win.shape[1]), pot_x=int(win.shape[2]),
+                num_slices=len(sites), sites_size=3 * max_sites, species=int(win.shape[0]),
+                cells=list(w['cells']), kv=w['kv'], semi=w['semi'], slice_t=t)
+
+
+def render(reference=REFERENCE, out=OUT):
+    from jinja2 import Template
+    os.makedirs(out, exist_ok=True)
+    with open(os.path.join(reference, 'namsa', 'probe_kernels.cu')) as f:
+        probe_t = Template(f.read())
+    with open(os.path.join(reference, 'namsa', 'potential_kernels.cu')) as f:
+        pot_t = Template(f.read())
+    meta = {}
+    for tag in WORKLOADS:
+        p = workload_params(tag)
+        # same variables as ProbeKernels / PotentialKernels (namsa/cuda_kernels.py:16-19, 42-51)
+        probe_src = probe_t.render(type='pycuda::complex<float>', y_sampling=np.int32(p['ny']),
+                                   x_sampling=np.int32(p['nx']))
+        pot_src = pot_t.render(y_sampling=np.int32(p['ny']), x_sampling=np.int32(p['nx']),
+                               pot_shape_y=np.int32(p['pot_y']), pot_shape_x=np.int32(p['pot_x']),
+                               sites_size=np.int32(p['sites_size']), num_slices=np.int32(p['num_slices']))
+        with open(os.path.join(out, f'ref_probe_kernels_{tag}.cu'), 'w') as f:
+            f.write(probe_src)
+        with open(os.path.join(out, f'ref_potential_kernels_{tag}.cu'), 'w') as f:
+            f.write(pot_src)
+        meta[tag] = p
+    with open(os.path.join(out, 'workloads.json'), 'w') as f:
+        json.dump(meta, f, indent=1)
+    return meta
+
+
+def available(reference=REFERENCE):
+    return os.path.exists(os.path.join(reference, 'namsa', 'probe_kernels.cu'))
+
+
+if __name__ == '__main__':
+    print(json.dumps(render(), indent=1))

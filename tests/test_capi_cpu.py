@@ -47,3 +47,33 @@ def test_argument_errors_without_device(libmsx):
     assert libmsx.msx_multislice(None, None, 1, None, None, None, 1, 1.0, 0.02, 1.0, 1.0, None, 1, 1, None) == \
         _lib.MSX_ERR_INVALID
     assert libmsx.msx_plan_destroy(None) == 0
+
+
+def test_reference_gpu_harness_exports_and_site_layout():
+    """The checker's reference-GPU harness (oracle/refgpu_harness.cu) loads, exports
+    its entry points, and lays out site lists as the reference does (triplets of
+    window index, y pixel, x pixel per slice) with the zero-window index as padding."""
+    import numpy as np
+    import pytest
+    from oracle import msa_oracle as O
+    from oracle import refgpu as R
+    try:
+        ref = R.RefGPU('c1')
+    except R.RefGPUUnavailable as e:
+        pytest.skip(str(e))
+    for name in ['refgpu_build_potential', 'refgpu_build_probe', 'refgpu_ctx_create', 'refgpu_ctx_destroy',
+                 'refgpu_propagator', 'refgpu_propagate', 'refgpu_shape', 'refgpu_last_error']:
+        assert hasattr(ref.L, name)
+    meta = ref.meta
+    assert (ref.ny, ref.nx, ref.S) == (meta['ny'], meta['nx'], meta['num_slices'])
+    sc = O.si_supercell(*meta['cells'])
+    geom = O.Geometry(np.column_stack([sc['x'], sc['y'], sc['z']]), sc['atomic_number'], meta['kv'], meta['semi'],
+                      [meta['ny'], meta['nx']])
+    sites = ref.sites(geom, meta['slice_t'], 1)
+    assert sites.shape == (ref.S, ref.sites_size)
+    want = O.slice_sites_gpu(geom, meta['slice_t'])
+    for s in range(ref.S):
+        trip = sites[s].reshape(-1, 3)
+        n = len(want[s])
+        np.testing.assert_array_equal(trip[:n], want[s].astype(np.float32))
+        assert np.all(trip[n:, 0] == 1)
