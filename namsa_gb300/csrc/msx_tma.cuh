@@ -3,8 +3,9 @@
 // Each CTA loops over tiles (a group of rows, or a group of columns of one
 // wave).  While it transforms tile i out of one shared-memory stage, the bulk
 // copy engine (cp.async.bulk for rows, cp.async.bulk.tensor for column tiles)
-// fills the other stage with tile i+1; one mbarrier per stage tracks the
-// bytes in flight.  Results go straight from registers to global memory.
+// fills the next stage(s) with the following tiles; one mbarrier per stage
+// tracks the bytes in flight.  Results go straight from registers to global
+// memory.
 //
 // The row pass exchanges Stockham stages in place inside the staged rows, with
 // an XOR swizzle of the element index (bits [S, S+4) folded into bits [0, 4))
@@ -14,11 +15,12 @@
 //   P(kx, ky) mask(kx, ky) / N = px[kx] * py[ky]  for  lo[kx] <= ky <= hi[kx],  else 0,
 // where [lo, hi] is the band of the float32 mask comparison in column kx.
 //
-// Waits: only thread 0 polls an mbarrier, with a clock64 limit of about one
-// second; it publishes the outcome through shared memory and a CTA barrier,
-// so the whole CTA leaves together.  On a timeout the kernel sets bit 0 of
-// *err, waits (again bounded) for the other stage's copy if one was issued,
-// and returns.
+// Waits: every mbarrier wait has a clock64 limit of about one second.  In the
+// column pass thread 0 polls and publishes the outcome through shared memory
+// and a CTA barrier, so the whole CTA leaves together; in the row pass each
+// warp polls for itself and leaves on its own.  On a timeout the kernel sets
+// bit 0 of *err, thread 0 waits (again bounded) for the copies it issued that
+// have not landed, and the threads return.
 #pragma once
 #include <cuda.h>
 #include <cuda_runtime.h>
@@ -90,64 +92,94 @@ struct TmaPassArgs {
 };
 
 // ----------------------------------------------------------------------------- row pass
+// A tile is ROW_LINES rows of one y (from consecutive waves) plus that y's
+// transmission row.  STAGES stages cycle through the CTA's tiles; thread 0 is
+// the producer.  There is no CTA-wide barrier in the loop: every warp waits on
+// the stage's `full` barrier itself, transforms its own rows in place, and
+// releases the stage on its `empty` barrier (one arrival per warp) after a
+// proxy fence (its in-place exchanges are generic-proxy writes that the next
+// bulk copy into the stage must follow).  Thread 0 refills a stage only after
+// all warps released it, so warps may drift up to STAGES - 1 tiles apart.
 template <class S>
 struct RowTma {
   static constexpr int NX = S::N;
   static constexpr int L = S::ROW_LINES;
   static constexpr int STAGE = (L + 1) * NX;  // float2 words: L rows + the transmission row
-  static constexpr size_t smem() { return 16 + sizeof(float2) * ((size_t)2 * STAGE + S::TW_PAD); }
+  static constexpr size_t bytes(int stages) {
+    return sizeof(float2) * ((size_t)stages * STAGE + S::TW_PAD) + 2 * stages * sizeof(uint64_t);
+  }
+  // CTAs per SM that the shared memory allows (228 KB per SM, 1 KB reserved per CTA)
+  static constexpr int fit(int stages) { return (int)(233472 / (bytes(stages) + 1024)); }
+  // three stages when that keeps the occupancy the registers allow, else two
+  static constexpr int STAGES = fit(3) >= (fit(2) < S::MINB ? fit(2) : S::MINB) ? 3 : 2;
+  static constexpr size_t smem() { return bytes(STAGES); }
 };
+
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
 
 template <class S>
 __global__ void __launch_bounds__(S::THREADS, S::MINB) row_pass_tma_kernel(TmaPassArgs a) {
   constexpr int NX = S::N, T = S::T, E = S::E, L = S::ROW_LINES, STAGE = RowTma<S>::STAGE;
+  constexpr int NS = RowTma<S>::STAGES, WARPS = S::WARPS;
   extern __shared__ __align__(1024) float2 smem[];
-  float2* stage = smem;                                   // 2 stages
-  float2* tw = smem + 2 * STAGE;
-  uint64_t* bar = reinterpret_cast<uint64_t*>(tw + S::TW_PAD);
-  __shared__ int ok_flag;
+  float2* stage = smem;
+  float2* tw = smem + NS * STAGE;
+  uint64_t* full = reinterpret_cast<uint64_t*>(tw + S::TW_PAD);
+  uint64_t* empty = full + NS;
   const int tid = threadIdx.x;
   for (int i = tid; i < S::TW; i += blockDim.x) tw[i] = a.tw[i];
   if (tid == 0) {
-    mbar_init(&bar[0], 1);
-    mbar_init(&bar[1], 1);
+    for (int s = 0; s < NS; ++s) {
+      mbar_init(&full[s], 1);
+      mbar_init(&empty[s], WARPS);
+    }
     fence_mbar_init();
   }
   __syncthreads();
   const int pchunks = (a.G + L - 1) / L;
   const int ntiles = a.Ny * pchunks;
+  const int mine = (int)blockIdx.x < ntiles ? (ntiles - 1 - (int)blockIdx.x) / (int)gridDim.x + 1 : 0;
 
-  auto issue = [&](int tile, int s) {
+  auto issue = [&](int k) {  // this CTA's k-th tile into stage k % NS
+    const int tile = blockIdx.x + k * gridDim.x;
     const int y = tile / pchunks, pc = tile - y * pchunks;
     const int p0 = pc * L;
     const int nl = min(L, a.G - p0);
-    float2* dst = stage + s * STAGE;
-    mbar_expect_tx(&bar[s], (uint32_t)((nl + 1) * NX * sizeof(float2)));
+    float2* dst = stage + (k % NS) * STAGE;
+    uint64_t* bar = &full[k % NS];
+    mbar_expect_tx(bar, (uint32_t)((nl + 1) * NX * sizeof(float2)));
     for (int i = 0; i < nl; ++i)
-      bulk_g2s(dst + i * NX, a.psi + ((size_t)(p0 + i) * a.Ny + y) * NX, NX * sizeof(float2), &bar[s]);
-    bulk_g2s(dst + L * NX, a.trans + (size_t)y * NX, NX * sizeof(float2), &bar[s]);
+      bulk_g2s(dst + i * NX, a.psi + ((size_t)(p0 + i) * a.Ny + y) * NX, NX * sizeof(float2), bar);
+    bulk_g2s(dst + L * NX, a.trans + (size_t)y * NX, NX * sizeof(float2), bar);
   };
 
   const int warp = tid >> 5, lane = tid & 31;
   const int lw = lane / T, t = lane % T;
   const int slot = warp * S::LPW + lw;  // line slot within a tile
-  int it = 0;
-  int pending = -1;  // stage of a load issued but not yet waited for
-  if (tid == 0 && blockIdx.x < ntiles) { issue(blockIdx.x, 0); pending = 0; }
-  for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x, ++it) {
-    const int s = it & 1;
-    const int next = tile + gridDim.x;
-    if (tid == 0) {
-      if (next < ntiles) { issue(next, s ^ 1); pending = s ^ 1; }
-      ok_flag = mbar_wait_bounded(&bar[s], (it >> 1) & 1) ? 1 : 0;
-      if (pending == s) pending = -1;
-      if (!ok_flag) {
-        atomicOr(a.err, 1);
-        if (pending >= 0) mbar_wait_bounded(&bar[pending], ((it + 1) >> 1) & 1);
+  int issued = 0;                       // tiles handed to the copy engine (thread 0 only)
+  if (tid == 0)
+    for (; issued < NS - 1 && issued < mine; ++issued) issue(issued);
+  for (int k = 0; k < mine; ++k) {
+    const int s = k % NS;
+    int pok = 1;
+    if (warp == 0) {
+      if (lane == 0 && issued < mine) {
+        // the stage of tile `issued` last held tile issued - NS
+        if (issued >= NS) pok = mbar_wait_bounded(&empty[issued % NS], ((issued / NS) - 1) & 1) ? 1 : 0;
+        if (pok) issue(issued++);
       }
+      pok = __shfl_sync(0xffffffffu, pok, 0);
     }
-    __syncthreads();
-    if (!ok_flag) return;
+    const int ok = __all_sync(0xffffffffu, mbar_wait_bounded(&full[s], (k / NS) & 1) ? 1 : 0) && pok;
+    if (!ok) {
+      if (lane == 0) atomicOr(a.err, 1);
+      if (tid == 0)  // copies in flight must land before the CTA's shared memory is released
+        for (int j = k; j < issued; ++j) mbar_wait_bounded(&full[j % NS], (j / NS) & 1);
+      return;
+    }
+    const int tile = blockIdx.x + k * gridDim.x;
     const int y = tile / pchunks, pc = tile - y * pchunks;
     const int p0 = pc * L;
     const int nl = min(L, a.G - p0);
@@ -166,8 +198,9 @@ __global__ void __launch_bounds__(S::THREADS, S::MINB) row_pass_tma_kernel(TmaPa
 #pragma unroll
       for (int m = 0; m < E; ++m) out[t + T * m] = v[m];
     }
-    fence_proxy_async();  // this stage is refilled by the copy engine two tiles later
-    __syncthreads();
+    fence_proxy_async();  // this warp's exchanges precede the next bulk copy into the stage
+    __syncwarp();
+    if (lane == 0) mbar_arrive(&empty[s]);
   }
 }
 
