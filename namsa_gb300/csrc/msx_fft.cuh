@@ -223,6 +223,7 @@ template <int N, int T, class Rad> struct LineFFT;
 
 template <int N, int T, int... Rs>
 struct LineFFT<N, T, Radices<Rs...>> {
+  using Rad = Radices<Rs...>;
   static constexpr int E = N / T;
   static_assert(N % T == 0, "threads must divide the line");
   static constexpr int kStages = sizeof...(Rs);

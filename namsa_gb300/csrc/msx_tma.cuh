@@ -288,4 +288,131 @@ __global__ void __launch_bounds__(S::THREADS, S::MINB) col_mid_tma_kernel(const 
   }
 }
 
+// ----------------------------------------------------------------------------- column pass, warp-owned columns
+// For schedules with 16 threads per column and 16-column tiles, every warp owns
+// two whole columns (lane = 2 t + c_local), so the FFT exchanges need only warp
+// synchronisation and the loop has no CTA-wide barrier (stages cycle with the
+// same full/empty protocol as the row pass).  The tensor map loads each
+// 128-byte tile row with the 128-byte swizzle: the 16-byte chunk holding
+// columns (2j, 2j+1) of row r sits at chunk j ^ (r mod 8).  The exchanges
+// address element i of a column at row i ^ ((i >> SH) & 7), SH = log2 of the
+// first radix; with the swizzle this keeps the gathers, the first-stage
+// scatters and the natural-order loads at two wavefronts per warp access (the
+// minimum for 32 eight-byte lanes), checked index by index for every schedule
+// that qualifies.
+template <class S>
+struct ColWarp {
+  static constexpr bool OK = (S::T == 16 && S::C == 16 && S::THREADS == 256);
+  static constexpr int NY = S::N;
+  static constexpr int BOXR = ColTma<S>::BOXR, NBOX = ColTma<S>::NBOX;
+  static constexpr int STAGE = 16 * NY;  // float2 words
+  static constexpr size_t bytes(int stages) {
+    return 1024 + sizeof(float2) * ((size_t)stages * STAGE + S::TW_PAD + NY) + 2 * stages * sizeof(uint64_t);
+  }
+  static constexpr int fit(int stages) { return bytes(stages) > 232448 ? 0 : (int)(233472 / (bytes(stages) + 1024)); }
+  // three stages when that keeps the occupancy the registers allow, else two
+  static constexpr int STAGES = fit(3) >= (fit(2) < S::MINB ? fit(2) : S::MINB) ? 3 : 2;
+  static constexpr size_t smem() { return bytes(STAGES); }
+};
+
+template <int SH>
+struct SwizzledColumn {
+  float2* tile;  // 1024-byte aligned stage: 16 columns, 128 bytes per row
+  int c;
+  __device__ __forceinline__ float2& row(int r) const {
+    return tile[r * 16 + ((((c >> 1) ^ (r & 7)) << 1) | (c & 1))];
+  }
+  __device__ __forceinline__ float2& operator[](int i) const { return row(i ^ ((i >> SH) & 7)); }
+};
+
+template <class Rad> struct FirstRadixOf;
+template <int R0, int... Rs>
+struct FirstRadixOf<Radices<R0, Rs...>> { static constexpr int value = R0; };
+
+template <class S>
+__global__ void __launch_bounds__(S::THREADS, S::MINB) col_mid_warp_kernel(const __grid_constant__ CUtensorMap map,
+                                                                     TmaPassArgs a) {
+  constexpr int NY = S::N, T = S::T, E = S::E, C = S::C;
+  constexpr int BOXR = ColWarp<S>::BOXR, NBOX = ColWarp<S>::NBOX, STAGE = ColWarp<S>::STAGE;
+  constexpr int NS = ColWarp<S>::STAGES, WARPS = S::WARPS;
+  constexpr int SH = ilog2(FirstRadixOf<typename S::FFT::Rad>::value);
+  extern __shared__ __align__(1024) unsigned char smem_raw[];
+  float2* stage = reinterpret_cast<float2*>(smem_raw + ((1024 - (smem_u32(smem_raw) & 1023)) & 1023));
+  float2* tw = stage + NS * STAGE;
+  float2* py = tw + S::TW_PAD;
+  uint64_t* full = reinterpret_cast<uint64_t*>(py + NY);
+  uint64_t* empty = full + NS;
+  const int tid = threadIdx.x;
+  for (int i = tid; i < S::TW; i += blockDim.x) tw[i] = a.tw[i];
+  for (int i = tid; i < NY; i += blockDim.x) py[i] = a.pyx[i];
+  if (tid == 0) {
+    for (int s = 0; s < NS; ++s) {
+      mbar_init(&full[s], 1);
+      mbar_init(&empty[s], WARPS);
+    }
+    fence_mbar_init();
+  }
+  __syncthreads();
+  const int tiles_x = a.Nx / C;
+  const int ntiles = tiles_x * a.G;
+  const int mine = (int)blockIdx.x < ntiles ? (ntiles - 1 - (int)blockIdx.x) / (int)gridDim.x + 1 : 0;
+
+  auto issue = [&](int k) {
+    const int tile = blockIdx.x + k * gridDim.x;
+    const int p = tile % a.G, xt = tile / a.G;
+    float2* dst = stage + (k % NS) * STAGE;
+    uint64_t* bar = &full[k % NS];
+    mbar_expect_tx(bar, (uint32_t)(STAGE * sizeof(float2)));
+#pragma unroll
+    for (int b = 0; b < NBOX; ++b) tma2d_g2s(dst + b * BOXR * C, &map, xt * C, p * NY + b * BOXR, bar);
+  };
+
+  const int warp = tid >> 5, lane = tid & 31;
+  const int t = lane >> 1, c = 2 * warp + (lane & 1);
+  int issued = 0;
+  if (tid == 0)
+    for (; issued < NS - 1 && issued < mine; ++issued) issue(issued);
+  for (int k = 0; k < mine; ++k) {
+    const int s = k % NS;
+    const int tile = blockIdx.x + k * gridDim.x;
+    const int p = tile % a.G, xt = tile / a.G;
+    const int x = xt * C + c;
+    const float2 px = __ldg(a.pyx + NY + x);  // consumed after the forward transform
+    const int2 bd = __ldg(a.band + x);
+    int pok = 1;
+    if (warp == 0) {
+      if (lane == 0 && issued < mine) {
+        if (issued >= NS) pok = mbar_wait_bounded(&empty[issued % NS], ((issued / NS) - 1) & 1) ? 1 : 0;
+        if (pok) issue(issued++);
+      }
+      pok = __shfl_sync(0xffffffffu, pok, 0);
+    }
+    const int ok = __all_sync(0xffffffffu, mbar_wait_bounded(&full[s], (k / NS) & 1) ? 1 : 0) && pok;
+    if (!ok) {
+      if (lane == 0) atomicOr(a.err, 1);
+      if (tid == 0)
+        for (int j = k; j < issued; ++j) mbar_wait_bounded(&full[j % NS], (j / NS) & 1);
+      return;
+    }
+    SwizzledColumn<SH> buf{stage + s * STAGE, c};
+    float2 v[E];
+#pragma unroll
+    for (int m = 0; m < E; ++m) v[m] = buf.row(t + T * m);
+    S::FFT::template run<false, false>(v, buf, tw, t);
+#pragma unroll
+    for (int m = 0; m < E; ++m) {
+      const int ky = t + T * m;
+      const float2 f = (ky >= bd.x && ky <= bd.y) ? cmul(px, py[ky]) : make_float2(0.f, 0.f);
+      v[m] = cmul(v[m], f);
+    }
+    S::FFT::template run<true, false>(v, buf, tw, t);
+    float2* col = a.psi + (size_t)p * NY * a.Nx + x;
+#pragma unroll
+    for (int m = 0; m < E; ++m) col[(t + T * m) * a.Nx] = v[m];
+    fence_proxy_async();
+    __syncwarp();
+    if (lane == 0) mbar_arrive(&empty[s]);
+  }
+}
+
 }  // namespace msx

@@ -90,3 +90,48 @@ def test_supercell_loader_and_detector(tmp_path):
     np.testing.assert_allclose(arr2['x'], sc['x'], rtol=1e-6)
     det = M.annular_detector(np.array([64, 64]), np.array([0.1, 0.1]), 0.025, 0.05, 0.1)
     assert det.shape == (64, 64) and det.dtype == bool and 0 < det.sum() < 64 * 64
+
+
+def _col_wavefronts(words):
+    slots = {}
+    for w in set(words):
+        slots.setdefault(w % 16, set()).add(w)
+    return max(len(v) for v in slots.values())
+
+
+@pytest.mark.parametrize('n,rads', [(256, (16, 16)), (384, (8, 8, 6)), (512, (32, 16))])
+def test_warp_column_layout_is_bank_conflict_free(n, rads):
+    """Index-level check of the warp-owned column pass layout (csrc/msx_tma.cuh,
+    col_mid_warp_kernel): 16 threads per column, lane = 2 t + c_local, tile rows of
+    16 complex64 stored with the 128-byte swizzle (chunk j of row r at j ^ (r & 7)),
+    exchange slot of element i at row i ^ ((i >> log2(first radix)) & 7).  Every
+    warp access (natural-order load, Stockham scatters and gathers of each stage)
+    must take two 128-byte wavefronts, the minimum for 32 eight-byte lanes."""
+    T = 16
+    E = n // T
+    sh = int(np.log2(rads[0]))
+
+    def perm(i):
+        return i ^ ((i >> sh) & 7)
+
+    def addr(row, c):
+        return row * 16 + (((c >> 1) ^ (row & 7)) << 1) + (c & 1)
+
+    assert sorted(perm(i) for i in range(n)) == list(range(n))
+    for warp in range(8):
+        lanes = [(l >> 1, 2 * warp + (l & 1)) for l in range(32)]
+        for m in range(E):
+            assert _col_wavefronts([addr(t + T * m, c) for t, c in lanes]) == 2
+        ns = 1
+        for si, R in enumerate(rads):
+            if si < len(rads) - 1:
+                for q in range(E // R):
+                    for r in range(R):
+                        ws = []
+                        for t, c in lanes:
+                            j = t + T * q
+                            ws.append(addr(perm((j // ns) * ns * R + (j % ns) + r * ns), c))
+                        assert _col_wavefronts(ws) == 2
+                for m in range(E):
+                    assert _col_wavefronts([addr(perm(t + T * m), c) for t, c in lanes]) == 2
+            ns *= R
