@@ -291,28 +291,33 @@ __global__ void __launch_bounds__(S::THREADS, S::MINB) col_mid_tma_kernel(const 
 // ----------------------------------------------------------------------------- column pass, warp-owned columns
 // For schedules with 16 threads per column and 16-column tiles, every warp owns
 // two whole columns (lane = 2 t + c_local), so the FFT exchanges need only warp
-// synchronisation and the loop has no CTA-wide barrier (stages cycle with the
-// same full/empty protocol as the row pass).  The tensor map loads each
-// 128-byte tile row with the 128-byte swizzle: the 16-byte chunk holding
-// columns (2j, 2j+1) of row r sits at chunk j ^ (r mod 8).  The exchanges
-// address element i of a column at row i ^ ((i >> SH) & 7), SH = log2 of the
-// first radix; with the swizzle this keeps the gathers, the first-stage
-// scatters and the natural-order loads at two wavefronts per warp access (the
-// minimum for 32 eight-byte lanes), checked index by index for every schedule
-// that qualifies.
+// synchronisation.  The tensor map moves each 128-byte tile row with the
+// 128-byte swizzle: the 16-byte chunk holding columns (2j, 2j+1) of row r sits
+// at chunk j ^ (r mod 8).  The exchanges address element i of a column at row
+// i ^ ((i >> SH) & 7), SH = log2 of the first radix; with the swizzle this keeps
+// the natural-order loads, the Stockham scatters and the gathers at two
+// wavefronts per warp access (the minimum for 32 eight-byte lanes).
+//
+// Results go back into the stage in natural row order and leave by a tensor
+// store of the whole tile, so global writes stay full 128-byte rows.  Three
+// stages rotate: tile k-1 being stored, tile k being transformed, tile k+1
+// being loaded.  Thread 0 drives the copy engine: at the start of tile k it
+// waits until every warp has written tile k-1 (`done`, one arrival per warp),
+// stores it, waits until the store of tile k-2 has read its stage, and loads
+// tile k+1 into that stage.  The other warps only wait for their own tile's
+// `full` barrier.
 template <class S>
 struct ColWarp {
   static constexpr bool OK = (S::T == 16 && S::C == 16 && S::THREADS == 256);
   static constexpr int NY = S::N;
   static constexpr int BOXR = ColTma<S>::BOXR, NBOX = ColTma<S>::NBOX;
   static constexpr int STAGE = 16 * NY;  // float2 words
-  static constexpr size_t bytes(int stages) {
-    return 1024 + sizeof(float2) * ((size_t)stages * STAGE + S::TW_PAD + NY) + 2 * stages * sizeof(uint64_t);
+  static constexpr int STAGES = 3;
+  static constexpr size_t smem() {
+    return 1024 + sizeof(float2) * ((size_t)STAGES * STAGE + S::TW_PAD + NY) + 2 * STAGES * sizeof(uint64_t);
   }
-  static constexpr int fit(int stages) { return bytes(stages) > 232448 ? 0 : (int)(233472 / (bytes(stages) + 1024)); }
-  // three stages when that keeps the occupancy the registers allow, else two
-  static constexpr int STAGES = fit(3) >= (fit(2) < S::MINB ? fit(2) : S::MINB) ? 3 : 2;
-  static constexpr size_t smem() { return bytes(STAGES); }
+  // CTAs per SM to compile for: the schedule's, unless shared memory holds only one
+  static constexpr int MINB = 2 * (smem() + 1024) <= 233472 ? S::MINB : 1;
 };
 
 template <int SH>
@@ -329,9 +334,21 @@ template <class Rad> struct FirstRadixOf;
 template <int R0, int... Rs>
 struct FirstRadixOf<Radices<R0, Rs...>> { static constexpr int value = R0; };
 
+__device__ __forceinline__ void tma2d_s2g(const CUtensorMap* map, int x, int y, const void* src) {
+  asm volatile("cp.async.bulk.tensor.2d.global.shared::cta.bulk_group [%0, {%1, %2}], [%3];" ::"l"(
+                   reinterpret_cast<uint64_t>(map)),
+               "r"(x), "r"(y), "r"(smem_u32(src))
+               : "memory");
+}
+__device__ __forceinline__ void bulk_commit() { asm volatile("cp.async.bulk.commit_group;" ::: "memory"); }
+// wait until at most N of this thread's committed bulk stores still read shared memory
+template <int N>
+__device__ __forceinline__ void bulk_wait_read() { asm volatile("cp.async.bulk.wait_group.read %0;" ::"n"(N) : "memory"); }
+__device__ __forceinline__ void bulk_wait_all() { asm volatile("cp.async.bulk.wait_group 0;" ::: "memory"); }
+
 template <class S>
-__global__ void __launch_bounds__(S::THREADS, S::MINB) col_mid_warp_kernel(const __grid_constant__ CUtensorMap map,
-                                                                     TmaPassArgs a) {
+__global__ void __launch_bounds__(S::THREADS, ColWarp<S>::MINB) col_mid_warp_kernel(const __grid_constant__ CUtensorMap map,
+                                                                          TmaPassArgs a) {
   constexpr int NY = S::N, T = S::T, E = S::E, C = S::C;
   constexpr int BOXR = ColWarp<S>::BOXR, NBOX = ColWarp<S>::NBOX, STAGE = ColWarp<S>::STAGE;
   constexpr int NS = ColWarp<S>::STAGES, WARPS = S::WARPS;
@@ -341,14 +358,14 @@ __global__ void __launch_bounds__(S::THREADS, S::MINB) col_mid_warp_kernel(const
   float2* tw = stage + NS * STAGE;
   float2* py = tw + S::TW_PAD;
   uint64_t* full = reinterpret_cast<uint64_t*>(py + NY);
-  uint64_t* empty = full + NS;
+  uint64_t* done = full + NS;
   const int tid = threadIdx.x;
   for (int i = tid; i < S::TW; i += blockDim.x) tw[i] = a.tw[i];
   for (int i = tid; i < NY; i += blockDim.x) py[i] = a.pyx[i];
   if (tid == 0) {
     for (int s = 0; s < NS; ++s) {
       mbar_init(&full[s], 1);
-      mbar_init(&empty[s], WARPS);
+      mbar_init(&done[s], WARPS);
     }
     fence_mbar_init();
   }
@@ -357,41 +374,61 @@ __global__ void __launch_bounds__(S::THREADS, S::MINB) col_mid_warp_kernel(const
   const int ntiles = tiles_x * a.G;
   const int mine = (int)blockIdx.x < ntiles ? (ntiles - 1 - (int)blockIdx.x) / (int)gridDim.x + 1 : 0;
 
-  auto issue = [&](int k) {
+  auto coords = [&](int k, int& x0, int& y0) {
     const int tile = blockIdx.x + k * gridDim.x;
-    const int p = tile % a.G, xt = tile / a.G;
+    x0 = (tile / a.G) * C;
+    y0 = (tile % a.G) * NY;
+  };
+  auto load = [&](int k) {
+    int x0, y0;
+    coords(k, x0, y0);
     float2* dst = stage + (k % NS) * STAGE;
     uint64_t* bar = &full[k % NS];
     mbar_expect_tx(bar, (uint32_t)(STAGE * sizeof(float2)));
 #pragma unroll
-    for (int b = 0; b < NBOX; ++b) tma2d_g2s(dst + b * BOXR * C, &map, xt * C, p * NY + b * BOXR, bar);
+    for (int b = 0; b < NBOX; ++b) tma2d_g2s(dst + b * BOXR * C, &map, x0, y0 + b * BOXR, bar);
+  };
+  auto store = [&](int k) {
+    int x0, y0;
+    coords(k, x0, y0);
+    const float2* src = stage + (k % NS) * STAGE;
+#pragma unroll
+    for (int b = 0; b < NBOX; ++b) tma2d_s2g(&map, x0, y0 + b * BOXR, src + b * BOXR * C);
+    bulk_commit();
   };
 
   const int warp = tid >> 5, lane = tid & 31;
   const int t = lane >> 1, c = 2 * warp + (lane & 1);
-  int issued = 0;
-  if (tid == 0)
-    for (; issued < NS - 1 && issued < mine; ++issued) issue(issued);
+  int loaded = 0;  // tiles handed to the copy engine for loading (thread 0 only)
+  if (tid == 0 && mine > 0) load(loaded++);
   for (int k = 0; k < mine; ++k) {
     const int s = k % NS;
-    const int tile = blockIdx.x + k * gridDim.x;
-    const int p = tile % a.G, xt = tile / a.G;
-    const int x = xt * C + c;
+    int x0, y0;
+    coords(k, x0, y0);
+    const int x = x0 + c;
     const float2 px = __ldg(a.pyx + NY + x);  // consumed after the forward transform
     const int2 bd = __ldg(a.band + x);
     int pok = 1;
     if (warp == 0) {
-      if (lane == 0 && issued < mine) {
-        if (issued >= NS) pok = mbar_wait_bounded(&empty[issued % NS], ((issued / NS) - 1) & 1) ? 1 : 0;
-        if (pok) issue(issued++);
+      if (lane == 0) {
+        if (k >= 1) {
+          pok = mbar_wait_bounded(&done[(k - 1) % NS], ((k - 1) / NS) & 1) ? 1 : 0;
+          if (pok) store(k - 1);
+        }
+        if (pok && loaded < mine) {
+          bulk_wait_read<1>();  // the store of tile k-2 has left the stage that tile k+1 reuses
+          load(loaded++);
+        }
       }
       pok = __shfl_sync(0xffffffffu, pok, 0);
     }
     const int ok = __all_sync(0xffffffffu, mbar_wait_bounded(&full[s], (k / NS) & 1) ? 1 : 0) && pok;
     if (!ok) {
       if (lane == 0) atomicOr(a.err, 1);
-      if (tid == 0)
-        for (int j = k; j < issued; ++j) mbar_wait_bounded(&full[j % NS], (j / NS) & 1);
+      if (tid == 0) {  // copies in flight must finish before the CTA's shared memory is released
+        for (int j = k; j < loaded; ++j) mbar_wait_bounded(&full[j % NS], (j / NS) & 1);
+        bulk_wait_all();
+      }
       return;
     }
     SwizzledColumn<SH> buf{stage + s * STAGE, c};
@@ -406,12 +443,19 @@ __global__ void __launch_bounds__(S::THREADS, S::MINB) col_mid_warp_kernel(const
       v[m] = cmul(v[m], f);
     }
     S::FFT::template run<true, false>(v, buf, tw, t);
-    float2* col = a.psi + (size_t)p * NY * a.Nx + x;
+    __syncwarp();  // every lane's last gather precedes the natural-order write-back
 #pragma unroll
-    for (int m = 0; m < E; ++m) col[(t + T * m) * a.Nx] = v[m];
-    fence_proxy_async();
+    for (int m = 0; m < E; ++m) buf.row(t + T * m) = v[m];
+    fence_proxy_async();  // the tensor store reads these writes
     __syncwarp();
-    if (lane == 0) mbar_arrive(&empty[s]);
+    if (lane == 0) mbar_arrive(&done[s]);
+  }
+  if (tid == 0 && mine > 0) {
+    if (mbar_wait_bounded(&done[(mine - 1) % NS], ((mine - 1) / NS) & 1))
+      store(mine - 1);
+    else
+      atomicOr(a.err, 1);
+    bulk_wait_all();
   }
 }
 
