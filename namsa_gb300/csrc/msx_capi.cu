@@ -161,9 +161,7 @@ int prepare_tma(msx_plan* p) {
   const cuuint32_t box[2] = {(cuuint32_t)p->col_ops->col_c, (cuuint32_t)p->col_ops->col_boxr};
   const cuuint32_t estr[2] = {1, 1};
   CUresult r = enc(&p->map, CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 2, p->psi, dims, strides, box, estr,
-                   CU_TENSOR_MAP_INTERLEAVE_NONE,
-                   p->col_ops->col_swizzle ? CU_TENSOR_MAP_SWIZZLE_128B : CU_TENSOR_MAP_SWIZZLE_NONE,
-                   CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                   CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
                    CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
   if (r != CUDA_SUCCESS) return fail(MSX_ERR_CUDA, "cuTensorMapEncodeTiled failed (%d)", (int)r);
   int sms = 0, rr = 0, cr = 0, dummy = 0;

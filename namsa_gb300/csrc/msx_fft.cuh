@@ -279,7 +279,10 @@ struct LineFFT<N, T, Radices<Rs...>> {
     for (int m = 0; m < E; ++m) v[m] = buf[t + T * m];
   }
 
-  template <bool INV, bool CTA, int Ns, int TwOff, class Buf, int R0, int... Rest>
+  // PRESYNC = false skips the synchronisation before this stage's scatter (the
+  // caller guarantees that nobody still reads the exchange buffer); later
+  // exchanges of the same transform always synchronise.
+  template <bool INV, bool CTA, int Ns, int TwOff, bool PRESYNC, class Buf, int R0, int... Rest>
   static __device__ __forceinline__ void stages(float2 (&v)[E], const Buf& buf, const float2* tw, int t) {
     float2 out[E];
     butterflies<R0, Ns, TwOff, INV>(v, out, tw, t);
@@ -287,20 +290,20 @@ struct LineFFT<N, T, Radices<Rs...>> {
 #pragma unroll
       for (int m = 0; m < E; ++m) v[m] = out[m];
     } else {
-      line_sync<CTA>();   // previous readers of buf are done
+      if constexpr (PRESYNC) line_sync<CTA>();   // previous readers of buf are done
       scatter<R0, Ns>(out, buf, t);
       line_sync<CTA>();
       gather(v, buf, t);
       constexpr int nextOff = (Ns > 1) ? TwOff + (R0 - 1) * Ns : TwOff;
-      stages<INV, CTA, Ns * R0, nextOff, Buf, Rest...>(v, buf, tw, t);
+      stages<INV, CTA, Ns * R0, nextOff, true, Buf, Rest...>(v, buf, tw, t);
     }
   }
 
   // In-place line transform of the E values held by thread t (unnormalised).
   // All T threads of the line must call it together.
-  template <bool INV, bool CTA, class Buf>
+  template <bool INV, bool CTA, class Buf, bool PRESYNC = true>
   static __device__ __forceinline__ void run(float2 (&v)[E], const Buf& buf, const float2* tw, int t) {
-    stages<INV, CTA, 1, 0, Buf, Rs...>(v, buf, tw, t);
+    stages<INV, CTA, 1, 0, PRESYNC, Buf, Rs...>(v, buf, tw, t);
   }
 
   // Host emulation of run() on a whole line (data[N] in natural order), used

@@ -16,7 +16,6 @@ struct SchedOps {
   int tw_words;
   int col_c;                  // columns per column-pass tile
   int col_boxr;               // rows per tensor-map box of the column tile
-  int col_swizzle;            // 1: the column tensor map uses the 128-byte swizzle (warp-owned columns)
   void (*host_twiddles)(float2*);
   cudaError_t (*configure)();
   cudaError_t (*row)(float2* psi, const float2* trans, const float2* tw, int G, int Ny, cudaStream_t st);
@@ -45,9 +44,6 @@ template <class S> struct SchedImpl {
     if (e == cudaSuccess) e = cudaFuncSetAttribute(row_pass_kernel<S, ROW_F>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)S::row_smem());
     if (e == cudaSuccess) e = cudaFuncSetAttribute(row_pass_tma_kernel<S>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)RowTma<S>::smem());
     if (e == cudaSuccess) e = cudaFuncSetAttribute(col_mid_tma_kernel<S>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ColTma<S>::smem());
-    if constexpr (ColWarp<S>::OK)
-      if (e == cudaSuccess)
-        e = cudaFuncSetAttribute(col_mid_warp_kernel<S>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ColWarp<S>::smem());
     return e;
   }
   static cudaError_t row(float2* psi, const float2* trans, const float2* tw, int G, int Ny, cudaStream_t st) {
@@ -78,23 +74,14 @@ template <class S> struct SchedImpl {
   static cudaError_t col_tma(const CUtensorMap& map, const TmaPassArgs& a, int ctas, cudaStream_t st) {
     const int ntiles = (a.Nx / S::C) * a.G;
     const int grid = ntiles < ctas ? ntiles : ctas;
-    if constexpr (ColWarp<S>::OK)
-      col_mid_warp_kernel<S><<<grid, S::THREADS, ColWarp<S>::smem(), st>>>(map, a);
-    else
-      col_mid_tma_kernel<S><<<grid, S::THREADS, ColTma<S>::smem(), st>>>(map, a);
+    col_mid_tma_kernel<S><<<grid, S::THREADS, ColTma<S>::smem(), st>>>(map, a);
     return cudaGetLastError();
   }
   static cudaError_t occupancy(int* row_per_sm, int* col_per_sm) {
     cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(row_per_sm, row_pass_tma_kernel<S>, S::THREADS,
                                                                   RowTma<S>::smem());
-    if (e == cudaSuccess) {
-      if constexpr (ColWarp<S>::OK)
-        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(col_per_sm, col_mid_warp_kernel<S>, S::THREADS,
-                                                          ColWarp<S>::smem());
-      else
-        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(col_per_sm, col_mid_tma_kernel<S>, S::THREADS,
-                                                          ColTma<S>::smem());
-    }
+    if (e == cudaSuccess)
+      e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(col_per_sm, col_mid_tma_kernel<S>, S::THREADS, ColTma<S>::smem());
     return e;
   }
   static cudaError_t row_mode(int rmode, float2* psi, const float2* trans, const float2* tw, int G, int Ny,
@@ -110,7 +97,7 @@ template <class S> struct SchedImpl {
     return cudaGetLastError();
   }
   static SchedOps ops(const char* name) {
-    return SchedOps{S::N, name, S::TW, S::C, ColTma<S>::BOXR, ColWarp<S>::OK ? 1 : 0, &host_twiddles, &configure, &row, &col,
+    return SchedOps{S::N, name, S::TW, S::C, ColTma<S>::BOXR, &host_twiddles, &configure, &row, &col,
                     &row_tma, &col_tma, &occupancy, &row_mode};
   }
 };

@@ -205,6 +205,23 @@ __global__ void __launch_bounds__(S::THREADS, S::MINB) row_pass_tma_kernel(TmaPa
 }
 
 // ----------------------------------------------------------------------------- column pass
+// A tile is C columns of one wave (tensor-map boxes of BOXR rows x C columns,
+// columns interleaved element by element).  The C columns' T threads each are
+// spread over the CTA (thread = c + C t keeps every shared-memory access on
+// consecutive columns), so exchanges use CTA barriers; the tile needs three:
+//   #0  every thread has waited for the tile's bytes (the outcome is combined
+//       with __syncthreads_and, so the CTA leaves together on a timeout) and
+//       has finished the previous tile;
+//   #1  after the forward transform's scatter into the exchange scratch;
+//   #2  after the inverse transform's scatter, which reuses the tile's own
+//       stage (its natural-order contents were read before #1).
+// No barrier precedes either scatter: #0 orders the scratch against the
+// previous tile's reads and #1 orders the stage against this tile's loads.
+// Where a third tile-sized buffer does not fit beside the two stages without
+// costing occupancy, both transforms exchange in the stage and each scatter is
+// preceded by a barrier (five per tile).
+// Thread 0 refills the previous tile's stage with tile k+1 right after #0
+// (that stage was last written by generic stores, fenced before #0).
 template <class S>
 struct ColTma {
   static constexpr int NY = S::N;
@@ -212,7 +229,14 @@ struct ColTma {
   static constexpr int BOXR = NY < 128 ? NY : 128;  // rows per tensor-map box
   static constexpr int NBOX = NY / BOXR;
   static constexpr int STAGE = C * NY;
-  static constexpr size_t smem() { return 16 + sizeof(float2) * ((size_t)2 * STAGE + S::TW_PAD + NY); }
+  static constexpr size_t bytes(int buffers) { return 16 + sizeof(float2) * ((size_t)buffers * STAGE + S::TW_PAD + NY); }
+  static constexpr int fit(int buffers) {
+    return bytes(buffers) > 232448 ? 0 : (int)(233472 / (bytes(buffers) + 1024));
+  }
+  // a separate exchange scratch when it fits without costing occupancy; otherwise
+  // both transforms exchange in the stage itself (two more barriers per tile)
+  static constexpr bool SCRATCH = fit(3) >= (fit(2) < S::MINB ? fit(2) : S::MINB);
+  static constexpr size_t smem() { return bytes(SCRATCH ? 3 : 2); }
 };
 
 template <class S>
@@ -221,152 +245,18 @@ __global__ void __launch_bounds__(S::THREADS, S::MINB) col_mid_tma_kernel(const 
   constexpr int NY = S::N, T = S::T, E = S::E, C = S::C;
   constexpr int BOXR = ColTma<S>::BOXR, NBOX = ColTma<S>::NBOX, STAGE = ColTma<S>::STAGE;
   extern __shared__ __align__(1024) float2 smem[];
+  constexpr bool SCR = ColTma<S>::SCRATCH;
   float2* stage = smem;
-  float2* tw = smem + 2 * STAGE;
-  float2* py = tw + S::TW_PAD;
-  uint64_t* bar = reinterpret_cast<uint64_t*>(py + NY);
-  __shared__ int ok_flag;
-  const int tid = threadIdx.x;
-  for (int i = tid; i < S::TW; i += blockDim.x) tw[i] = a.tw[i];
-  for (int i = tid; i < NY; i += blockDim.x) py[i] = a.pyx[i];
-  if (tid == 0) {
-    mbar_init(&bar[0], 1);
-    mbar_init(&bar[1], 1);
-    fence_mbar_init();
-  }
-  __syncthreads();
-  const int tiles_x = a.Nx / C;
-  const int ntiles = tiles_x * a.G;
-
-  auto issue = [&](int tile, int s) {
-    const int p = tile % a.G, xt = tile / a.G;
-    float2* dst = stage + s * STAGE;
-    mbar_expect_tx(&bar[s], (uint32_t)(STAGE * sizeof(float2)));
-#pragma unroll
-    for (int b = 0; b < NBOX; ++b) tma2d_g2s(dst + b * BOXR * C, &map, xt * C, p * NY + b * BOXR, &bar[s]);
-  };
-
-  const int c = tid % C, t = tid / C;
-  int it = 0;
-  int pending = -1;
-  if (tid == 0 && blockIdx.x < ntiles) { issue(blockIdx.x, 0); pending = 0; }
-  for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x, ++it) {
-    const int s = it & 1;
-    const int next = tile + gridDim.x;
-    if (tid == 0) {
-      if (next < ntiles) { issue(next, s ^ 1); pending = s ^ 1; }
-      ok_flag = mbar_wait_bounded(&bar[s], (it >> 1) & 1) ? 1 : 0;
-      if (pending == s) pending = -1;
-      if (!ok_flag) {
-        atomicOr(a.err, 1);
-        if (pending >= 0) mbar_wait_bounded(&bar[pending], ((it + 1) >> 1) & 1);
-      }
-    }
-    __syncthreads();
-    if (!ok_flag) return;
-    const int p = tile % a.G, xt = tile / a.G;
-    const int x = xt * C + c;
-    const float2 px = __ldg(a.pyx + NY + x);  // issued early: consumed after the forward transform
-    const int2 bd = __ldg(a.band + x);
-    InterleavedLine<C> buf{stage + s * STAGE + c};
-    float2 v[E];
-#pragma unroll
-    for (int m = 0; m < E; ++m) v[m] = buf[t + T * m];
-    S::FFT::template run<false, true>(v, buf, tw, t);
-#pragma unroll
-    for (int m = 0; m < E; ++m) {
-      const int ky = t + T * m;
-      const float2 f = (ky >= bd.x && ky <= bd.y) ? cmul(px, py[ky]) : make_float2(0.f, 0.f);
-      v[m] = cmul(v[m], f);
-    }
-    S::FFT::template run<true, true>(v, buf, tw, t);
-    float2* col = a.psi + (size_t)p * NY * a.Nx + x;
-#pragma unroll
-    for (int m = 0; m < E; ++m) col[(t + T * m) * a.Nx] = v[m];
-    fence_proxy_async();
-    __syncthreads();
-  }
-}
-
-// ----------------------------------------------------------------------------- column pass, warp-owned columns
-// For schedules with 16 threads per column and 16-column tiles, every warp owns
-// two whole columns (lane = 2 t + c_local), so the FFT exchanges need only warp
-// synchronisation.  The tensor map moves each 128-byte tile row with the
-// 128-byte swizzle: the 16-byte chunk holding columns (2j, 2j+1) of row r sits
-// at chunk j ^ (r mod 8).  The exchanges address element i of a column at row
-// i ^ ((i >> SH) & 7), SH = log2 of the first radix; with the swizzle this keeps
-// the natural-order loads, the Stockham scatters and the gathers at two
-// wavefronts per warp access (the minimum for 32 eight-byte lanes).
-//
-// Results go back into the stage in natural row order and leave by a tensor
-// store of the whole tile, so global writes stay full 128-byte rows.  Three
-// stages rotate: tile k-1 being stored, tile k being transformed, tile k+1
-// being loaded.  Thread 0 drives the copy engine: at the start of tile k it
-// waits until every warp has written tile k-1 (`done`, one arrival per warp),
-// stores it, waits until the store of tile k-2 has read its stage, and loads
-// tile k+1 into that stage.  The other warps only wait for their own tile's
-// `full` barrier.
-template <class S>
-struct ColWarp {
-  static constexpr bool OK = (S::T == 16 && S::C == 16 && S::THREADS == 256);
-  static constexpr int NY = S::N;
-  static constexpr int BOXR = ColTma<S>::BOXR, NBOX = ColTma<S>::NBOX;
-  static constexpr int STAGE = 16 * NY;  // float2 words
-  static constexpr int STAGES = 3;
-  static constexpr size_t smem() {
-    return 1024 + sizeof(float2) * ((size_t)STAGES * STAGE + S::TW_PAD + NY) + 2 * STAGES * sizeof(uint64_t);
-  }
-  // CTAs per SM to compile for: the schedule's, unless shared memory holds only one
-  static constexpr int MINB = 2 * (smem() + 1024) <= 233472 ? S::MINB : 1;
-};
-
-template <int SH>
-struct SwizzledColumn {
-  float2* tile;  // 1024-byte aligned stage: 16 columns, 128 bytes per row
-  int c;
-  __device__ __forceinline__ float2& row(int r) const {
-    return tile[r * 16 + ((((c >> 1) ^ (r & 7)) << 1) | (c & 1))];
-  }
-  __device__ __forceinline__ float2& operator[](int i) const { return row(i ^ ((i >> SH) & 7)); }
-};
-
-template <class Rad> struct FirstRadixOf;
-template <int R0, int... Rs>
-struct FirstRadixOf<Radices<R0, Rs...>> { static constexpr int value = R0; };
-
-__device__ __forceinline__ void tma2d_s2g(const CUtensorMap* map, int x, int y, const void* src) {
-  asm volatile("cp.async.bulk.tensor.2d.global.shared::cta.bulk_group [%0, {%1, %2}], [%3];" ::"l"(
-                   reinterpret_cast<uint64_t>(map)),
-               "r"(x), "r"(y), "r"(smem_u32(src))
-               : "memory");
-}
-__device__ __forceinline__ void bulk_commit() { asm volatile("cp.async.bulk.commit_group;" ::: "memory"); }
-// wait until at most N of this thread's committed bulk stores still read shared memory
-template <int N>
-__device__ __forceinline__ void bulk_wait_read() { asm volatile("cp.async.bulk.wait_group.read %0;" ::"n"(N) : "memory"); }
-__device__ __forceinline__ void bulk_wait_all() { asm volatile("cp.async.bulk.wait_group 0;" ::: "memory"); }
-
-template <class S>
-__global__ void __launch_bounds__(S::THREADS, ColWarp<S>::MINB) col_mid_warp_kernel(const __grid_constant__ CUtensorMap map,
-                                                                          TmaPassArgs a) {
-  constexpr int NY = S::N, T = S::T, E = S::E, C = S::C;
-  constexpr int BOXR = ColWarp<S>::BOXR, NBOX = ColWarp<S>::NBOX, STAGE = ColWarp<S>::STAGE;
-  constexpr int NS = ColWarp<S>::STAGES, WARPS = S::WARPS;
-  constexpr int SH = ilog2(FirstRadixOf<typename S::FFT::Rad>::value);
-  extern __shared__ __align__(1024) unsigned char smem_raw[];
-  float2* stage = reinterpret_cast<float2*>(smem_raw + ((1024 - (smem_u32(smem_raw) & 1023)) & 1023));
-  float2* tw = stage + NS * STAGE;
+  float2* scratch = smem + 2 * STAGE;  // used when SCR
+  float2* tw = stage + (SCR ? 3 : 2) * STAGE;
   float2* py = tw + S::TW_PAD;
   uint64_t* full = reinterpret_cast<uint64_t*>(py + NY);
-  uint64_t* done = full + NS;
   const int tid = threadIdx.x;
   for (int i = tid; i < S::TW; i += blockDim.x) tw[i] = a.tw[i];
   for (int i = tid; i < NY; i += blockDim.x) py[i] = a.pyx[i];
   if (tid == 0) {
-    for (int s = 0; s < NS; ++s) {
-      mbar_init(&full[s], 1);
-      mbar_init(&done[s], WARPS);
-    }
+    mbar_init(&full[0], 1);
+    mbar_init(&full[1], 1);
     fence_mbar_init();
   }
   __syncthreads();
@@ -374,88 +264,56 @@ __global__ void __launch_bounds__(S::THREADS, ColWarp<S>::MINB) col_mid_warp_ker
   const int ntiles = tiles_x * a.G;
   const int mine = (int)blockIdx.x < ntiles ? (ntiles - 1 - (int)blockIdx.x) / (int)gridDim.x + 1 : 0;
 
-  auto coords = [&](int k, int& x0, int& y0) {
+  auto load = [&](int k) {  // this CTA's k-th tile into stage k & 1
     const int tile = blockIdx.x + k * gridDim.x;
-    x0 = (tile / a.G) * C;
-    y0 = (tile % a.G) * NY;
-  };
-  auto load = [&](int k) {
-    int x0, y0;
-    coords(k, x0, y0);
-    float2* dst = stage + (k % NS) * STAGE;
-    uint64_t* bar = &full[k % NS];
+    const int p = tile % a.G, xt = tile / a.G;
+    float2* dst = stage + (k & 1) * STAGE;
+    uint64_t* bar = &full[k & 1];
     mbar_expect_tx(bar, (uint32_t)(STAGE * sizeof(float2)));
 #pragma unroll
-    for (int b = 0; b < NBOX; ++b) tma2d_g2s(dst + b * BOXR * C, &map, x0, y0 + b * BOXR, bar);
-  };
-  auto store = [&](int k) {
-    int x0, y0;
-    coords(k, x0, y0);
-    const float2* src = stage + (k % NS) * STAGE;
-#pragma unroll
-    for (int b = 0; b < NBOX; ++b) tma2d_s2g(&map, x0, y0 + b * BOXR, src + b * BOXR * C);
-    bulk_commit();
+    for (int b = 0; b < NBOX; ++b) tma2d_g2s(dst + b * BOXR * C, &map, xt * C, p * NY + b * BOXR, bar);
   };
 
-  const int warp = tid >> 5, lane = tid & 31;
-  const int t = lane >> 1, c = 2 * warp + (lane & 1);
-  int loaded = 0;  // tiles handed to the copy engine for loading (thread 0 only)
-  if (tid == 0 && mine > 0) load(loaded++);
+  const int c = tid % C, t = tid / C;
+  int loaded = 0;  // tiles handed to the copy engine (thread 0 only)
+  if (tid == 0)
+    for (; loaded < 2 && loaded < mine; ++loaded) load(loaded);
   for (int k = 0; k < mine; ++k) {
-    const int s = k % NS;
-    int x0, y0;
-    coords(k, x0, y0);
-    const int x = x0 + c;
+    const int s = k & 1;
+    const int tile = blockIdx.x + k * gridDim.x;
+    const int p = tile % a.G, xt = tile / a.G;
+    const int x = xt * C + c;
     const float2 px = __ldg(a.pyx + NY + x);  // consumed after the forward transform
     const int2 bd = __ldg(a.band + x);
-    int pok = 1;
-    if (warp == 0) {
-      if (lane == 0) {
-        if (k >= 1) {
-          pok = mbar_wait_bounded(&done[(k - 1) % NS], ((k - 1) / NS) & 1) ? 1 : 0;
-          if (pok) store(k - 1);
-        }
-        if (pok && loaded < mine) {
-          bulk_wait_read<1>();  // the store of tile k-2 has left the stage that tile k+1 reuses
-          load(loaded++);
-        }
-      }
-      pok = __shfl_sync(0xffffffffu, pok, 0);
-    }
-    const int ok = __all_sync(0xffffffffu, mbar_wait_bounded(&full[s], (k / NS) & 1) ? 1 : 0) && pok;
-    if (!ok) {
-      if (lane == 0) atomicOr(a.err, 1);
-      if (tid == 0) {  // copies in flight must finish before the CTA's shared memory is released
-        for (int j = k; j < loaded; ++j) mbar_wait_bounded(&full[j % NS], (j / NS) & 1);
-        bulk_wait_all();
+    const bool ok = mbar_wait_bounded(&full[s], (k >> 1) & 1);
+    if (!__syncthreads_and(ok)) {  // #0
+      if (tid == 0) {
+        atomicOr(a.err, 1);
+        for (int j = k; j < loaded; ++j) mbar_wait_bounded(&full[j & 1], (j >> 1) & 1);
       }
       return;
     }
-    SwizzledColumn<SH> buf{stage + s * STAGE, c};
+    if (tid == 0 && k >= 1 && loaded < mine) load(loaded++);  // tile k+1 into the stage of tile k-1
+    float2* st = stage + s * STAGE;
+    InterleavedLine<C> in{st + c};
     float2 v[E];
 #pragma unroll
-    for (int m = 0; m < E; ++m) v[m] = buf.row(t + T * m);
-    S::FFT::template run<false, false>(v, buf, tw, t);
+    for (int m = 0; m < E; ++m) v[m] = in[t + T * m];
+    if constexpr (SCR)
+      S::FFT::template run<false, true, InterleavedLine<C>, false>(v, InterleavedLine<C>{scratch + c}, tw, t);  // #1
+    else
+      S::FFT::template run<false, true, InterleavedLine<C>, true>(v, in, tw, t);
 #pragma unroll
     for (int m = 0; m < E; ++m) {
       const int ky = t + T * m;
       const float2 f = (ky >= bd.x && ky <= bd.y) ? cmul(px, py[ky]) : make_float2(0.f, 0.f);
       v[m] = cmul(v[m], f);
     }
-    S::FFT::template run<true, false>(v, buf, tw, t);
-    __syncwarp();  // every lane's last gather precedes the natural-order write-back
+    S::FFT::template run<true, true, InterleavedLine<C>, !SCR>(v, in, tw, t);  // #2
+    float2* col = a.psi + (size_t)p * NY * a.Nx + x;
 #pragma unroll
-    for (int m = 0; m < E; ++m) buf.row(t + T * m) = v[m];
-    fence_proxy_async();  // the tensor store reads these writes
-    __syncwarp();
-    if (lane == 0) mbar_arrive(&done[s]);
-  }
-  if (tid == 0 && mine > 0) {
-    if (mbar_wait_bounded(&done[(mine - 1) % NS], ((mine - 1) / NS) & 1))
-      store(mine - 1);
-    else
-      atomicOr(a.err, 1);
-    bulk_wait_all();
+    for (int m = 0; m < E; ++m) col[(t + T * m) * a.Nx] = v[m];
+    fence_proxy_async();  // the inverse exchange wrote the stage that the copy engine refills next
   }
 }
 
