@@ -546,7 +546,8 @@ def run_precision(args):
     a = 3.905
     rng = np.random.default_rng(0)
     out = {}
-    for n, cells, forms in [(512, 32, ('fp32_fft', 'bf16x3_tensor_core')), (1024, 64, ('fp32_fft',))]:
+    for n, cells, forms in [(512, 32, ('fp32_fft', 'bf16x3_tensor_core', 'bf16x3_tensor_core_compensated')),
+                            (1024, 64, ('fp32_fft',))]:
         sc = structures.srtio3((cells, cells, int(np.ceil(400 / a))))
         cr = CR.Crystal(sc, n, a / 2, kv=300, semi_angle=25e-3, ratio=1)
         pos = rng.uniform(0, a, size=(64, 2)).astype(np.float32)
@@ -566,11 +567,13 @@ def run_precision(args):
             if form == 'fp32_fft':
                 got = CR.fine_multislice(cr, pos)
             else:
+                engine.tc_set_compensation(form.endswith('compensated'))
                 w = cr.waves(pos)
                 for s in range(cr.trans_fine.shape[0]):
                     engine.step_waves_tc(w, cr.trans_fine[s], cr.ptab_fine)
                 got = cr.plan.cbed_waves(w, cr.sim.norm_dev)
                 engine.tc_check()
+                engine.tc_set_compensation(True)
             torch.cuda.synchronize()
             dt = time.perf_counter() - t1
             g = got.cpu().numpy()[sample]

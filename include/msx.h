@@ -290,16 +290,21 @@ MSX_API int msx_batch_check(msx_batch* batch);
  * Split-BF16 tensor-core DFT stages (precision study; no reference
  * counterpart).  A length-n DFT of complex lines as a 2n x 2n real GEMM on
  * tcgen05 with bfloat16 hi/lo operand splits (hi.hi + hi.lo + lo.hi, FP32
- * accumulation).  n = 256 or 512.
+ * accumulation) and, by default, a per-line norm compensation: each output
+ * line is rescaled so that |Z|^2 = n |X|^2 (Parseval), which removes the
+ * uniform loss of the accumulation.  n = 256 or 512.
  *  msx_tc_dft:        z (lines, n) = sum_m x[m] e^{sign 2 pi i m k / n}, lines % 128 == 0
  *  msx_step_waves_tc: the msx_plan_step_waves slice with all four 1-D DFTs on the
  *                     tensor cores (square n x n grids)
+ *  msx_tc_set_compensation: 1 (default) / 0 turns the norm compensation on / off
+ *                     for the calling host thread
  *  msx_tc_check:      synchronises; MSX_ERR_TIMEOUT if a bounded wait gave up
  * Scratch is held per host thread and grows with the largest call.
  */
 MSX_API int msx_tc_dft(const float* x_dev, int lines, int n, int sign, float* z_dev, void* stream);
 MSX_API int msx_step_waves_tc(float* waves_dev, int num_waves, int n, const float* trans_dev, const float* ptab_dev,
                               void* stream);
+MSX_API int msx_tc_set_compensation(int enable);
 MSX_API int msx_tc_check(void);
 
 /*

@@ -62,6 +62,7 @@ SIGNATURES = [
     ('msx_batch_check', _c.c_int, [_vp]),
     ('msx_tc_dft', _c.c_int, [_vp, _c.c_int, _c.c_int, _c.c_int, _vp, _vp]),
     ('msx_step_waves_tc', _c.c_int, [_vp, _c.c_int, _c.c_int, _vp, _vp, _vp]),
+    ('msx_tc_set_compensation', _c.c_int, [_c.c_int]),
     ('msx_tc_check', _c.c_int, []),
     ('msx_corrector_create', _c.c_int, [_c.c_int, _c.c_int, _c.c_int, _c.c_int, _c.c_int, _c.POINTER(_vp)]),
     ('msx_corrector_destroy', _c.c_int, [_vp]),

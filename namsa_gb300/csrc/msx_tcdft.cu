@@ -67,7 +67,7 @@ __device__ __forceinline__ void mma_commit(uint64_t* bar) {
 __global__ void __launch_bounds__(128, 1)
 tc_gemm_kernel(const uint8_t* __restrict__ a_hi, const uint8_t* __restrict__ a_lo, const uint8_t* __restrict__ b_hi,
                const uint8_t* __restrict__ b_lo, int kblocks, int ntiles_n, int N, float* __restrict__ Z,
-               int* __restrict__ err) {
+               double* __restrict__ out_norm, int* __restrict__ err) {
   extern __shared__ __align__(1024) uint8_t smem_raw[];
   // the 128-byte swizzle is anchored to 1024-byte boundaries: align the stages explicitly
   uint8_t* smem = smem_raw + ((1024u - (smem_u32(smem_raw) & 1023u)) & 1023u);
@@ -139,6 +139,7 @@ tc_gemm_kernel(const uint8_t* __restrict__ a_hi, const uint8_t* __restrict__ a_l
   if (ok) {
     // lane quarter of this warp: TMEM lanes 32*warp .. 32*warp+31 = tile rows
     const int row = mt * BM + warp * 32 + lane;
+    float sq = 0.f;  // this row's sum of squares over the tile's columns
     for (int c0 = 0; c0 < BN; c0 += 32) {
       uint32_t r[32];
       const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0;
@@ -156,9 +157,12 @@ tc_gemm_kernel(const uint8_t* __restrict__ a_hi, const uint8_t* __restrict__ a_l
       for (int i = 0; i < 32; ++i) {
         const int j = nt * BN + c0 + i;  // output column: real parts then imaginary parts
         const int e = j < N ? j : j - N;
-        Z[((size_t)row * N + e) * 2 + (j < N ? 0 : 1)] = __uint_as_float(r[i]);
+        const float z = __uint_as_float(r[i]);
+        Z[((size_t)row * N + e) * 2 + (j < N ? 0 : 1)] = z;
+        sq = fmaf(z, z, sq);
       }
     }
+    if (out_norm) atomicAdd(out_norm + row, (double)sq);
   }
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   __syncthreads();
@@ -167,14 +171,23 @@ tc_gemm_kernel(const uint8_t* __restrict__ a_hi, const uint8_t* __restrict__ a_l
 
 // A tiles from complex lines: A[l][n] = X[l][n] * mult[l % lm][n] (mult optional),
 // real parts at k = n, imaginary parts at k = N + n, split into bf16 hi + lo.
+// With in_norm, also accumulates each line's sum |A|^2 (the warps of a line
+// reduce first; N is a multiple of 32, so a warp never straddles two lines).
 __global__ void tc_split_kernel(const float2* __restrict__ X, long long lines, int N, const float2* __restrict__ mult,
-                                int lm, __nv_bfloat16* __restrict__ a_hi, __nv_bfloat16* __restrict__ a_lo) {
+                                int lm, __nv_bfloat16* __restrict__ a_hi, __nv_bfloat16* __restrict__ a_lo,
+                                double* __restrict__ in_norm) {
   const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= lines * N) return;
+  if (i >= lines * N) return;  // whole warps leave together: lines * N is a multiple of 32
   const long long l = i / N;
   const int n = (int)(i % N);
   float2 v = X[i];
   if (mult) v = cmul(v, mult[(size_t)(l % lm) * N + n]);
+  if (in_norm) {
+    float q = fmaf(v.x, v.x, v.y * v.y);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) q += __shfl_xor_sync(0xffffffffu, q, o);
+    if ((threadIdx.x & 31) == 0) atomicAdd(in_norm + l, (double)q);
+  }
   const int kblocks = 2 * N / BK;
   const long long mt = l / BM;
   const int m = (int)(l % BM);
@@ -187,6 +200,23 @@ __global__ void tc_split_kernel(const float2* __restrict__ X, long long lines, i
     const size_t byte = ((size_t)mt * kblocks + kk / BK) * A_BYTES + sw128_offset(m, kk % BK);
     a_hi[byte / 2] = hi;
     a_lo[byte / 2] = lo;
+  }
+}
+
+// Norm compensation: a length-N DFT multiplies each line's norm by N exactly
+// (Parseval), so Z[l] *= sqrt(N * |A_l|^2 / |Z_l|^2) removes the uniform scale
+// error of the split-bf16 products and their FP32 accumulation, leaving the
+// random part of the rounding.
+__global__ void tc_rescale_kernel(float2* __restrict__ Z, long long lines, int N, const double* __restrict__ in_norm,
+                                  const double* __restrict__ out_norm) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= lines * N) return;
+  const long long l = i / N;
+  const double zo = out_norm[l];
+  if (zo > 0.0) {
+    const float f = (float)sqrt((double)N * in_norm[l] / zo);
+    float2 z = Z[i];
+    Z[i] = make_float2(z.x * f, z.y * f);
   }
 }
 
@@ -245,11 +275,13 @@ struct TcState {
   __nv_bfloat16 *fwd_hi = nullptr, *fwd_lo = nullptr, *inv_hi = nullptr, *inv_lo = nullptr;
   __nv_bfloat16 *a_hi = nullptr, *a_lo = nullptr;
   float2 *z0 = nullptr, *z1 = nullptr, *ptab_t = nullptr;
+  double *nin = nullptr, *nout = nullptr;  // per-line norms for the compensation
   int* err = nullptr;
   size_t lines_cap = 0;
   bool configured = false;
 };
 thread_local TcState g_tc;  // one per host thread; sized by the largest call
+thread_local bool g_tc_compensate = true;
 
 int tc_prepare(int N, size_t lines) {
   TcState& s = g_tc;
@@ -274,11 +306,13 @@ int tc_prepare(int N, size_t lines) {
     if (cudaMalloc(&s.err, sizeof(int)) || cudaMemset(s.err, 0, sizeof(int))) return tfail(MSX_ERR_ALLOC, "tc error word");
   }
   if (lines > s.lines_cap) {
-    for (void* p : {(void*)s.a_hi, (void*)s.a_lo, (void*)s.z0, (void*)s.z1, (void*)s.ptab_t})
+    for (void* p : {(void*)s.a_hi, (void*)s.a_lo, (void*)s.z0, (void*)s.z1, (void*)s.ptab_t, (void*)s.nin,
+                    (void*)s.nout})
       if (p) cudaFree(p);
     const size_t abytes = sizeof(__nv_bfloat16) * lines * 2 * N;
     if (cudaMalloc(&s.a_hi, abytes) || cudaMalloc(&s.a_lo, abytes) || cudaMalloc(&s.z0, sizeof(float2) * lines * N) ||
-        cudaMalloc(&s.z1, sizeof(float2) * lines * N) || cudaMalloc(&s.ptab_t, sizeof(float2) * (size_t)N * N))
+        cudaMalloc(&s.z1, sizeof(float2) * lines * N) || cudaMalloc(&s.ptab_t, sizeof(float2) * (size_t)N * N) ||
+        cudaMalloc(&s.nin, sizeof(double) * lines) || cudaMalloc(&s.nout, sizeof(double) * lines))
       return tfail(MSX_ERR_ALLOC, "tensor-core DFT scratch: allocation failed");
     s.lines_cap = lines;
   }
@@ -294,14 +328,22 @@ int tc_prepare(int N, size_t lines) {
 int tc_dft(const float2* X, size_t lines, int N, const float2* mult, int lm, int sign, float2* Z, cudaStream_t st) {
   TcState& s = g_tc;
   const long long n = (long long)lines * N;
-  tc_split_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(X, (long long)lines, N, mult, lm, s.a_hi, s.a_lo);
+  const bool comp = g_tc_compensate;
+  if (comp) {
+    cudaMemsetAsync(s.nin, 0, sizeof(double) * lines, st);
+    cudaMemsetAsync(s.nout, 0, sizeof(double) * lines, st);
+  }
+  tc_split_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(X, (long long)lines, N, mult, lm, s.a_hi, s.a_lo,
+                                                               comp ? s.nin : nullptr);
   const int kblocks = 2 * N / BK, ntn = 2 * N / BN;
   const unsigned grid = (unsigned)((lines / BM) * ntn);
   tc_gemm_kernel<<<grid, 128, SMEM_BYTES, st>>>(reinterpret_cast<const uint8_t*>(s.a_hi),
                                                  reinterpret_cast<const uint8_t*>(s.a_lo),
                                                  reinterpret_cast<const uint8_t*>(sign < 0 ? s.fwd_hi : s.inv_hi),
                                                  reinterpret_cast<const uint8_t*>(sign < 0 ? s.fwd_lo : s.inv_lo),
-                                                 kblocks, ntn, N, reinterpret_cast<float*>(Z), s.err);
+                                                 kblocks, ntn, N, reinterpret_cast<float*>(Z),
+                                                 comp ? s.nout : nullptr, s.err);
+  if (comp) tc_rescale_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(Z, (long long)lines, N, s.nin, s.nout);
   const cudaError_t e = cudaGetLastError();
   return e == cudaSuccess ? MSX_OK : tfail(MSX_ERR_CUDA, cudaGetErrorString(e));
 }
@@ -341,6 +383,11 @@ int msx_step_waves_tc(float* waves_dev, int num_waves, int n, const float* trans
   if ((rc = tc_dft(s.z0, lines, n, nullptr, 1, +1, w, st))) return rc;     // inverse DFT_x
   const cudaError_t e = cudaGetLastError();
   return e == cudaSuccess ? MSX_OK : tfail(MSX_ERR_CUDA, cudaGetErrorString(e));
+}
+
+int msx_tc_set_compensation(int enable) {
+  g_tc_compensate = enable != 0;
+  return MSX_OK;
 }
 
 int msx_tc_check(void) {

@@ -159,6 +159,11 @@ def step_waves_tc(waves, trans, ptab):
     return waves
 
 
+def tc_set_compensation(enable):
+    """Per-line norm compensation of the tensor-core DFTs (default on) for this host thread."""
+    _lib.check(lib().msx_tc_set_compensation(int(bool(enable))))
+
+
 def tc_check():
     _lib.check(lib().msx_tc_check())
 
