@@ -67,7 +67,7 @@ __device__ __forceinline__ void mma_commit(uint64_t* bar) {
 __global__ void __launch_bounds__(128, 1)
 tc_gemm_kernel(const uint8_t* __restrict__ a_hi, const uint8_t* __restrict__ a_lo, const uint8_t* __restrict__ b_hi,
                const uint8_t* __restrict__ b_lo, int kblocks, int ntiles_n, int N, float* __restrict__ Z,
-               double* __restrict__ out_norm, int* __restrict__ err) {
+               float* __restrict__ out_norm, int* __restrict__ err) {
   extern __shared__ __align__(1024) uint8_t smem_raw[];
   // the 128-byte swizzle is anchored to 1024-byte boundaries: align the stages explicitly
   uint8_t* smem = smem_raw + ((1024u - (smem_u32(smem_raw) & 1023u)) & 1023u);
@@ -162,7 +162,7 @@ tc_gemm_kernel(const uint8_t* __restrict__ a_hi, const uint8_t* __restrict__ a_l
         sq = fmaf(z, z, sq);
       }
     }
-    if (out_norm) atomicAdd(out_norm + row, (double)sq);
+    if (out_norm) out_norm[(size_t)row * ntiles_n + nt] = sq;  // one partial per (line, N tile)
   }
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   __syncthreads();
@@ -171,52 +171,61 @@ tc_gemm_kernel(const uint8_t* __restrict__ a_hi, const uint8_t* __restrict__ a_l
 
 // A tiles from complex lines: A[l][n] = X[l][n] * mult[l % lm][n] (mult optional),
 // real parts at k = n, imaginary parts at k = N + n, split into bf16 hi + lo.
-// With in_norm, also accumulates each line's sum |A|^2 (the warps of a line
-// reduce first; N is a multiple of 32, so a warp never straddles two lines).
-__global__ void tc_split_kernel(const float2* __restrict__ X, long long lines, int N, const float2* __restrict__ mult,
-                                int lm, __nv_bfloat16* __restrict__ a_hi, __nv_bfloat16* __restrict__ a_lo,
-                                double* __restrict__ in_norm) {
-  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= lines * N) return;  // whole warps leave together: lines * N is a multiple of 32
-  const long long l = i / N;
-  const int n = (int)(i % N);
-  float2 v = X[i];
-  if (mult) v = cmul(v, mult[(size_t)(l % lm) * N + n]);
-  if (in_norm) {
-    float q = fmaf(v.x, v.x, v.y * v.y);
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) q += __shfl_xor_sync(0xffffffffu, q, o);
-    if ((threadIdx.x & 31) == 0) atomicAdd(in_norm + l, (double)q);
-  }
+// One CTA per line; with in_norm it also stores the line's sum |A|^2.
+__global__ void __launch_bounds__(256) tc_split_kernel(const float2* __restrict__ X, int N,
+                                                       const float2* __restrict__ mult, int lm,
+                                                       __nv_bfloat16* __restrict__ a_hi, __nv_bfloat16* __restrict__ a_lo,
+                                                       float* __restrict__ in_norm) {
+  __shared__ float red[8];
+  const long long l = blockIdx.x;
   const int kblocks = 2 * N / BK;
   const long long mt = l / BM;
   const int m = (int)(l % BM);
+  float q = 0.f;
+  for (int n = threadIdx.x; n < N; n += blockDim.x) {
+    float2 v = X[l * N + n];
+    if (mult) v = cmul(v, mult[(size_t)(l % lm) * N + n]);
+    q = fmaf(v.x, v.x, fmaf(v.y, v.y, q));
 #pragma unroll
-  for (int part = 0; part < 2; ++part) {
-    const float x = part ? v.y : v.x;
-    const int kk = part ? N + n : n;
-    const __nv_bfloat16 hi = __float2bfloat16_rn(x);
-    const __nv_bfloat16 lo = __float2bfloat16_rn(x - __bfloat162float(hi));
-    const size_t byte = ((size_t)mt * kblocks + kk / BK) * A_BYTES + sw128_offset(m, kk % BK);
-    a_hi[byte / 2] = hi;
-    a_lo[byte / 2] = lo;
+    for (int part = 0; part < 2; ++part) {
+      const float x = part ? v.y : v.x;
+      const int kk = part ? N + n : n;
+      const __nv_bfloat16 hi = __float2bfloat16_rn(x);
+      const __nv_bfloat16 lo = __float2bfloat16_rn(x - __bfloat162float(hi));
+      const size_t byte = ((size_t)mt * kblocks + kk / BK) * A_BYTES + sw128_offset(m, kk % BK);
+      a_hi[byte / 2] = hi;
+      a_lo[byte / 2] = lo;
+    }
+  }
+  if (in_norm) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) q += __shfl_xor_sync(0xffffffffu, q, o);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = q;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      float t = 0.f;
+      for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += red[w];
+      in_norm[l] = t;
+    }
   }
 }
 
 // Norm compensation: a length-N DFT multiplies each line's norm by N exactly
 // (Parseval), so Z[l] *= sqrt(N * |A_l|^2 / |Z_l|^2) removes the uniform scale
-// error of the split-bf16 products and their FP32 accumulation, leaving the
-// random part of the rounding.
-__global__ void tc_rescale_kernel(float2* __restrict__ Z, long long lines, int N, const double* __restrict__ in_norm,
-                                  const double* __restrict__ out_norm) {
-  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= lines * N) return;
-  const long long l = i / N;
-  const double zo = out_norm[l];
-  if (zo > 0.0) {
-    const float f = (float)sqrt((double)N * in_norm[l] / zo);
-    float2 z = Z[i];
-    Z[i] = make_float2(z.x * f, z.y * f);
+// error of the split-bf16 products and their FP32 accumulation (the tensor
+// core's accumulation loses magnitude systematically), leaving the random part
+// of the rounding.  One CTA per line; |Z_l|^2 is the sum of the GEMM's
+// per-tile partials.
+__global__ void __launch_bounds__(256) tc_rescale_kernel(float2* __restrict__ Z, int N, const float* __restrict__ in_norm,
+                                                         const float* __restrict__ out_part, int parts) {
+  const long long l = blockIdx.x;
+  float zo = 0.f;
+  for (int j = 0; j < parts; ++j) zo += out_part[l * parts + j];
+  if (!(zo > 0.f)) return;
+  const float f = sqrtf((float)N * in_norm[l] / zo);
+  for (int n = threadIdx.x; n < N; n += blockDim.x) {
+    const float2 z = Z[l * N + n];
+    Z[l * N + n] = make_float2(z.x * f, z.y * f);
   }
 }
 
@@ -275,7 +284,7 @@ struct TcState {
   __nv_bfloat16 *fwd_hi = nullptr, *fwd_lo = nullptr, *inv_hi = nullptr, *inv_lo = nullptr;
   __nv_bfloat16 *a_hi = nullptr, *a_lo = nullptr;
   float2 *z0 = nullptr, *z1 = nullptr, *ptab_t = nullptr;
-  double *nin = nullptr, *nout = nullptr;  // per-line norms for the compensation
+  float *nin = nullptr, *nout = nullptr;  // per-line input norms and per-(line, N tile) output partials
   int* err = nullptr;
   size_t lines_cap = 0;
   bool configured = false;
@@ -312,7 +321,7 @@ int tc_prepare(int N, size_t lines) {
     const size_t abytes = sizeof(__nv_bfloat16) * lines * 2 * N;
     if (cudaMalloc(&s.a_hi, abytes) || cudaMalloc(&s.a_lo, abytes) || cudaMalloc(&s.z0, sizeof(float2) * lines * N) ||
         cudaMalloc(&s.z1, sizeof(float2) * lines * N) || cudaMalloc(&s.ptab_t, sizeof(float2) * (size_t)N * N) ||
-        cudaMalloc(&s.nin, sizeof(double) * lines) || cudaMalloc(&s.nout, sizeof(double) * lines))
+        cudaMalloc(&s.nin, sizeof(float) * lines) || cudaMalloc(&s.nout, sizeof(float) * lines * (2 * N / BN)))
       return tfail(MSX_ERR_ALLOC, "tensor-core DFT scratch: allocation failed");
     s.lines_cap = lines;
   }
@@ -327,14 +336,8 @@ int tc_prepare(int N, size_t lines) {
 // Z (lines x N complex) = DFT of sign `sign` of X (lines x N) (X * mult when mult != null)
 int tc_dft(const float2* X, size_t lines, int N, const float2* mult, int lm, int sign, float2* Z, cudaStream_t st) {
   TcState& s = g_tc;
-  const long long n = (long long)lines * N;
   const bool comp = g_tc_compensate;
-  if (comp) {
-    cudaMemsetAsync(s.nin, 0, sizeof(double) * lines, st);
-    cudaMemsetAsync(s.nout, 0, sizeof(double) * lines, st);
-  }
-  tc_split_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(X, (long long)lines, N, mult, lm, s.a_hi, s.a_lo,
-                                                               comp ? s.nin : nullptr);
+  tc_split_kernel<<<(unsigned)lines, 256, 0, st>>>(X, N, mult, lm, s.a_hi, s.a_lo, comp ? s.nin : nullptr);
   const int kblocks = 2 * N / BK, ntn = 2 * N / BN;
   const unsigned grid = (unsigned)((lines / BM) * ntn);
   tc_gemm_kernel<<<grid, 128, SMEM_BYTES, st>>>(reinterpret_cast<const uint8_t*>(s.a_hi),
@@ -343,7 +346,7 @@ int tc_dft(const float2* X, size_t lines, int N, const float2* mult, int lm, int
                                                  reinterpret_cast<const uint8_t*>(sign < 0 ? s.fwd_lo : s.inv_lo),
                                                  kblocks, ntn, N, reinterpret_cast<float*>(Z),
                                                  comp ? s.nout : nullptr, s.err);
-  if (comp) tc_rescale_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(Z, (long long)lines, N, s.nin, s.nout);
+  if (comp) tc_rescale_kernel<<<(unsigned)lines, 256, 0, st>>>(Z, N, s.nin, s.nout, ntn);
   const cudaError_t e = cudaGetLastError();
   return e == cudaSuccess ? MSX_OK : tfail(MSX_ERR_CUDA, cudaGetErrorString(e));
 }

@@ -64,3 +64,26 @@ def test_tc_multislice_cbed_vs_fp64():
     ref = O.multislice_gpu(cr.trans_fine.cpu().numpy().astype(np.complex128), psik, P, pos, norm, geom)
     err = O.rel_l2(got, ref)
     assert err.max() < 1e-3, err
+
+
+def test_tc_dft_norm_compensation_keeps_parseval():
+    """With the compensation (default) every output line has |Z|^2 = n |X|^2 to
+    float rounding; without it the tensor-core accumulation loses norm."""
+    rng = np.random.default_rng(7)
+    n, lines = 512, 256
+    x = (rng.standard_normal((lines, n)) + 1j * rng.standard_normal((lines, n))).astype(np.complex64)
+    xd = torch.from_numpy(x).to(DEV)
+    want = n * np.sum(np.abs(x.astype(np.complex128)) ** 2, axis=1)
+    try:
+        engine.tc_set_compensation(False)
+        z0 = engine.tc_dft(xd, -1).cpu().numpy().astype(np.complex128)
+    finally:
+        engine.tc_set_compensation(True)
+    z1 = engine.tc_dft(xd, -1).cpu().numpy().astype(np.complex128)
+    engine.tc_check()
+    r0 = np.sum(np.abs(z0) ** 2, axis=1) / want
+    r1 = np.sum(np.abs(z1) ** 2, axis=1) / want
+    assert np.abs(r1 - 1).max() < 2e-6, np.abs(r1 - 1).max()
+    assert np.abs(r0 - 1).mean() > np.abs(r1 - 1).mean()
+    ref = np.fft.fft(x.astype(np.complex128), axis=1)
+    assert np.linalg.norm(z1 - ref) / np.linalg.norm(ref) < 5e-5
