@@ -308,6 +308,16 @@ MSX_API int msx_tc_set_compensation(int enable);
 MSX_API int msx_tc_check(void);
 
 /*
+ * Self-test of the bounded in-kernel wait (no reference counterpart).  One CTA
+ * waits on an mbarrier with a limit of 2^limit_log2 cycles (10..31); with
+ * arrive = 0 nothing arrives, so the wait runs out and the call returns
+ * MSX_ERR_TIMEOUT, the status a pass reports through msx_plan_check when one
+ * of its copies never lands.  With arrive = 1 it returns MSX_OK.  Synchronises
+ * `stream`.
+ */
+MSX_API int msx_selftest_wait(int arrive, int limit_log2, void* stream);
+
+/*
  * Learned coarse-slice corrector (no counterpart in the reference): a
  * spectral-convolution network mapping the wave after one thick slice and
  * that slice's transmission t_c to the wave of the equivalent fine slices.

@@ -64,6 +64,7 @@ SIGNATURES = [
     ('msx_step_waves_tc', _c.c_int, [_vp, _c.c_int, _c.c_int, _vp, _vp, _vp]),
     ('msx_tc_set_compensation', _c.c_int, [_c.c_int]),
     ('msx_tc_check', _c.c_int, []),
+    ('msx_selftest_wait', _c.c_int, [_c.c_int, _c.c_int, _c.c_void_p]),
     ('msx_corrector_create', _c.c_int, [_c.c_int, _c.c_int, _c.c_int, _c.c_int, _c.c_int, _c.POINTER(_vp)]),
     ('msx_corrector_destroy', _c.c_int, [_vp]),
     ('msx_corrector_params', _c.c_int, [_vp, _c.POINTER(_vp), _c.POINTER(_vp), _c.POINTER(_c.c_size_t)]),

@@ -47,11 +47,12 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
       : "memory");
   return ok != 0;
 }
-// Bounded wait: gives up after ~2^31 cycles (about one second at GB300 clocks).
-__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity) {
+// Bounded wait: gives up after `limit` cycles (default 2^31, about one second at
+// GB300 clocks).
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity, long long limit = (1LL << 31)) {
   const long long t0 = clock64();
   while (!mbar_try_wait(bar, parity)) {
-    if (clock64() - t0 > (1LL << 31)) return false;
+    if (clock64() - t0 > limit) return false;
   }
   return true;
 }

@@ -168,6 +168,11 @@ def tc_check():
     _lib.check(lib().msx_tc_check())
 
 
+def selftest_wait(arrive, limit_log2=22):
+    """Run the bounded-wait self-test; raises MsxError (code TIMEOUT) when the wait ran out."""
+    _lib.check(lib().msx_selftest_wait(int(bool(arrive)), int(limit_log2), _stream()))
+
+
 class Plan:
     """A multislice plan: resident wave workspace, schedules and graph cache."""
 

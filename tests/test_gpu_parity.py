@@ -172,6 +172,24 @@ def test_errors_surface_as_exceptions():
                         np.float32(kmax), lam, st, np.float32(kmax / 3), crop=100)
 
 
+def test_bounded_wait_runs_out_and_the_context_stays_usable():
+    """A wait with nothing arriving runs out after its limit (2^22 cycles here) and
+    is reported as MSX_ERR_TIMEOUT; the same wait with an arrival succeeds, and
+    the context keeps running passes afterwards."""
+    with pytest.raises(_lib.MsxError) as e:
+        engine.selftest_wait(False, 22)
+    assert e.value.code == _lib.MSX_ERR_TIMEOUT
+    engine.selftest_wait(True, 22)
+    g, trans, psik, norm, pos, kmax, lam, st = random_case(64, 64, S=2, P=2, seed=9)
+    plan = engine.Plan(64, 64)
+    out = plan.multislice(torch.from_numpy(trans).to(DEV), torch.from_numpy(psik).to(DEV),
+                          torch.tensor([norm], dtype=torch.float64, device=DEV), torch.from_numpy(pos).to(DEV),
+                          np.float32(kmax), lam, st, np.float32(kmax / 3))
+    plan.check()
+    assert torch.isfinite(out).all() and out.sum().item() > 0
+    plan.close()
+
+
 # ----------------------------------------------------------------------------- full pipelines
 def test_config1_pipeline_vs_fp64():
     """Plain single-probe CBED, Si [001] 4x4x20 cells, 256^2, 80 slices, 100 keV,
