@@ -249,7 +249,8 @@ struct LineFFT<N, T, Radices<Rs...>> {
 #pragma unroll
       for (int r = 0; r < R; ++r) u[r] = v[q + r * Q];
       if constexpr (Ns > 1) {
-        const int k = (t + T * q) % Ns;
+        // when Ns divides T every butterfly of the thread uses the same twiddles
+        const int k = (T % Ns == 0) ? (t % Ns) : (t + T * q) % Ns;
 #pragma unroll
         for (int r = 1; r < R; ++r) {
           const float2 w = tw[TwOff + (r - 1) * Ns + k];
