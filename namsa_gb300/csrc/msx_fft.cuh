@@ -219,15 +219,10 @@ __device__ __forceinline__ void line_sync() {
 // r = 1..Ri-1, k = 0..Ns-1 (forward sign; the inverse uses the conjugate).
 template <int... Rs> struct Radices;
 
-// DERIVE = true: in every stage with a single butterfly per thread (Q = 1) the
-// thread's twiddles w_r = W^{k r}, r = 1..R-1, come from the table only for r a
-// power of two; the others are products w_r = w_{r - low(r)} * w_{low(r)}
-// (at most three products deep for R = 16), trading shared-memory loads for
-// FMA-pipe work.
-template <int N, int T, class Rad, bool DERIVE = false> struct LineFFT;
+template <int N, int T, class Rad> struct LineFFT;
 
-template <int N, int T, int... Rs, bool DERIVE>
-struct LineFFT<N, T, Radices<Rs...>, DERIVE> {
+template <int N, int T, int... Rs>
+struct LineFFT<N, T, Radices<Rs...>> {
   using Rad = Radices<Rs...>;
   static constexpr int E = N / T;
   static_assert(N % T == 0, "threads must divide the line");
@@ -256,21 +251,10 @@ struct LineFFT<N, T, Radices<Rs...>, DERIVE> {
       if constexpr (Ns > 1) {
         // when Ns divides T every butterfly of the thread uses the same twiddles
         const int k = (T % Ns == 0) ? (t % Ns) : (t + T * q) % Ns;
-        if constexpr (DERIVE && Q == 1 && R > 2) {
-          float2 w[R];
 #pragma unroll
-          for (int r = 1; r < R; r <<= 1) w[r] = tw[TwOff + (r - 1) * Ns + k];
-#pragma unroll
-          for (int r = 3; r < R; ++r)
-            if ((r & (r - 1)) != 0) w[r] = cmul(w[r - (r & -r)], w[r & -r]);
-#pragma unroll
-          for (int r = 1; r < R; ++r) u[r] = INV ? cmulc(u[r], w[r]) : cmul(u[r], w[r]);
-        } else {
-#pragma unroll
-          for (int r = 1; r < R; ++r) {
-            const float2 w = tw[TwOff + (r - 1) * Ns + k];
-            u[r] = INV ? cmulc(u[r], w) : cmul(u[r], w);
-          }
+        for (int r = 1; r < R; ++r) {
+          const float2 w = tw[TwOff + (r - 1) * Ns + k];
+          u[r] = INV ? cmulc(u[r], w) : cmul(u[r], w);
         }
       }
       Dft<R, INV>::run(u);

@@ -48,12 +48,6 @@ struct Sched {
   static_assert(T <= 32 && 32 % T == 0, "a row line must live inside one warp");
 };
 
-// The same schedule with derived twiddles (LineFFT DERIVE) in its one-butterfly stages.
-template <int N_, int T_, int COL_C_, int MINB_, int... Rs>
-struct SchedD : Sched<N_, T_, COL_C_, MINB_, Rs...> {
-  using FFT = LineFFT<N_, T_, Radices<Rs...>, true>;
-};
-
 template <int TW>
 __device__ __forceinline__ void load_twiddles(float2* dst, const float2* __restrict__ src) {
   for (int i = threadIdx.x; i < TW; i += blockDim.x) dst[i] = src[i];

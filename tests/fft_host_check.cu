@@ -46,7 +46,6 @@ int main() {
   w = fmax(w, check<LineFFT<512, 32, Radices<16, 16, 2>>, 512>());
   w = fmax(w, check<LineFFT<512, 32, Radices<8, 8, 8>>, 512>());
   w = fmax(w, check<LineFFT<512, 32, Radices<16, 2, 16>>, 512>());
-  w = fmax(w, check<LineFFT<512, 32, Radices<16, 2, 16>, true>, 512>());
   w = fmax(w, check<LineFFT<768, 32, Radices<8, 8, 12>>, 768>());
   w = fmax(w, check<LineFFT<1024, 32, Radices<32, 32>>, 1024>());
   w = fmax(w, check<LineFFT<1024, 32, Radices<16, 8, 8>>, 1024>());
