@@ -16,11 +16,11 @@
 // where [lo, hi] is the band of the float32 mask comparison in column kx.
 //
 // Waits: every mbarrier wait has a clock64 limit of about one second.  In the
-// column pass every thread waits and the outcome is combined by a CTA barrier,
-// so the whole CTA leaves together; in the row pass each warp waits for itself
-// and leaves on its own.  On a timeout the kernel sets bit 0 of *err, waits
-// (again bounded) for copies that may still be in flight into its shared
-// memory, and returns.
+// column pass thread 0 polls and publishes the outcome through shared memory
+// and a CTA barrier, so the whole CTA leaves together; in the row pass each
+// warp polls for itself and leaves on its own.  On a timeout the kernel sets
+// bit 0 of *err, thread 0 waits (again bounded) for the copies it issued that
+// have not landed, and the threads return.
 #pragma once
 #include <cuda.h>
 #include <cuda_runtime.h>
@@ -94,23 +94,20 @@ struct TmaPassArgs {
 
 // ----------------------------------------------------------------------------- row pass
 // A tile is ROW_LINES rows of one y (from consecutive waves) plus that y's
-// transmission row.  STAGES stages cycle through the CTA's tiles and all of
-// them are filled at the start.  There is no CTA-wide barrier in the loop:
-// every warp waits on the stage's `full` barrier itself, transforms its own
-// rows in place, and releases the stage on its `empty` barrier (one arrival per
-// warp) after a proxy fence (its in-place exchanges are generic-proxy writes
-// that the next bulk copy into the stage must follow).  The warp that releases
-// a stage last (a per-stage arrival counter tells it) waits on `empty` -- which
-// is complete by then and acquires the other warps' writes -- and refills the
-// stage with the tile STAGES ahead, so no warp waits for a producer.
+// transmission row.  STAGES stages cycle through the CTA's tiles; thread 0 is
+// the producer.  There is no CTA-wide barrier in the loop: every warp waits on
+// the stage's `full` barrier itself, transforms its own rows in place, and
+// releases the stage on its `empty` barrier (one arrival per warp) after a
+// proxy fence (its in-place exchanges are generic-proxy writes that the next
+// bulk copy into the stage must follow).  Thread 0 refills a stage only after
+// all warps released it, so warps may drift up to STAGES - 1 tiles apart.
 template <class S>
 struct RowTma {
   static constexpr int NX = S::N;
   static constexpr int L = S::ROW_LINES;
   static constexpr int STAGE = (L + 1) * NX;  // float2 words: L rows + the transmission row
   static constexpr size_t bytes(int stages) {
-    return sizeof(float2) * ((size_t)stages * STAGE + S::TW_PAD) + 2 * stages * sizeof(uint64_t) +
-           stages * sizeof(int);
+    return sizeof(float2) * ((size_t)stages * STAGE + S::TW_PAD) + 2 * stages * sizeof(uint64_t);
   }
   // CTAs per SM that the shared memory allows (228 KB per SM, 1 KB reserved per CTA)
   static constexpr int fit(int stages) { return (int)(233472 / (bytes(stages) + 1024)); }
@@ -132,10 +129,8 @@ __global__ void __launch_bounds__(S::THREADS, S::MINB) row_pass_tma_kernel(TmaPa
   float2* tw = smem + NS * STAGE;
   uint64_t* full = reinterpret_cast<uint64_t*>(tw + S::TW_PAD);
   uint64_t* empty = full + NS;
-  int* released = reinterpret_cast<int*>(empty + NS);  // per-stage count of warp releases
   const int tid = threadIdx.x;
   for (int i = tid; i < S::TW; i += blockDim.x) tw[i] = a.tw[i];
-  if (tid < NS) released[tid] = 0;
   if (tid == 0) {
     for (int s = 0; s < NS; ++s) {
       mbar_init(&full[s], 1);
@@ -164,16 +159,25 @@ __global__ void __launch_bounds__(S::THREADS, S::MINB) row_pass_tma_kernel(TmaPa
   const int warp = tid >> 5, lane = tid & 31;
   const int lw = lane / T, t = lane % T;
   const int slot = warp * S::LPW + lw;  // line slot within a tile
+  int issued = 0;                       // tiles handed to the copy engine (thread 0 only)
   if (tid == 0)
-    for (int j = 0; j < NS && j < mine; ++j) issue(j);
+    for (; issued < NS - 1 && issued < mine; ++issued) issue(issued);
   for (int k = 0; k < mine; ++k) {
     const int s = k % NS;
-    if (!__all_sync(0xffffffffu, mbar_wait_bounded(&full[s], (k / NS) & 1) ? 1 : 0)) {
-      if (lane == 0) {
-        atomicOr(a.err, 1);
-        // copies that may still be in flight must land before the CTA's shared memory is released
-        for (int j = k; j < mine && j < k + NS; ++j) mbar_wait_bounded(&full[j % NS], (j / NS) & 1);
+    int pok = 1;
+    if (warp == 0) {
+      if (lane == 0 && issued < mine) {
+        // the stage of tile `issued` last held tile issued - NS
+        if (issued >= NS) pok = mbar_wait_bounded(&empty[issued % NS], ((issued / NS) - 1) & 1) ? 1 : 0;
+        if (pok) issue(issued++);
       }
+      pok = __shfl_sync(0xffffffffu, pok, 0);
+    }
+    const int ok = __all_sync(0xffffffffu, mbar_wait_bounded(&full[s], (k / NS) & 1) ? 1 : 0) && pok;
+    if (!ok) {
+      if (lane == 0) atomicOr(a.err, 1);
+      if (tid == 0)  // copies in flight must land before the CTA's shared memory is released
+        for (int j = k; j < issued; ++j) mbar_wait_bounded(&full[j % NS], (j / NS) & 1);
       return;
     }
     const int tile = blockIdx.x + k * gridDim.x;
@@ -197,16 +201,7 @@ __global__ void __launch_bounds__(S::THREADS, S::MINB) row_pass_tma_kernel(TmaPa
     }
     fence_proxy_async();  // this warp's exchanges precede the next bulk copy into the stage
     __syncwarp();
-    if (lane == 0) {
-      mbar_arrive(&empty[s]);
-      if (atomicAdd(&released[s], 1) % WARPS == WARPS - 1 && k + NS < mine) {
-        // last warp out: every warp has arrived, so this wait completes at once
-        if (mbar_wait_bounded(&empty[s], (k / NS) & 1))
-          issue(k + NS);
-        else
-          atomicOr(a.err, 1);
-      }
-    }
+    if (lane == 0) mbar_arrive(&empty[s]);
   }
 }
 
