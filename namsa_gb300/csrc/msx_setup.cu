@@ -263,22 +263,32 @@ __global__ void pfac_kernel(int Ny, int Nx, float kmax, double lambda, double sl
     sincospif(2.0f * (float)f, &sn, &cs);
     const float inv_n = (float)(1.0 / ((double)Ny * (double)Nx));
     pyx[Ny + i] = make_float2(cs * inv_n, -sn * inv_n);
-    int lo = 1, hi = 0;
-    bool found = false;
-    for (int y = 0; y < Ny; ++y) {
-      if ((float)krad_exact(i, y, Nx, Ny, kmax) < k_band) {
-        if (!found) { lo = y; found = true; }
-        hi = y;
+  }
+  // band of column x: one warp per column, the lanes stride over the rows; the
+  // first and last passing rows are the minimum and maximum over the lanes
+  const int warp = i >> 5, lane = i & 31;
+  if (warp < Nx) {
+    int lo = Ny, hi = -1;
+    for (int y = lane; y < Ny; y += 32) {
+      if ((float)krad_exact(warp, y, Nx, Ny, kmax) < k_band) {
+        lo = min(lo, y);
+        hi = max(hi, y);
       }
     }
-    band[i] = make_int2(lo, hi);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      lo = min(lo, __shfl_xor_sync(0xffffffffu, lo, o));
+      hi = max(hi, __shfl_xor_sync(0xffffffffu, hi, o));
+    }
+    if (lane == 0) band[warp] = hi < 0 ? make_int2(1, 0) : make_int2(lo, hi);
   }
 }
 
 cudaError_t launch_pfac(int Ny, int Nx, float kmax, double lambda, double slice_t, float k_band, float2* pyx,
                         int2* band, cudaStream_t st) {
-  const int n = Ny > Nx ? Ny : Nx;
-  pfac_kernel<<<(n + 127) / 128, 128, 0, st>>>(Ny, Nx, kmax, lambda, slice_t, k_band, pyx, band);
+  // 32 threads per column for the bands; that also covers the Ny + Nx factors
+  const long long threads = 32LL * Nx > (long long)(Ny > Nx ? Ny : Nx) ? 32LL * Nx : (long long)(Ny > Nx ? Ny : Nx);
+  pfac_kernel<<<(unsigned)((threads + 127) / 128), 128, 0, st>>>(Ny, Nx, kmax, lambda, slice_t, k_band, pyx, band);
   return cudaGetLastError();
 }
 
