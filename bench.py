@@ -482,7 +482,7 @@ def run_uneven(args):
 def run_corrector(args):
     """Learned coarse-slice corrector: train on device-generated pairs (Si, SrTiO3,
     random crystals, 256^2, 200 keV, ~1000 A), then compare coarse+corrector with
-    plain fine-slice multislice (the judge) on held-out positions: CBED error and
+    plain fine-slice multislice (the error reference) on held-out positions: CBED error and
     probes/s of both."""
     import torch
     from namsa_gb300 import corrector as CR, engine
