@@ -5,11 +5,12 @@ for the potential kernel, the window shape, the padded site-list length and the
 slice count) into namsa/probe_kernels.cu and namsa/potential_kernels.cu, and
 pycuda's SourceModule compiles the result (namsa/cuda_kernels.py:8-57).  This
 script performs the same rendering, with the same template variables, for the
-two Si [001] workloads the parity tests use, and writes the rendered sources
-into ``oracle/_ref/`` (git-ignored, never part of the product):
+workloads the parity tests use, and writes the rendered sources into
+``oracle/_ref/`` (git-ignored, never part of the product):
 
   c1  Si 4x4x20 cells (face-inclusive), 256^2, 100 keV, t = a/4 (80 slices)
   c2  Si 8x8x50 cells (face-inclusive), 512^2, 200 keV, t = a/4 (199 slices)
+  c4  SrTiO3 12x12x16 cells, 256^2, 300 keV, t = a/2 (three species)
 
 plus ``oracle/_ref/workloads.json`` with the rendered parameters.  The sources
 are then compiled against the stand-in header ``oracle/pycuda-complex.hpp`` and
@@ -33,10 +34,17 @@ OUT = os.path.join(HERE, '_ref')
 REFERENCE = os.environ.get('NAMSA_REFERENCE', '/root/reference')
 
 A_SI = 5.431
+A_STO = 3.905
 WORKLOADS = {
-    'c1': dict(cells=(4, 4, 20), n=256, kv=100.0, semi=20e-3),
-    'c2': dict(cells=(8, 8, 50), n=512, kv=200.0, semi=30e-3),
+    'c1': dict(crystal='si', cells=(4, 4, 20), n=256, kv=100.0, semi=20e-3, slice_t=A_SI / 4),
+    'c2': dict(crystal='si', cells=(8, 8, 50), n=512, kv=200.0, semi=30e-3, slice_t=A_SI / 4),
+    'c4': dict(crystal='srtio3', cells=(12, 12, 16), n=256, kv=300.0, semi=25e-3, slice_t=A_STO / 2),
 }
+
+
+def supercell(crystal, cells):
+    from oracle import msa_oracle as O
+    return O.si_supercell(*cells) if crystal == 'si' else O.srtio3_supercell(*cells)
 
 
 def workload_params(tag):
@@ -45,17 +53,17 @@ def workload_params(tag):
     sys.path.insert(0, ROOT)
     from oracle import msa_oracle as O
     w = WORKLOADS[tag]
-    sc = O.si_supercell(*w['cells'])
+    sc = supercell(w['crystal'], w['cells'])
     xyz = np.column_stack([sc['x'], sc['y'], sc['z']]).astype(np.float32)
     geom = O.Geometry(xyz, sc['atomic_number'], w['kv'], w['semi'], [w['n'], w['n']])
     kirk = np.load(os.path.join(ROOT, 'namsa_gb300', 'data', 'kirkland_params.npy'))
     _, win = O.atom_windows(geom, kirk)
-    t = A_SI / 4
+    t = w['slice_t']
     sites = O.slice_sites_gpu(geom, t)
     max_sites = max(len(s) for s in sites)
     return dict(tag=tag, ny=w['n'], nx=w['n'], pot_y=int(win.shape[1]), pot_x=int(win.shape[2]),
                 num_slices=len(sites), sites_size=3 * max_sites, species=int(win.shape[0]),
-                cells=list(w['cells']), kv=w['kv'], semi=w['semi'], slice_t=t)
+                crystal=w['crystal'], cells=list(w['cells']), kv=w['kv'], semi=w['semi'], slice_t=t)
 
 
 def render(reference=REFERENCE, out=OUT):

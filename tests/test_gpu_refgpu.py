@@ -7,7 +7,8 @@ driven in MSAGPU's order (oracle/refgpu_harness.cu), on identical inputs.
   (probe_kernels.cu:196-206); at the edge its slope is 40 per 1/Angstrom, so float
   rounding of k moves it by up to ~1e-5.  The engine evaluates it in double.
 * CBED: relative L2 <= 1e-4 per pattern (FP32 engine vs FP32 reference path), for
-  the single-probe Si 256^2 case and 64 positions of the Si 512^2 1024-position scan
+  the single-probe Si 256^2 case, 64 positions of the Si 512^2 1024-position scan
+  and a three-species SrTiO3 256^2 case at 300 keV with defocus and Cs
 
 The harness libraries are built by oracle/build_ref.py from kernels rendered where
 the reference checkout exists; without them these tests skip with that reason.
@@ -25,6 +26,8 @@ PROBE_C1 = {'smooth_apert': True, 'apert_smooth': 50, 'spherical_phase': True,
             'aberration_dict': {'C1': 0., 'C3': 0., 'C5': 0.}, 'scherzer': False}
 PROBE_C2 = {'smooth_apert': True, 'apert_smooth': 50, 'spherical_phase': True,
             'aberration_dict': {'C1': 0., 'C3': 1e4, 'C5': 0.}, 'scherzer': False}
+PROBE_C4 = {'smooth_apert': False, 'apert_smooth': 50, 'spherical_phase': True,
+            'aberration_dict': {'C1': 50., 'C3': 1e4, 'C5': 1e6}, 'scherzer': False}
 
 
 def _ref(tag):
@@ -37,10 +40,11 @@ def _ref(tag):
 
 def _case(tag):
     from namsa_gb300 import msa as M
+    from oracle import render_ref_kernels as RR
     ref = _ref(tag)
     meta = ref.meta
     torch.cuda.set_device(0)
-    sc = O.si_supercell(*meta['cells'])
+    sc = RR.supercell(meta.get('crystal', 'si'), meta['cells'])
     n = meta['ny']
     sim = M.MSAGPU(meta['kv'], meta['semi'], sc, sampling=np.array([n, n]), debye_waller=False)
     sim.setup_device(0)
@@ -52,7 +56,7 @@ def _case(tag):
     return ref, sim, geom, win
 
 
-@pytest.mark.parametrize('tag', ['c1', 'c2'])
+@pytest.mark.parametrize('tag', ['c1', 'c2', 'c4'])
 def test_transmission_bit_identical_to_reference_kernel(tag):
     ref, sim, geom, win = _case(tag)
     t_ref = ref.build_potential(geom, ref.meta['slice_t'], win)
@@ -62,7 +66,7 @@ def test_transmission_bit_identical_to_reference_kernel(tag):
     sim.close()
 
 
-@pytest.mark.parametrize('tag,pd', [('c1', PROBE_C1), ('c2', PROBE_C2)])
+@pytest.mark.parametrize('tag,pd', [('c1', PROBE_C1), ('c2', PROBE_C2), ('c4', PROBE_C4)])
 def test_probe_matches_reference_kernels(tag, pd):
     ref, sim, geom, _ = _case(tag)
     sim.build_probe(pd)
@@ -107,3 +111,9 @@ def test_cbed_scan_si512_sampled_matches_reference_gpu_path():
     err, got, want = _cbed_parity('c2', PROBE_C2, pos)
     assert err.shape == (64,)
     assert err.max() <= 1e-4, (err.mean(), err.max())
+
+
+def test_cbed_srtio3_three_species_matches_reference_gpu_path():
+    pos = np.array([[0., 0.], [1.0, 1.9], [-2.2, 0.7]])
+    err, got, want = _cbed_parity('c4', PROBE_C4, pos)
+    assert err.max() <= 1e-4, err
