@@ -307,6 +307,36 @@ struct LineFFT<N, T, Radices<Rs...>> {
     stages<INV, CTA, 1, 0, PRESYNC, Buf, Rs...>(v, buf, tw, t);
   }
 
+  // Exchanges alternate between two buffers, b0 for the X0-th exchange of the
+  // sequence, b1 for the next, and so on, and no scatter is preceded by a
+  // synchronisation: a scatter into one buffer can only race with reads of the
+  // same buffer two exchanges earlier, and the synchronisation after the
+  // intervening scatter already separates them.  The caller orders the first
+  // scatter into each buffer against earlier readers.
+  static constexpr int kExchanges = kStages - 1;
+  template <bool INV, bool CTA, int Ns, int TwOff, int X, class Buf, int R0, int... Rest>
+  static __device__ __forceinline__ void stages_alt(float2 (&v)[E], const Buf& b0, const Buf& b1, const float2* tw,
+                                                    int t) {
+    float2 out[E];
+    butterflies<R0, Ns, TwOff, INV>(v, out, tw, t);
+    if constexpr (sizeof...(Rest) == 0) {
+#pragma unroll
+      for (int m = 0; m < E; ++m) v[m] = out[m];
+    } else {
+      const Buf& buf = (X & 1) ? b1 : b0;
+      scatter<R0, Ns>(out, buf, t);
+      line_sync<CTA>();
+      gather(v, buf, t);
+      constexpr int nextOff = (Ns > 1) ? TwOff + (R0 - 1) * Ns : TwOff;
+      stages_alt<INV, CTA, Ns * R0, nextOff, X + 1, Buf, Rest...>(v, b0, b1, tw, t);
+    }
+  }
+  template <bool INV, bool CTA, int X0, class Buf>
+  static __device__ __forceinline__ void run_alt(float2 (&v)[E], const Buf& b0, const Buf& b1, const float2* tw,
+                                                 int t) {
+    stages_alt<INV, CTA, 1, 0, X0, Buf, Rs...>(v, b0, b1, tw, t);
+  }
+
   // Host emulation of run() on a whole line (data[N] in natural order), used
   // by the host-side unit test of the index arithmetic and the codelets.
   template <bool INV, int Ns, int TwOff, int R0, int... Rest>

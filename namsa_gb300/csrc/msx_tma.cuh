@@ -209,18 +209,20 @@ __global__ void __launch_bounds__(S::THREADS, S::MINB) row_pass_tma_kernel(TmaPa
 // A tile is C columns of one wave (tensor-map boxes of BOXR rows x C columns,
 // columns interleaved element by element).  The C columns' T threads each are
 // spread over the CTA (thread = c + C t keeps every shared-memory access on
-// consecutive columns), so exchanges use CTA barriers; the tile needs three:
-//   #0  every thread has waited for the tile's bytes (the outcome is combined
-//       with __syncthreads_and, so the CTA leaves together on a timeout) and
-//       has finished the previous tile;
-//   #1  after the forward transform's scatter into the exchange scratch;
-//   #2  after the inverse transform's scatter, which reuses the tile's own
-//       stage (its natural-order contents were read before #1).
-// No barrier precedes either scatter: #0 orders the scratch against the
-// previous tile's reads and #1 orders the stage against this tile's loads.
+// consecutive columns), so exchanges use CTA barriers: #0, where every thread
+// has waited for the tile's bytes (the outcome is combined with
+// __syncthreads_and, so the CTA leaves together on a timeout) and has finished
+// the previous tile, and then one after each exchange's scatter.  The
+// exchanges alternate between a separate scratch and the tile's own stage
+// (scratch first; the inverse transform continues the alternation), so no
+// scatter needs a barrier before it: #0 orders the scratch against the previous
+// tile's reads, the first exchange's barrier orders the stage against this
+// tile's loads, and each later scatter is two exchanges after the last reads of
+// its buffer.  Two-stage transforms take three barriers per tile, three-stage
+// ones five.
 // Where a third tile-sized buffer does not fit beside the two stages without
 // costing occupancy, both transforms exchange in the stage and each scatter is
-// preceded by a barrier (five per tile).
+// preceded by a barrier as well.
 // Thread 0 refills the previous tile's stage with tile k+1 right after #0
 // (that stage was last written by generic stores, fenced before #0).
 template <class S>
@@ -300,8 +302,12 @@ __global__ void __launch_bounds__(S::THREADS, S::MINB) col_mid_tma_kernel(const 
     float2 v[E];
 #pragma unroll
     for (int m = 0; m < E; ++m) v[m] = in[t + T * m];
+    // with the scratch, the exchanges alternate scratch, stage, scratch, ... over
+    // the forward transform and continue the alternation into the inverse one
+    constexpr int NXCH = S::FFT::kExchanges;
+    const InterleavedLine<C> scr{scratch + c};
     if constexpr (SCR)
-      S::FFT::template run<false, true, InterleavedLine<C>, false>(v, InterleavedLine<C>{scratch + c}, tw, t);  // #1
+      S::FFT::template run_alt<false, true, 0>(v, scr, in, tw, t);  // #1 (and one per further exchange)
     else
       S::FFT::template run<false, true, InterleavedLine<C>, true>(v, in, tw, t);
 #pragma unroll
@@ -310,7 +316,10 @@ __global__ void __launch_bounds__(S::THREADS, S::MINB) col_mid_tma_kernel(const 
       const float2 f = (ky >= bd.x && ky <= bd.y) ? cmul(px, py[ky]) : make_float2(0.f, 0.f);
       v[m] = cmul(v[m], f);
     }
-    S::FFT::template run<true, true, InterleavedLine<C>, !SCR>(v, in, tw, t);  // #2
+    if constexpr (SCR)
+      S::FFT::template run_alt<true, true, NXCH % 2>(v, scr, in, tw, t);  // #2 ...
+    else
+      S::FFT::template run<true, true, InterleavedLine<C>, true>(v, in, tw, t);
     float2* col = a.psi + (size_t)p * NY * a.Nx + x;
 #pragma unroll
     for (int m = 0; m < E; ++m) col[(t + T * m) * a.Nx] = v[m];
