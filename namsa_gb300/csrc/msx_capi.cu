@@ -122,15 +122,21 @@ int upload_twiddles(const SchedOps& op, float2** dst) {
   return MSX_OK;
 }
 
+// Grows the wave workspace to `waves`.  The new buffer is allocated before the
+// old one is released, so on failure the plan keeps its previous workspace.
 int ensure_workspace(msx_plan* p, size_t waves) {
   if (waves <= p->psi_waves) return MSX_OK;
+  float2* fresh = nullptr;
+  cudaError_t e = cudaMalloc(&fresh, sizeof(float2) * waves * (size_t)p->ny * p->nx);
+  if (e != cudaSuccess) {
+    cudaGetLastError();  // clear the sticky-free allocation error
+    return fail(MSX_ERR_ALLOC, "workspace of %zu waves (%d x %d) failed: %s", waves, p->ny, p->nx,
+                cudaGetErrorString(e));
+  }
   if (p->psi) cudaFree(p->psi);
-  p->psi = nullptr;
-  p->psi_waves = 0;
-  cudaError_t e = cudaMalloc(&p->psi, sizeof(float2) * waves * (size_t)p->ny * p->nx);
-  if (e != cudaSuccess) return fail(MSX_ERR_ALLOC, "workspace of %zu waves (%d x %d) failed: %s", waves, p->ny, p->nx,
-                                    cudaGetErrorString(e));
+  p->psi = fresh;
   p->psi_waves = waves;
+  p->map_ok = false;  // the tensor map describes the old buffer until prepare_tma runs
   return MSX_OK;
 }
 
@@ -216,8 +222,15 @@ int slice_passes(msx_plan* p, const float2* trans_s, int gn, const ColArgs& c, b
   return MSX_OK;
 }
 
+// A plan can only run groups its workspace holds (an allocation that failed
+// leaves the previous workspace, or none).
+bool workspace_holds(const msx_plan* p, int waves) { return p->psi && waves >= 0 && (size_t)waves <= p->psi_waves; }
+
 int enqueue_multislice(msx_plan* p, const MsArgs& a, cudaStream_t st) {
   const int ny = p->ny, nx = p->nx;
+  const int gmax = a.num_probes < a.group ? a.num_probes : a.group;
+  if (!workspace_holds(p, gmax))
+    return fail(MSX_ERR_ALLOC, "the plan's workspace does not hold %d waves (an earlier allocation failed)", gmax);
   MSX_CUDA(launch_ptab(ny, nx, a.kmax, a.lambda, a.slice_t, a.k_band, p->ptab, st), "propagator table");
   if (p->use_tma && p->map_ok)
     MSX_CUDA(launch_pfac(ny, nx, a.kmax, a.lambda, a.slice_t, a.k_band, p->pyx, p->band, st), "propagator factors");
@@ -425,10 +438,19 @@ int msx_plan_set_schedule(msx_plan* p, int row_schedule, int col_schedule, int g
   p->col_sched = col_schedule;
   p->row_ops = &rops[row_schedule];
   p->col_ops = &cops[col_schedule];
+  const int old_group = p->group;
   if (group > 0) p->group = group;
   drop_graph(p);
   rc = ensure_workspace(p, (size_t)p->group);
-  if (rc != MSX_OK) return rc;
+  if (rc != MSX_OK) {
+    // keep the previous group (and its workspace); the new schedule still applies
+    const std::string msg = g_err;
+    p->group = old_group;
+    const int rc2 = (p->psi && (size_t)p->group <= p->psi_waves) ? prepare_tma(p) : MSX_OK;
+    if (rc2 != MSX_OK) return rc2;
+    g_err = msg;
+    return MSX_ERR_ALLOC;
+  }
   return prepare_tma(p);
 }
 
@@ -628,6 +650,8 @@ int msx_plan_profile(msx_plan* p, const float* trans_dev, int num_slices, const 
     return fail(MSX_ERR_INVALID, "profile needs slices, probes, inputs and iters > 0");
   const int ny = p->ny, nx = p->nx;
   const int gn = num_probes < p->group ? num_probes : p->group;
+  if (!workspace_holds(p, gn))
+    return fail(MSX_ERR_ALLOC, "the plan's workspace does not hold %d waves (an earlier allocation failed)", gn);
   const size_t wave = (size_t)ny * nx;
   cudaStream_t st = (cudaStream_t)stream;
   cudaEvent_t ev[4];

@@ -388,9 +388,14 @@ class MSAGPU:
         self._probes_host = value
 
     def check_simulation(self):
-        """Integrated intensity per pattern (msa.py:363-371)."""
+        """Integrated intensity per pattern (msa.py:363-371).  Patterns that are not
+        finite (NaN or Inf inputs) raise a RuntimeWarning naming how many."""
         prob = self.cbed.double().sum((1, 2)).cpu().numpy()
-        if prob.max() > 1.0 or prob.min() < 0.95:
+        bad = ~np.isfinite(prob)
+        if bad.any():
+            warn(f'{int(bad.sum())} of {prob.size} CBED patterns are not finite (NaN or Inf in the inputs)',
+                 RuntimeWarning)
+        elif prob.max() > 1.0 or prob.min() < 0.95:
             print('Significant deviation of the probability from unity is found.\n'
                   'Change the sampling and/or slice thickness!')
         return prob

@@ -190,6 +190,45 @@ def test_bounded_wait_runs_out_and_the_context_stays_usable():
     plan.close()
 
 
+def test_failed_workspace_allocation_keeps_the_plan_usable():
+    """Host-side allocation failure: a 65535-wave group of 1024^2 waves (512 GiB)
+    cannot be allocated.  set_schedule reports MSX_ERR_ALLOC and the plan keeps its
+    previous group and workspace, so it still computes correct CBEDs."""
+    g, trans, psik, norm, pos, kmax, lam, st = random_case(1024, 1024, S=1, P=2, seed=11)
+    plan = engine.Plan(1024, 1024, 4)
+    with pytest.raises(_lib.MsxError) as e:
+        plan.set_schedule(group=65535)
+    assert e.value.code == _lib.MSX_ERR_ALLOC
+    assert plan.schedule[2] == 4
+    got = plan.multislice(torch.from_numpy(trans).to(DEV), torch.from_numpy(psik).to(DEV),
+                          torch.tensor([norm], dtype=torch.float64, device=DEV), torch.from_numpy(pos).to(DEV),
+                          np.float32(kmax), lam, st, np.float32(kmax / 3)).cpu().numpy()
+    plan.check()
+    P, _ = O.propagator_gpu(g, st, 1 / 3)
+    ref = O.multislice_gpu(trans.astype(np.complex128), psik, P, pos, norm, g)
+    assert O.rel_l2(got, ref).max() < 2e-5
+    plan.close()
+
+
+def test_nan_inputs_are_flagged_by_check_simulation():
+    """A NaN in the probe propagates into every pattern; check_simulation reports it."""
+    sc = O.si_supercell(2, 2, 2)
+    sim = M.MSAGPU(200, 25e-3, sc, sampling=np.array([64, 64]), debye_waller=False)
+    sim.setup_device(0)
+    sim.calc_atomic_potentials()
+    sim.build_potential_slices(5.431 / 4)
+    sim.build_probe({'smooth_apert': True, 'apert_smooth': 50, 'spherical_phase': True,
+                     'aberration_dict': {'C1': 0., 'C3': 0., 'C5': 0.}, 'scherzer': False})
+    sim.psi_k_dev[3, 5] = float('nan')
+    sim.probe_positions = np.zeros((2, 2))
+    sim.num_probes = 2
+    sim.multislice()
+    with pytest.warns(RuntimeWarning, match='not finite'):
+        prob = sim.check_simulation()
+    assert not np.isfinite(prob).any()
+    sim.close()
+
+
 # ----------------------------------------------------------------------------- full pipelines
 def test_config1_pipeline_vs_fp64():
     """Plain single-probe CBED, Si [001] 4x4x20 cells, 256^2, 80 slices, 100 keV,
