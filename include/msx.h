@@ -176,6 +176,24 @@ MSX_API int msx_multislice(msx_plan* plan, const float* trans_dev, int num_slice
                    void* stream);
 
 /*
+ * msx_multislice with host buffers, as the reference's multislice takes the
+ * slices and probe from the host and returns the CBED stack there
+ * (namsa/msa.py:767-924): trans_host (num_slices, ny, nx) complex64,
+ * psi_k_host (ny, nx) complex64, the normalisation as a value, positions_host
+ * (num_probes, 2) float32 [y, x], cbed_host (num_probes, crop_y, crop_x) float32.
+ * The uploads run on the plan's copy stream in chunks of 8 slices while the
+ * first group already computes, and each group's patterns are downloaded while
+ * the next group computes.  Stream-ordered like msx_multislice: `stream` waits
+ * for the last download, so the host buffers must stay valid until then; they
+ * should be page-locked for the copies to overlap.  The plan holds the device
+ * copies of the inputs and of the CBED stack.
+ */
+MSX_API int msx_multislice_host(msx_plan* plan, const float* trans_host, int num_slices, const float* psi_k_host,
+                                double normalization, const float* positions_host, int num_probes, float kmax,
+                                double lambda, double slice_t, float k_band, float* cbed_host, int crop_y, int crop_x,
+                                void* stream);
+
+/*
  * Real-space wave stepping, for workflows that act on the wave between slices
  * (the learned coarse-slice corrector).  No single reference counterpart: the
  * steps are those of namsa/msa.py:959-990 exposed one at a time.  waves are

@@ -42,6 +42,8 @@ SIGNATURES = [
     ('msx_plan_check', _c.c_int, [_vp]),
     ('msx_multislice', _c.c_int, [_vp, _vp, _c.c_int, _vp, _vp, _vp, _c.c_int, _c.c_float, _c.c_double,
                                   _c.c_double, _c.c_float, _vp, _c.c_int, _c.c_int, _vp]),
+    ('msx_multislice_host', _c.c_int, [_vp, _vp, _c.c_int, _vp, _c.c_double, _vp, _c.c_int, _c.c_float,
+                                       _c.c_double, _c.c_double, _c.c_float, _vp, _c.c_int, _c.c_int, _vp]),
     ('msx_propagator_table', _c.c_int, [_c.c_int, _c.c_int, _c.c_float, _c.c_double, _c.c_double, _c.c_float, _vp,
                                         _vp]),
     ('msx_plan_probe_waves', _c.c_int, [_vp, _vp, _vp, _c.c_int, _c.c_float, _vp, _vp]),

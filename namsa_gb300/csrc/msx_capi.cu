@@ -107,6 +107,19 @@ struct msx_plan {
   float* partial = nullptr;      // detector partial sums
   size_t partial_words = 0;
   float2* inv_n = nullptr;       // constant (1/N, 0) table for CBEDs of real-space waves
+  // host-buffer calls (msx_multislice_host): a copy stream and device copies of
+  // the inputs and of the CBED stack, grown as needed
+  cudaStream_t copy = nullptr;
+  cudaEvent_t ev_copy = nullptr;
+  float2* io_trans = nullptr;
+  size_t io_trans_words = 0;
+  float2* io_psik = nullptr;
+  size_t io_psik_words = 0;
+  float* io_pos = nullptr;
+  size_t io_pos_words = 0;
+  double* io_norm = nullptr;
+  float* io_cbed = nullptr;
+  size_t io_cbed_words = 0;
 };
 
 namespace {
@@ -222,11 +235,39 @@ int slice_passes(msx_plan* p, const float2* trans_s, int gn, const ColArgs& c, b
   return MSX_OK;
 }
 
+// Copy pipeline of msx_multislice_host: the first group waits for each chunk of
+// uploaded slices only when it reaches it, and each group's CBED block goes
+// back to the host on the copy stream while the next group computes.
+struct HostPipe {
+  cudaStream_t copy;
+  int chunk;                              // slices per upload chunk
+  const std::vector<cudaEvent_t>* chunk_ev;  // recorded on the copy stream after each chunk
+  std::vector<cudaEvent_t>* group_ev;        // recorded on the work stream after each group
+  float* cbed_host;
+  size_t pattern_words;                   // crop_y * crop_x
+};
+
 // A plan can only run groups its workspace holds (an allocation that failed
 // leaves the previous workspace, or none).
 bool workspace_holds(const msx_plan* p, int waves) { return p->psi && waves >= 0 && (size_t)waves <= p->psi_waves; }
 
-int enqueue_multislice(msx_plan* p, const MsArgs& a, cudaStream_t st) {
+// Grows a plan-owned device buffer of `words` elements of T.
+template <class T>
+int grow(T** buf, size_t* have, size_t words, const char* what) {
+  if (words <= *have && *buf) return MSX_OK;
+  T* fresh = nullptr;
+  const cudaError_t e = cudaMalloc(&fresh, sizeof(T) * (words ? words : 1));
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return fail(MSX_ERR_ALLOC, "%s: allocation of %zu bytes failed", what, sizeof(T) * words);
+  }
+  if (*buf) cudaFree(*buf);
+  *buf = fresh;
+  *have = words;
+  return MSX_OK;
+}
+
+int enqueue_multislice(msx_plan* p, const MsArgs& a, cudaStream_t st, const HostPipe* hp = nullptr) {
   const int ny = p->ny, nx = p->nx;
   const int gmax = a.num_probes < a.group ? a.num_probes : a.group;
   if (!workspace_holds(p, gmax))
@@ -237,7 +278,18 @@ int enqueue_multislice(msx_plan* p, const MsArgs& a, cudaStream_t st) {
   const size_t wave = (size_t)ny * nx;
   const int y0 = ny / 2 - a.crop_y / 2, x0 = nx / 2 - a.crop_x / 2;
   const float2* trans = reinterpret_cast<const float2*>(a.trans);
-  for (int g0 = 0; g0 < a.num_probes; g0 += a.group) {
+  // group done: hand its CBED block to the copy stream (host-buffer calls)
+  auto hand_off = [&](int gi, int g0, int gn) -> int {
+    if (!hp) return MSX_OK;
+    cudaEvent_t ev = (*hp->group_ev)[gi];
+    MSX_CUDA(cudaEventRecord(ev, st), "cudaEventRecord");
+    MSX_CUDA(cudaStreamWaitEvent(hp->copy, ev, 0), "cudaStreamWaitEvent");
+    MSX_CUDA(cudaMemcpyAsync(hp->cbed_host + (size_t)g0 * hp->pattern_words, a.cbed + (size_t)g0 * hp->pattern_words,
+                             sizeof(float) * (size_t)gn * hp->pattern_words, cudaMemcpyDeviceToHost, hp->copy),
+             "CBED download");
+    return MSX_OK;
+  };
+  for (int g0 = 0, gi = 0; g0 < a.num_probes; g0 += a.group, ++gi) {
     const int gn = (a.num_probes - g0 < a.group) ? a.num_probes - g0 : a.group;
     ColArgs c{};
     c.psi = p->psi;
@@ -256,12 +308,16 @@ int enqueue_multislice(msx_plan* p, const MsArgs& a, cudaStream_t st) {
       c.x_begin = x0;
       c.ncols = a.crop_x;
       MSX_CUDA(p->col_ops->col(COL_INIT_FINAL, c, st), "probe-only pass");
+      const int rc = hand_off(gi, g0, gn);
+      if (rc != MSX_OK) return rc;
       continue;
     }
     c.x_begin = 0;
     c.ncols = nx;
     MSX_CUDA(p->col_ops->col(COL_INIT, c, st), "probe formation pass");
     for (int s = 0; s < a.num_slices; ++s) {
+      if (hp && gi == 0 && s % hp->chunk == 0)
+        MSX_CUDA(cudaStreamWaitEvent(st, (*hp->chunk_ev)[s / hp->chunk], 0), "cudaStreamWaitEvent");
       const int rc = slice_passes(p, trans + (size_t)s * wave, gn, c, s + 1 < a.num_slices, st);
       if (rc != MSX_OK) return rc;
       if (s + 1 == a.num_slices) {
@@ -277,6 +333,8 @@ int enqueue_multislice(msx_plan* p, const MsArgs& a, cudaStream_t st) {
           f.x_begin = x0;
           f.ncols = a.crop_x;
           MSX_CUDA(p->col_ops->col(COL_FINAL, f, st), "final column pass");
+          const int rc2 = hand_off(gi, g0, gn);
+          if (rc2 != MSX_OK) return rc2;
         }
       }
     }
@@ -409,6 +467,10 @@ int msx_plan_destroy(msx_plan* p) {
   if (p->inv_n) cudaFree(p->inv_n);
   if (p->tw_row) cudaFree(p->tw_row);
   if (p->tw_col) cudaFree(p->tw_col);
+  for (void* q : {(void*)p->io_trans, (void*)p->io_psik, (void*)p->io_pos, (void*)p->io_norm, (void*)p->io_cbed})
+    if (q) cudaFree(q);
+  if (p->ev_copy) cudaEventDestroy(p->ev_copy);
+  if (p->copy) cudaStreamDestroy(p->copy);
   if (p->ev_in) cudaEventDestroy(p->ev_in);
   if (p->ev_out) cudaEventDestroy(p->ev_out);
   if (p->work) cudaStreamDestroy(p->work);
@@ -640,6 +702,87 @@ int msx_plan_cbed_waves(msx_plan* p, float* waves_dev, int num_waves, const doub
   c.Nx = p->nx; c.x_begin = p->nx / 2 - crop_x / 2; c.ncols = crop_x; c.y0 = p->ny / 2 - crop_y / 2; c.crop_y = crop_y;
   MSX_CUDA(p->col_ops->col(COL_FINAL, c, st), "final column pass");
   return MSX_OK;
+}
+
+int msx_multislice_host(msx_plan* p, const float* trans_host, int num_slices, const float* psi_k_host,
+                        double normalization, const float* positions_host, int num_probes, float kmax, double lambda,
+                        double slice_t, float k_band, float* cbed_host, int crop_y, int crop_x, void* stream) {
+  if (!p) return fail(MSX_ERR_INVALID, "null plan");
+  if (num_probes < 0 || num_slices < 0) return fail(MSX_ERR_INVALID, "negative probe or slice count");
+  if (num_probes == 0) return MSX_OK;
+  if (crop_y <= 0 || crop_x <= 0 || crop_y > p->ny || crop_x > p->nx)
+    return fail(MSX_ERR_INVALID, "crop %d x %d outside the %d x %d grid", crop_y, crop_x, p->ny, p->nx);
+  if (!psi_k_host || !positions_host || !cbed_host || (num_slices > 0 && !trans_host))
+    return fail(MSX_ERR_INVALID, "null pointer");
+  if (!(normalization > 0) || !(kmax > 0) || !(lambda > 0) || !(slice_t >= 0) || !(k_band >= 0))
+    return fail(MSX_ERR_INVALID, "normalisation, kmax, lambda must be positive; slice thickness and k_band non-negative");
+  int dev = 0;
+  MSX_CUDA(cudaGetDevice(&dev), "cudaGetDevice");
+  if (dev != p->device) return fail(MSX_ERR_INVALID, "plan belongs to device %d, current device is %d", p->device, dev);
+  if (!p->copy) {
+    MSX_CUDA(cudaStreamCreateWithFlags(&p->copy, cudaStreamNonBlocking), "copy stream");
+    MSX_CUDA(cudaEventCreateWithFlags(&p->ev_copy, cudaEventDisableTiming), "cudaEventCreate");
+  }
+  const size_t wave = (size_t)p->ny * p->nx, pattern = (size_t)crop_y * crop_x;
+  int rc = grow(&p->io_trans, &p->io_trans_words, wave * num_slices, "transmission slices");
+  if (rc == MSX_OK) rc = grow(&p->io_psik, &p->io_psik_words, wave, "k-space probe");
+  if (rc == MSX_OK) rc = grow(&p->io_pos, &p->io_pos_words, 2 * (size_t)num_probes, "positions");
+  size_t one = p->io_norm ? 1 : 0;
+  if (rc == MSX_OK) rc = grow(&p->io_norm, &one, 1, "normalisation");
+  if (rc == MSX_OK) rc = grow(&p->io_cbed, &p->io_cbed_words, pattern * num_probes, "CBED stack");
+  if (rc != MSX_OK) return rc;
+
+  cudaStream_t caller = (cudaStream_t)stream, w = p->work, cp = p->copy;
+  // everything here follows the caller's earlier work and this plan's earlier calls
+  MSX_CUDA(cudaEventRecord(p->ev_in, caller), "cudaEventRecord");
+  MSX_CUDA(cudaStreamWaitEvent(w, p->ev_in, 0), "cudaStreamWaitEvent");
+  MSX_CUDA(cudaEventRecord(p->ev_out, w), "cudaEventRecord");
+  MSX_CUDA(cudaStreamWaitEvent(cp, p->ev_out, 0), "cudaStreamWaitEvent");
+
+  const int chunk = 8;
+  const int nchunks = (num_slices + chunk - 1) / chunk;
+  const int ngroups = (num_probes + p->group - 1) / p->group;
+  std::vector<cudaEvent_t> chunk_ev(nchunks + 1, nullptr), group_ev(ngroups, nullptr);
+  auto release = [&]() {  // events still pending are released when they complete
+    for (cudaEvent_t e : chunk_ev) if (e) cudaEventDestroy(e);
+    for (cudaEvent_t e : group_ev) if (e) cudaEventDestroy(e);
+  };
+  for (auto& e : chunk_ev)
+    if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) { release(); return fail(MSX_ERR_CUDA, "cudaEventCreate"); }
+  for (auto& e : group_ev)
+    if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) { release(); return fail(MSX_ERR_CUDA, "cudaEventCreate"); }
+  auto run = [&]() -> int {
+    MSX_CUDA(cudaMemcpyAsync(p->io_psik, psi_k_host, sizeof(float2) * wave, cudaMemcpyHostToDevice, cp), "probe upload");
+    MSX_CUDA(cudaMemcpyAsync(p->io_pos, positions_host, sizeof(float) * 2 * num_probes, cudaMemcpyHostToDevice, cp),
+             "position upload");
+    // by value through a launch argument: no host memory to keep alive, no staging
+    MSX_CUDA(launch_store_double(p->io_norm, normalization, cp), "normalisation");
+    MSX_CUDA(cudaEventRecord(chunk_ev[nchunks], cp), "cudaEventRecord");
+    for (int i = 0; i < nchunks; ++i) {
+      const int s0 = i * chunk, s1 = (s0 + chunk < num_slices) ? s0 + chunk : num_slices;
+      MSX_CUDA(cudaMemcpyAsync(p->io_trans + (size_t)s0 * wave, trans_host + 2 * (size_t)s0 * wave,
+                               sizeof(float2) * (size_t)(s1 - s0) * wave, cudaMemcpyHostToDevice, cp),
+               "slice upload");
+      MSX_CUDA(cudaEventRecord(chunk_ev[i], cp), "cudaEventRecord");
+    }
+    MSX_CUDA(cudaStreamWaitEvent(w, chunk_ev[nchunks], 0), "cudaStreamWaitEvent");
+    MsArgs a;
+    std::memset(&a, 0, sizeof(a));
+    a.trans = reinterpret_cast<const float*>(p->io_trans); a.num_slices = num_slices;
+    a.psik = reinterpret_cast<const float*>(p->io_psik); a.norm = p->io_norm; a.pos = p->io_pos;
+    a.num_probes = num_probes; a.kmax = kmax; a.lambda = lambda; a.slice_t = slice_t; a.k_band = k_band;
+    a.cbed = p->io_cbed; a.crop_y = crop_y; a.crop_x = crop_x;
+    a.group = p->group; a.row_sched = p->row_sched; a.col_sched = p->col_sched;
+    HostPipe hp{cp, chunk, &chunk_ev, &group_ev, cbed_host, pattern};
+    int r = enqueue_multislice(p, a, w, &hp);
+    if (r != MSX_OK) return r;
+    MSX_CUDA(cudaEventRecord(p->ev_copy, cp), "cudaEventRecord");
+    MSX_CUDA(cudaStreamWaitEvent(caller, p->ev_copy, 0), "cudaStreamWaitEvent");
+    return MSX_OK;
+  };
+  rc = run();
+  release();
+  return rc;
 }
 
 int msx_plan_profile(msx_plan* p, const float* trans_dev, int num_slices, const float* psi_k_dev,

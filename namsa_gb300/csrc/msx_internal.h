@@ -12,6 +12,8 @@ cudaError_t launch_potential(const int4* sites, const int* slice_off, int num_sl
                              int Ny, int Nx, float sigma, float2* trans, float* pot, cudaStream_t st);
 cudaError_t launch_probe(int Ny, int Nx, float kmax, double lambda, float k_semi, double C1, double C3, double C5,
                          int smooth, float2* psik, float* aperture, double* norm, cudaStream_t st);
+// *dst = value, as a one-thread kernel on st.
+cudaError_t launch_store_double(double* dst, double value, cudaStream_t st);
 // Sets the message returned by msx_last_error for the calling thread.
 void set_last_error(const char* msg);
 

@@ -284,6 +284,13 @@ __global__ void pfac_kernel(int Ny, int Nx, float kmax, double lambda, double sl
   }
 }
 
+__global__ void store_double_kernel(double* dst, double value) { *dst = value; }
+
+cudaError_t launch_store_double(double* dst, double value, cudaStream_t st) {
+  store_double_kernel<<<1, 1, 0, st>>>(dst, value);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_pfac(int Ny, int Nx, float kmax, double lambda, double slice_t, float k_band, float2* pyx,
                         int2* band, cudaStream_t st) {
   // 32 threads per column for the bands; that also covers the Ny + Nx factors

@@ -23,6 +23,18 @@ def _ptr(t):
     return _vp(0) if t is None else _vp(t.data_ptr())
 
 
+def _need_host(t, dtype, name, ndim=None):
+    if not isinstance(t, torch.Tensor) or t.is_cuda:
+        raise TypeError(f'{name} must be a host (CPU) torch tensor')
+    if t.dtype != dtype:
+        raise TypeError(f'{name} must be {dtype}, got {t.dtype}')
+    if not t.is_contiguous():
+        raise ValueError(f'{name} must be contiguous')
+    if ndim is not None and t.dim() != ndim:
+        raise ValueError(f'{name} must have {ndim} dimensions, got {tuple(t.shape)}')
+    return t
+
+
 def _need(t, dtype, name, ndim=None):
     if not isinstance(t, torch.Tensor):
         raise TypeError(f'{name} must be a torch tensor')
@@ -246,6 +258,30 @@ class Plan:
         _lib.check(lib().msx_multislice(self.handle, _ptr(trans), S, _ptr(psik), _ptr(norm), _ptr(positions), P,
                                         float(kmax), float(lam), float(slice_t), float(k_band), _ptr(out),
                                         int(cy), int(cx), _stream()))
+        return out
+
+    def multislice_host(self, trans, psik, norm, positions, kmax, lam, slice_t, k_band, crop=None, out=None):
+        """multislice() with host tensors in and out (page-locked for overlapped copies):
+        trans (S, ny, nx) and psik (ny, nx) complex64, norm a float, positions (P, 2)
+        float32; returns the (P, crop_y, crop_x) float32 host stack.  Enqueued on the
+        current stream; synchronise before reading the result."""
+        _need_host(trans, torch.complex64, 'trans', 3)
+        _need_host(psik, torch.complex64, 'psi_k', 2)
+        _need_host(positions, torch.float32, 'positions', 2)
+        S, ny, nx = trans.shape
+        if (ny, nx) != (self.ny, self.nx) or tuple(psik.shape) != (ny, nx):
+            raise ValueError(f'grid mismatch: plan {self.ny}x{self.nx}, trans {tuple(trans.shape)}, psi_k {tuple(psik.shape)}')
+        cy, cx = (ny, nx) if crop is None else ((crop, crop) if isinstance(crop, int) else crop)
+        P = positions.shape[0]
+        if out is None:
+            out = torch.empty((P, cy, cx), dtype=torch.float32, pin_memory=True)
+        else:
+            _need_host(out, torch.float32, 'out', 3)
+            if tuple(out.shape) != (P, cy, cx):
+                raise ValueError('out has the wrong shape')
+        _lib.check(lib().msx_multislice_host(self.handle, _ptr(trans), S, _ptr(psik), float(norm), _ptr(positions), P,
+                                             float(kmax), float(lam), float(slice_t), float(k_band), _ptr(out),
+                                             int(cy), int(cx), _stream()))
         return out
 
     def probe_waves(self, psik, positions, kmax):

@@ -190,6 +190,25 @@ def test_bounded_wait_runs_out_and_the_context_stays_usable():
     plan.close()
 
 
+@pytest.mark.parametrize('pinned', [True, False])
+def test_host_buffer_multislice_matches_device_call(pinned):
+    """msx_multislice_host (chunked uploads overlapping the first group, per-group
+    downloads) gives exactly the device call's CBEDs: 20 slices in 3 upload chunks,
+    7 positions in groups of 3, a central crop."""
+    g, trans, psik, norm, pos, kmax, lam, st = random_case(128, 128, S=20, P=7, seed=12)
+    plan = engine.Plan(128, 128, 3)
+    want = plan.multislice(torch.from_numpy(trans).to(DEV), torch.from_numpy(psik).to(DEV),
+                           torch.tensor([norm], dtype=torch.float64, device=DEV), torch.from_numpy(pos).to(DEV),
+                           np.float32(kmax), lam, st, np.float32(kmax / 3), crop=96).cpu().numpy()
+    host = (lambda a: torch.from_numpy(a).pin_memory()) if pinned else torch.from_numpy
+    got = plan.multislice_host(host(trans), host(psik), norm, host(pos), np.float32(kmax), lam, st,
+                               np.float32(kmax / 3), crop=96)
+    torch.cuda.synchronize()
+    plan.check()
+    np.testing.assert_array_equal(got.numpy(), want)
+    plan.close()
+
+
 def test_failed_workspace_allocation_keeps_the_plan_usable():
     """Host-side allocation failure: a 65535-wave group of 1024^2 waves (512 GiB)
     cannot be allocated.  set_schedule reports MSX_ERR_ALLOC and the plan keeps its
