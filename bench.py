@@ -448,6 +448,12 @@ def run_uneven(args):
     torch.cuda.synchronize()
     build_s = time.perf_counter() - t0
     batch = engine.Batch(branches=args.branches)
+    tuned = None
+    if args.autotune:
+        t1 = time.perf_counter()
+        batch.autotune(jobs)
+        torch.cuda.synchronize()
+        tuned = time.perf_counter() - t1
     for _ in range(max(args.warmup, 3)):
         batch.run(jobs)
     torch.cuda.synchronize()
@@ -470,7 +476,8 @@ def run_uneven(args):
             'vs_baseline': None, 'dtype': 'c64', 'data': 'synthetic (64 seeded random cubic crystals)',
             'config': {'workload': 'uneven batch of 64 random crystals, one CUDA graph', 'probes': P,
                        'probe_slices': ps, 'probe_slice_pixels_per_s': psp / (ms / 1e3),
-                       'grids': grids, 'branches': args.branches, 'build_s': build_s}}
+                       'grids': grids, 'branches': args.branches, 'build_s': build_s,
+                       'autotune_s': tuned}}
     print(json.dumps(line), flush=True)
     batch.close()
 

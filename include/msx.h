@@ -301,6 +301,11 @@ MSX_API int msx_batch_destroy(msx_batch* batch);
 /* Schedule and group size used for the (ny, nx) plans of the batch. */
 MSX_API int msx_batch_set_schedule(msx_batch* batch, int ny, int nx, int row_schedule, int col_schedule, int group);
 MSX_API int msx_batch_run(msx_batch* batch, const msx_job* jobs, int njobs, void* stream);
+/* msx_plan_autotune for every grid size of the job list, on the job of that
+ * size with the most positions (`iters` slices per candidate, workspace up to
+ * the batch's 512 MiB per plan); the winners become the batch's schedules.
+ * Synchronises `stream`. */
+MSX_API int msx_batch_autotune(msx_batch* batch, const msx_job* jobs, int njobs, int iters, void* stream);
 /* msx_plan_check over every plan of the batch. */
 MSX_API int msx_batch_check(msx_batch* batch);
 

@@ -61,6 +61,7 @@ SIGNATURES = [
     ('msx_batch_destroy', _c.c_int, [_vp]),
     ('msx_batch_set_schedule', _c.c_int, [_vp, _c.c_int, _c.c_int, _c.c_int, _c.c_int, _c.c_int]),
     ('msx_batch_run', _c.c_int, [_vp, _vp, _c.c_int, _vp]),
+    ('msx_batch_autotune', _c.c_int, [_vp, _vp, _c.c_int, _c.c_int, _vp]),
     ('msx_batch_check', _c.c_int, [_vp]),
     ('msx_tc_dft', _c.c_int, [_vp, _c.c_int, _c.c_int, _c.c_int, _vp, _vp]),
     ('msx_step_waves_tc', _c.c_int, [_vp, _c.c_int, _c.c_int, _vp, _vp, _vp]),

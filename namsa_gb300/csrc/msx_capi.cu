@@ -1041,6 +1041,39 @@ int msx_batch_set_schedule(msx_batch* b, int ny, int nx, int row_schedule, int c
   return MSX_OK;
 }
 
+int msx_batch_autotune(msx_batch* b, const msx_job* jobs, int njobs, int iters, void* stream) {
+  if (!b || (!jobs && njobs > 0) || njobs < 0 || iters <= 0) return fail(MSX_ERR_INVALID, "bad batch autotune arguments");
+  // one representative per grid: the job with the most positions (ties: the first)
+  std::vector<int> rep;
+  for (int i = 0; i < njobs; ++i) {
+    const msx_job& j = jobs[i];
+    if (j.num_slices <= 0 || j.num_probes <= 0) continue;
+    bool seen = false;
+    for (int& r : rep)
+      if (jobs[r].ny == j.ny && jobs[r].nx == j.nx) {
+        seen = true;
+        if (j.num_probes > jobs[r].num_probes) r = i;
+      }
+    if (!seen) rep.push_back(i);
+  }
+  for (int r : rep) {
+    const msx_job& j = jobs[r];
+    msx_plan* p = nullptr;
+    int rc = msx_plan_create(j.ny, j.nx, 0, &p);
+    if (rc != MSX_OK) return rc;
+    // the batch keeps at most 512 MiB of waves per plan and branch
+    rc = msx_plan_autotune(p, j.trans_dev, j.num_slices, j.psi_k_dev, j.normalization_dev, j.positions_dev,
+                           j.num_probes, j.kmax, j.lambda, j.slice_t, j.k_band, iters, (size_t)512 << 20, nullptr,
+                           stream);
+    int row = 0, col = 0, group = 0;
+    if (rc == MSX_OK) rc = msx_plan_get_schedule(p, &row, &col, &group);
+    msx_plan_destroy(p);
+    if (rc == MSX_OK) rc = msx_batch_set_schedule(b, j.ny, j.nx, row, col, group);
+    if (rc != MSX_OK) return rc;
+  }
+  return MSX_OK;
+}
+
 int msx_batch_run(msx_batch* b, const msx_job* jobs, int njobs, void* stream) {
   if (!b) return fail(MSX_ERR_INVALID, "null batch");
   if (njobs < 0 || (njobs > 0 && !jobs)) return fail(MSX_ERR_INVALID, "bad job list");

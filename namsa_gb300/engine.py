@@ -367,9 +367,8 @@ class Batch:
     def set_schedule(self, ny, nx, row, col, group=0):
         _lib.check(lib().msx_batch_set_schedule(self._h, int(ny), int(nx), int(row), int(col), int(group)))
 
-    def run(self, jobs):
-        """jobs: list of dicts with keys trans, psik, norm, positions, kmax, lam, slice_t,
-        k_band, out (CUDA tensors / numbers as for Plan.multislice).  Returns the outs."""
+    @staticmethod
+    def _jobs(jobs):
         arr = (_lib.MsxJob * len(jobs))()
         for j, d in zip(arr, jobs):
             _need(d['trans'], torch.complex64, 'trans', 3)
@@ -384,9 +383,21 @@ class Batch:
             j.trans_dev, j.psi_k_dev = d['trans'].data_ptr(), d['psik'].data_ptr()
             j.normalization_dev, j.positions_dev = d['norm'].data_ptr(), d['positions'].data_ptr()
             j.cbed_out_dev = d['out'].data_ptr()
+        return arr
+
+    def run(self, jobs):
+        """jobs: list of dicts with keys trans, psik, norm, positions, kmax, lam, slice_t,
+        k_band, out (CUDA tensors / numbers as for Plan.multislice).  Returns the outs."""
+        arr = self._jobs(jobs)
         _lib.check(lib().msx_batch_run(self._h, ctypes.cast(arr, _vp), len(jobs), _stream()))
         self._keep = jobs  # the graph refers to these buffers until the next run
         return [d['out'] for d in jobs]
+
+    def autotune(self, jobs, iters=8):
+        """Autotune every grid size of `jobs` on its largest job; the winners become
+        the batch's schedules (and replace those of existing plans)."""
+        arr = self._jobs(jobs)
+        _lib.check(lib().msx_batch_autotune(self._h, ctypes.cast(arr, _vp), len(jobs), int(iters), _stream()))
 
     def check(self):
         _lib.check(lib().msx_batch_check(self._h))

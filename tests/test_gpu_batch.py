@@ -56,3 +56,23 @@ def test_batch_job_vs_fp64_oracle():
     err = O.rel_l2(j['out'].cpu().numpy(), ref)
     assert err.max() < 2e-5, err
     batch.close()
+
+
+def test_batch_autotune_keeps_results():
+    """msx_batch_autotune picks a schedule per grid size; the batch then still
+    matches single default-schedule calls to FP32 rounding."""
+    specs, sims, jobs = small_batch(17, 6)
+    batch = engine.Batch(branches=2)
+    batch.autotune(jobs, iters=2)
+    outs = [o.clone() for o in batch.run(jobs)]
+    torch.cuda.synchronize()
+    batch.check()
+    for j, o in zip(jobs, outs):
+        plan = engine.Plan(j['trans'].shape[1], j['trans'].shape[2])
+        ref = plan.multislice(j['trans'], j['psik'], j['norm'], j['positions'], j['kmax'], j['lam'], j['slice_t'],
+                              j['k_band'])
+        torch.cuda.synchronize()
+        err = (torch.linalg.vector_norm((o - ref).double()) / torch.linalg.vector_norm(ref.double())).item()
+        assert err < 1e-5, err
+        plan.close()
+    batch.close()
