@@ -11,6 +11,7 @@ workloads the parity tests use, and writes the rendered sources into
   c1  Si 4x4x20 cells (face-inclusive), 256^2, 100 keV, t = a/4 (80 slices)
   c2  Si 8x8x50 cells (face-inclusive), 512^2, 200 keV, t = a/4 (199 slices)
   c4  SrTiO3 12x12x16 cells, 256^2, 300 keV, t = a/2 (three species)
+  c5  SrTiO3 18x12x8 cells (x, y, z), a rectangular 256 x 384 (y, x) grid, 200 keV
 
 plus ``oracle/_ref/workloads.json`` with the rendered parameters.  The sources
 are then compiled against the stand-in header ``oracle/pycuda-complex.hpp`` and
@@ -39,6 +40,7 @@ WORKLOADS = {
     'c1': dict(crystal='si', cells=(4, 4, 20), n=256, kv=100.0, semi=20e-3, slice_t=A_SI / 4),
     'c2': dict(crystal='si', cells=(8, 8, 50), n=512, kv=200.0, semi=30e-3, slice_t=A_SI / 4),
     'c4': dict(crystal='srtio3', cells=(12, 12, 16), n=256, kv=300.0, semi=25e-3, slice_t=A_STO / 2),
+    'c5': dict(crystal='srtio3', cells=(18, 12, 8), n=(256, 384), kv=200.0, semi=25e-3, slice_t=A_STO / 2),
 }
 
 
@@ -53,15 +55,16 @@ def workload_params(tag):
     sys.path.insert(0, ROOT)
     from oracle import msa_oracle as O
     w = WORKLOADS[tag]
+    ny, nx = w['n'] if isinstance(w['n'], tuple) else (w['n'], w['n'])
     sc = supercell(w['crystal'], w['cells'])
     xyz = np.column_stack([sc['x'], sc['y'], sc['z']]).astype(np.float32)
-    geom = O.Geometry(xyz, sc['atomic_number'], w['kv'], w['semi'], [w['n'], w['n']])
+    geom = O.Geometry(xyz, sc['atomic_number'], w['kv'], w['semi'], [ny, nx])
     kirk = np.load(os.path.join(ROOT, 'namsa_gb300', 'data', 'kirkland_params.npy'))
     _, win = O.atom_windows(geom, kirk)
     t = w['slice_t']
     sites = O.slice_sites_gpu(geom, t)
     max_sites = max(len(s) for s in sites)
-    return dict(tag=tag, ny=w['n'], nx=w['n'], pot_y=int(win.shape[1]), pot_x=int(win.shape[2]),
+    return dict(tag=tag, ny=ny, nx=nx, pot_y=int(win.shape[1]), pot_x=int(win.shape[2]),
                 num_slices=len(sites), sites_size=3 * max_sites, species=int(win.shape[0]),
                 crystal=w['crystal'], cells=list(w['cells']), kv=w['kv'], semi=w['semi'], slice_t=t)
 

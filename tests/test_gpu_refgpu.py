@@ -8,7 +8,8 @@ driven in MSAGPU's order (oracle/refgpu_harness.cu), on identical inputs.
   rounding of k moves it by up to ~1e-5.  The engine evaluates it in double.
 * CBED: relative L2 <= 1e-4 per pattern (FP32 engine vs FP32 reference path), for
   the single-probe Si 256^2 case, 64 positions of the Si 512^2 1024-position scan
-  and a three-species SrTiO3 256^2 case at 300 keV with defocus and Cs
+  a three-species SrTiO3 256^2 case at 300 keV with defocus and Cs, and a rectangular
+  256 x 384 SrTiO3 grid
 
 The harness libraries are built by oracle/build_ref.py from kernels rendered where
 the reference checkout exists; without them these tests skip with that reason.
@@ -45,18 +46,18 @@ def _case(tag):
     meta = ref.meta
     torch.cuda.set_device(0)
     sc = RR.supercell(meta.get('crystal', 'si'), meta['cells'])
-    n = meta['ny']
-    sim = M.MSAGPU(meta['kv'], meta['semi'], sc, sampling=np.array([n, n]), debye_waller=False)
+    n = [meta['ny'], meta['nx']]
+    sim = M.MSAGPU(meta['kv'], meta['semi'], sc, sampling=np.array(n), debye_waller=False)
     sim.setup_device(0)
     sim.calc_atomic_potentials()
     sim.build_potential_slices(meta['slice_t'])
     xyz = np.column_stack([sc['x'], sc['y'], sc['z']]).astype(np.float32)
-    geom = O.Geometry(xyz, sc['atomic_number'], meta['kv'], meta['semi'], [n, n])
+    geom = O.Geometry(xyz, sc['atomic_number'], meta['kv'], meta['semi'], n)
     _, win = O.atom_windows(geom, M.kirkland_table())
     return ref, sim, geom, win
 
 
-@pytest.mark.parametrize('tag', ['c1', 'c2', 'c4'])
+@pytest.mark.parametrize('tag', ['c1', 'c2', 'c4', 'c5'])
 def test_transmission_bit_identical_to_reference_kernel(tag):
     ref, sim, geom, win = _case(tag)
     t_ref = ref.build_potential(geom, ref.meta['slice_t'], win)
@@ -66,7 +67,7 @@ def test_transmission_bit_identical_to_reference_kernel(tag):
     sim.close()
 
 
-@pytest.mark.parametrize('tag,pd', [('c1', PROBE_C1), ('c2', PROBE_C2), ('c4', PROBE_C4)])
+@pytest.mark.parametrize('tag,pd', [('c1', PROBE_C1), ('c2', PROBE_C2), ('c4', PROBE_C4), ('c5', PROBE_C2)])
 def test_probe_matches_reference_kernels(tag, pd):
     ref, sim, geom, _ = _case(tag)
     sim.build_probe(pd)
@@ -116,4 +117,11 @@ def test_cbed_scan_si512_sampled_matches_reference_gpu_path():
 def test_cbed_srtio3_three_species_matches_reference_gpu_path():
     pos = np.array([[0., 0.], [1.0, 1.9], [-2.2, 0.7]])
     err, got, want = _cbed_parity('c4', PROBE_C4, pos)
+    assert err.max() <= 1e-4, err
+
+
+def test_cbed_rectangular_grid_matches_reference_gpu_path():
+    pos = np.array([[0., 0.], [1.3, -2.1]])
+    err, got, want = _cbed_parity('c5', PROBE_C2, pos)
+    assert got.shape == (2, 256, 384)
     assert err.max() <= 1e-4, err
