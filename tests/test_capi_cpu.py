@@ -47,6 +47,14 @@ def test_argument_errors_without_device(libmsx):
     assert libmsx.msx_multislice(None, None, 1, None, None, None, 1, 1.0, 0.02, 1.0, 1.0, None, 1, 1, None) == \
         _lib.MSX_ERR_INVALID
     assert libmsx.msx_plan_destroy(None) == 0
+    # newer entry points reject bad arguments before touching a device
+    assert libmsx.msx_multislice_host(None, None, 1, None, ctypes.c_double(1.0), None, 1, ctypes.c_float(1.0),
+                                      ctypes.c_double(0.02), ctypes.c_double(1.0), ctypes.c_float(1.0), None, 1, 1,
+                                      None) == _lib.MSX_ERR_INVALID
+    assert libmsx.msx_batch_autotune(None, None, 0, 1, None) == _lib.MSX_ERR_INVALID
+    assert libmsx.msx_selftest_wait(0, 5, None) == _lib.MSX_ERR_INVALID
+    assert libmsx.msx_selftest_wait(0, 40, None) == _lib.MSX_ERR_INVALID
+    assert 'limit_log2' in _lib.last_error()
 
 
 def test_reference_gpu_harness_exports_and_site_layout():
