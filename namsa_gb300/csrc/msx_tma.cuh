@@ -281,13 +281,25 @@ __global__ void __launch_bounds__(S::THREADS, S::MINB) col_mid_tma_kernel(const 
   int loaded = 0;  // tiles handed to the copy engine (thread 0 only)
   if (tid == 0)
     for (; loaded < 2 && loaded < mine; ++loaded) load(loaded);
+  // this column's propagator factor and mask band, fetched one tile ahead
+  auto column_of = [&](int k) { return ((int)(blockIdx.x + k * gridDim.x) / a.G) * C + c; };
+  float2 px_next = make_float2(0.f, 0.f);
+  int2 bd_next = make_int2(1, 0);
+  if (mine > 0) {
+    px_next = __ldg(a.pyx + NY + column_of(0));
+    bd_next = __ldg(a.band + column_of(0));
+  }
   for (int k = 0; k < mine; ++k) {
     const int s = k & 1;
     const int tile = blockIdx.x + k * gridDim.x;
     const int p = tile % a.G, xt = tile / a.G;
     const int x = xt * C + c;
-    const float2 px = __ldg(a.pyx + NY + x);  // consumed after the forward transform
-    const int2 bd = __ldg(a.band + x);
+    const float2 px = px_next;
+    const int2 bd = bd_next;
+    if (k + 1 < mine) {
+      px_next = __ldg(a.pyx + NY + column_of(k + 1));
+      bd_next = __ldg(a.band + column_of(k + 1));
+    }
     const bool ok = mbar_wait_bounded(&full[s], (k >> 1) & 1);
     if (!__syncthreads_and(ok)) {  // #0
       if (tid == 0) {
