@@ -288,10 +288,10 @@ def run_ours(args):
     from namsa_gb300 import engine
 
     rank, world, local = dist_env()
+    torch.cuda.set_device(local)  # before the process group, so NCCL binds this rank's GPU
+    dev = torch.device('cuda', local)
     if world > 1:
         dist.init_process_group('nccl', init_method='env://')
-    torch.cuda.set_device(local)
-    dev = torch.device('cuda', local)
     want_cpu = (rank == 0 and world == 1 and not args.no_cpu_baseline)
 
     sim, build_ms = build_workload(local, need_potential=want_cpu)
