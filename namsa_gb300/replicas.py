@@ -13,6 +13,7 @@ tensors, gloo with host tensors).
 """
 from __future__ import annotations
 
+import os
 from datetime import timedelta
 
 import numpy as np
@@ -66,9 +67,12 @@ def max_over_ranks(value, group=None):
 
 def init_from_env(backend=None, timeout_s=300):
     """Process group from RANK / WORLD_SIZE / MASTER_ADDR / MASTER_PORT; NCCL when a GPU
-    is visible, gloo otherwise.  Returns (rank, world)."""
+    is visible, gloo otherwise.  With NCCL the process first selects GPU LOCAL_RANK
+    (one process per GPU).  Returns (rank, world)."""
     if not dist.is_initialized():
         backend = backend or ('nccl' if torch.cuda.is_available() else 'gloo')
+        if backend == 'nccl':
+            torch.cuda.set_device(int(os.environ.get('LOCAL_RANK', 0)))
         dist.init_process_group(backend, init_method='env://', timeout=timedelta(seconds=timeout_s))
     return dist.get_rank(), dist.get_world_size()
 
