@@ -43,10 +43,7 @@ WORKLOAD = 'Si[001] 8x8x50 cells, 512x512 c64, 199 slices (t=a/4), 200 keV, 30 m
 # DRAM bytes (read + write) per launch of a pass, from the ncu --set full capture
 # summarised in profiles/row_col_tma_passes_si512_g512.md, keyed by (pass, line
 # length, schedule index, waves per launch); other keys report null.
-NCU_TRAFFIC = {
-    ('row', 512, 1, 512): 1.076813e9 + 1.012529e9,   # row_pass_tma_kernel t32_r16x16x2
-    ('col', 512, 0, 512): 1.198959e9 + 1.012810e9,   # col_mid_tma_kernel t16_r32x16
-}
+NCU_TRAFFIC = {}
 
 
 def parse():
@@ -383,8 +380,16 @@ def run_ours(args):
     N = 512 * 512
     dom = 'row' if row_ms >= col_ms else 'col'
     dom_ms = max(row_ms, col_ms)
-    alg_bytes = 16.0 * N * gw + 8.0 * N
-    alg_flops = (10.0 * N * math.log2(512) + 15.0 * N) * gw
+    # From the second slice on the passes keep only the column tiles [lo, hi) that
+    # the bandwidth mask can reach (a fraction fb of the columns): the row pass reads
+    # whole rows and writes that range, the column pass reads and writes that range.
+    lo, hi = engine.band_columns(512, kmax32, kband, engine.col_tile(512, plan.schedule[1]))
+    fb = (hi - lo) / 512.0
+    row_bytes = 8.0 * N * gw * (1.0 + fb) + 8.0 * N
+    col_bytes = 16.0 * N * gw * fb + 8.0 * 512
+    alg_bytes = row_bytes if dom == 'row' else col_bytes
+    line_flops = (10.0 * N * math.log2(512) + 15.0 * N) * gw  # both transforms of every line of one pass
+    alg_flops = line_flops if dom == 'row' else line_flops * fb
     peaks = {}
     pk_path = os.path.join(ROOT, 'MEASURED_PEAKS.json')
     if os.path.exists(pk_path):
@@ -398,6 +403,7 @@ def run_ours(args):
     roof = {'bound': 'hbm', 'achieved': achieved, 'peak': hbm_peak, 'unit': 'GB/s', 'frac': achieved / hbm_peak,
             'traffic': NCU_TRAFFIC.get((dom, 512, plan.schedule[0] if dom == 'row' else plan.schedule[1], gw)),
             'kernel': f'{dom}_pass_kernel (512, {gw} waves per launch)', 'peak_source': f'{peak_src} hbm_gbs',
+            'band_columns': [lo, hi], 'algorithmic_bytes_per_launch': alg_bytes,
             'launch_ms': dom_ms, 'row_pass_ms': row_ms, 'col_pass_ms': col_ms,
             'fp32': {'achieved_tflops': alg_flops / (dom_ms / 1e3) / 1e12, 'peak_tflops': fp32_peak,
                      'frac': alg_flops / (dom_ms / 1e3) / 1e12 / fp32_peak,

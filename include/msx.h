@@ -76,6 +76,18 @@ MSX_API int msx_supported_size(int n);
 /* Number of compiled FFT schedules for line length n, and the name of one. */
 MSX_API int msx_num_schedules(int n);
 MSX_API int msx_schedule_name(int n, int index, char* buf, size_t len);
+/* Columns per tile of a schedule's column pass. */
+MSX_API int msx_schedule_col_tile(int n, int index, int* tile);
+
+/*
+ * Band-limited column range of the persistent passes (no counterpart in the
+ * reference, whose every slice transforms the whole grid).  Every column with
+ * |kx| >= k_band is zeroed whole by the bandwidth mask (msa.py:829-839), so from
+ * the second slice on the passes leave the columns outside [x_lo, x_hi) alone
+ * (they stay zero); the range is aligned to `tile` columns and keeps a 1e-6
+ * relative margin on k_band.  Host only.
+ */
+MSX_API int msx_band_columns(int nx, float kmax, float k_band, int tile, int* x_lo, int* x_hi);
 
 /*
  * Projected Kirkland potential windows of `nspecies` species.

@@ -28,6 +28,9 @@ SIGNATURES = [
     ('msx_supported_size', _c.c_int, [_c.c_int]),
     ('msx_num_schedules', _c.c_int, [_c.c_int]),
     ('msx_schedule_name', _c.c_int, [_c.c_int, _c.c_int, _c.c_char_p, _c.c_size_t]),
+    ('msx_schedule_col_tile', _c.c_int, [_c.c_int, _c.c_int, _c.POINTER(_c.c_int)]),
+    ('msx_band_columns', _c.c_int, [_c.c_int, _c.c_float, _c.c_float, _c.c_int, _c.POINTER(_c.c_int),
+                                    _c.POINTER(_c.c_int)]),
     ('msx_atom_windows', _c.c_int, [_vp, _c.c_int, _c.c_int, _c.c_int, _c.c_int, _c.c_double, _vp, _vp]),
     ('msx_build_transmission', _c.c_int, [_vp, _vp, _c.c_int, _vp, _c.c_int, _c.c_int, _c.c_int, _c.c_int,
                                           _c.c_float, _vp, _vp, _vp]),

@@ -218,11 +218,40 @@ struct MsArgs {
 };
 
 // One slice's row pass and (mid) column pass over a group of gn waves.
-int slice_passes(msx_plan* p, const float2* trans_s, int gn, const ColArgs& c, bool with_col, cudaStream_t st) {
+// Band-limited column range.  A column whose |kx| reaches the mask radius has
+// |k| >= k_band for every ky, so the column pass zeroes it whole; from the second
+// slice on those columns are zero on entry, stay zero through the row pass (which
+// then need not write them) and need no column pass.  [x_lo, x_hi) is the range
+// of column tiles (width C) holding every column with |kx| < k_band, with a
+// 1e-6 relative margin on k_band so that it contains every column the device's
+// float32 mask test keeps.  The whole grid when no column is in the band.
+void band_columns(int nx, float kmax, float k_band, int C, int* x_lo, int* x_hi) {
+  const double km = (double)kmax, lim = (double)k_band * (1.0 + 1e-6);
+  int lo = nx, hi = -1;
+  for (int j = 0; j < nx; ++j) {
+    const double kx = (double)j * km / (double)(nx - 1) - km / 2.0;
+    if (std::fabs(kx) < lim) {
+      lo = j < lo ? j : lo;
+      hi = j;
+    }
+  }
+  if (hi < 0 || C <= 0) {
+    *x_lo = 0;
+    *x_hi = nx;
+    return;
+  }
+  *x_lo = (lo / C) * C;
+  *x_hi = (hi / C + 1) * C < nx ? (hi / C + 1) * C : nx;
+}
+
+// x_lo, x_hi: the column range of the TMA passes (0, 0 = all columns); the
+// plain passes always cover every column.
+int slice_passes(msx_plan* p, const float2* trans_s, int gn, const ColArgs& c, bool with_col, cudaStream_t st,
+                 int x_lo = 0, int x_hi = 0) {
   if (p->use_tma && p->map_ok) {
     TmaPassArgs ta{};
     ta.psi = p->psi; ta.trans = trans_s; ta.tw = p->tw_row; ta.pyx = p->pyx; ta.band = p->band; ta.err = p->err;
-    ta.G = gn; ta.Ny = p->ny; ta.Nx = p->nx;
+    ta.G = gn; ta.Ny = p->ny; ta.Nx = p->nx; ta.x_lo = x_lo; ta.x_hi = x_hi;
     MSX_CUDA(p->row_ops->row_tma(ta, p->row_ctas, st), "row pass");
     if (with_col) {
       ta.tw = p->tw_col;
@@ -278,6 +307,8 @@ int enqueue_multislice(msx_plan* p, const MsArgs& a, cudaStream_t st, const Host
   const size_t wave = (size_t)ny * nx;
   const int y0 = ny / 2 - a.crop_y / 2, x0 = nx / 2 - a.crop_x / 2;
   const float2* trans = reinterpret_cast<const float2*>(a.trans);
+  int bx_lo = 0, bx_hi = 0;
+  band_columns(nx, a.kmax, a.k_band, p->col_ops->col_c, &bx_lo, &bx_hi);
   // group done: hand its CBED block to the copy stream (host-buffer calls)
   auto hand_off = [&](int gi, int g0, int gn) -> int {
     if (!hp) return MSX_OK;
@@ -318,7 +349,9 @@ int enqueue_multislice(msx_plan* p, const MsArgs& a, cudaStream_t st, const Host
     for (int s = 0; s < a.num_slices; ++s) {
       if (hp && gi == 0 && s % hp->chunk == 0)
         MSX_CUDA(cudaStreamWaitEvent(st, (*hp->chunk_ev)[s / hp->chunk], 0), "cudaStreamWaitEvent");
-      const int rc = slice_passes(p, trans + (size_t)s * wave, gn, c, s + 1 < a.num_slices, st);
+      // the first slice covers every column (the probe may reach beyond the band)
+      const int rc = slice_passes(p, trans + (size_t)s * wave, gn, c, s + 1 < a.num_slices, st, s > 0 ? bx_lo : 0,
+                                  s > 0 ? bx_hi : 0);
       if (rc != MSX_OK) return rc;
       if (s + 1 == a.num_slices) {
         ColArgs f = c;
@@ -374,6 +407,20 @@ int msx_schedule_name(int n, int index, char* buf, size_t len) {
     std::strncpy(buf, ops[index].name, len - 1);
     buf[len - 1] = '\0';
   }
+  return MSX_OK;
+}
+
+int msx_schedule_col_tile(int n, int index, int* tile) {
+  const SchedOps* ops;
+  const int cnt = schedule_table(n, &ops);
+  if (index < 0 || index >= cnt || !tile) return fail(MSX_ERR_INVALID, "no schedule %d for length %d", index, n);
+  *tile = ops[index].col_c;
+  return MSX_OK;
+}
+
+int msx_band_columns(int nx, float kmax, float k_band, int tile, int* x_lo, int* x_hi) {
+  if (nx <= 1 || tile <= 0 || !x_lo || !x_hi || !(kmax > 0)) return fail(MSX_ERR_INVALID, "band_columns arguments");
+  band_columns(nx, kmax, k_band, tile, x_lo, x_hi);
   return MSX_OK;
 }
 
@@ -808,16 +855,19 @@ int msx_plan_profile(msx_plan* p, const float* trans_dev, int num_slices, const 
   MSX_CUDA(p->col_ops->col(COL_INIT, c, st), "probe formation pass");
   float row_ms = 0, col_ms = 0;
   const float2* trans = reinterpret_cast<const float2*>(trans_dev);
+  // the steady-state passes of multislice: the band-limited column range
+  int bx_lo = 0, bx_hi = 0;
+  band_columns(nx, kmax, k_band, p->col_ops->col_c, &bx_lo, &bx_hi);
   for (int i = 0; i < iters; ++i) {
     const int s = i % num_slices;
     MSX_CUDA(cudaEventRecord(ev[0], st), "cudaEventRecord");
-    int rc = slice_passes(p, trans + (size_t)s * wave, gn, c, false, st);
+    int rc = slice_passes(p, trans + (size_t)s * wave, gn, c, false, st, bx_lo, bx_hi);
     if (rc != MSX_OK) return rc;
     MSX_CUDA(cudaEventRecord(ev[1], st), "cudaEventRecord");
     if (p->use_tma && p->map_ok) {
       TmaPassArgs ta{};
       ta.psi = p->psi; ta.tw = p->tw_col; ta.pyx = p->pyx; ta.band = p->band; ta.err = p->err;
-      ta.G = gn; ta.Ny = ny; ta.Nx = nx;
+      ta.G = gn; ta.Ny = ny; ta.Nx = nx; ta.x_lo = bx_lo; ta.x_hi = bx_hi;
       MSX_CUDA(p->col_ops->col_tma(p->map, ta, p->col_ctas, st), "column pass");
     } else {
       MSX_CUDA(p->col_ops->col(COL_MID, c, st), "column pass");
@@ -874,16 +924,18 @@ int msx_plan_autotune(msx_plan* p, const float* trans_dev, int num_slices, const
     c.psi = p->psi; c.ptab = p->ptab; c.psik = reinterpret_cast<const float2*>(psi_k_dev); c.pos_yx = positions_dev;
     c.tw = p->tw_col; c.norm = normalization_dev; c.G = g; c.Nx = p->nx; c.kmax = kmax; c.x_begin = 0; c.ncols = p->nx;
     MSX_CUDA(p->col_ops->col(COL_INIT, c, st), "probe formation pass");
+    int bx_lo = 0, bx_hi = 0;  // time the steady-state (band-limited) passes
+    band_columns(p->nx, kmax, k_band, p->col_ops->col_c, &bx_lo, &bx_hi);
     for (int pass = 0; pass < 2; ++pass) {  // pass 0 warms caches and clocks
       MSX_CUDA(cudaEventRecord(e0, st), "cudaEventRecord");
       for (int i = 0; i < iters; ++i) {
         if (row_pass) {
-          const int r2 = slice_passes(p, trans + (size_t)(i % num_slices) * wave, g, c, false, st);
+          const int r2 = slice_passes(p, trans + (size_t)(i % num_slices) * wave, g, c, false, st, bx_lo, bx_hi);
           if (r2 != MSX_OK) return r2;
         } else if (p->use_tma && p->map_ok) {
           TmaPassArgs ta{};
           ta.psi = p->psi; ta.tw = p->tw_col; ta.pyx = p->pyx; ta.band = p->band; ta.err = p->err;
-          ta.G = g; ta.Ny = p->ny; ta.Nx = p->nx;
+          ta.G = g; ta.Ny = p->ny; ta.Nx = p->nx; ta.x_lo = bx_lo; ta.x_hi = bx_hi;
           MSX_CUDA(p->col_ops->col_tma(p->map, ta, p->col_ctas, st), "column pass");
         } else {
           MSX_CUDA(p->col_ops->col(COL_MID, c, st), "column pass");

@@ -72,7 +72,8 @@ template <class S> struct SchedImpl {
     return cudaGetLastError();
   }
   static cudaError_t col_tma(const CUtensorMap& map, const TmaPassArgs& a, int ctas, cudaStream_t st) {
-    const int ntiles = (a.Nx / S::C) * a.G;
+    const int ntiles = ((a.x_hi > 0 ? a.x_hi : a.Nx) / S::C - a.x_lo / S::C) * a.G;
+    if (ntiles <= 0) return cudaSuccess;
     const int grid = ntiles < ctas ? ntiles : ctas;
     col_mid_tma_kernel<S><<<grid, S::THREADS, ColTma<S>::smem(), st>>>(map, a);
     return cudaGetLastError();

@@ -90,6 +90,9 @@ struct TmaPassArgs {
   const int2* band;       // [lo, hi] ky band per column (column pass)
   int* err;               // bit 0: a bounded wait gave up
   int G, Ny, Nx;
+  // columns [x_lo, x_hi) written by the row pass and processed by the column
+  // pass (x_hi == 0: all); the columns outside hold zeros that stay zero
+  int x_lo, x_hi;
 };
 
 // ----------------------------------------------------------------------------- row pass
@@ -196,8 +199,12 @@ __global__ void __launch_bounds__(S::THREADS, S::MINB) row_pass_tma_kernel(TmaPa
     S::FFT::template run<false, false>(v, buf, tw, t);
     if (slot < nl) {
       float2* out = a.psi + ((size_t)(p0 + slot) * a.Ny + y) * NX;
+      const int xlo = a.x_lo, xhi = a.x_hi > 0 ? a.x_hi : NX;
 #pragma unroll
-      for (int m = 0; m < E; ++m) out[t + T * m] = v[m];
+      for (int m = 0; m < E; ++m) {
+        const int xk = t + T * m;
+        if (xk >= xlo && xk < xhi) out[xk] = v[m];
+      }
     }
     fence_proxy_async();  // this warp's exchanges precede the next bulk copy into the stage
     __syncwarp();
@@ -263,13 +270,14 @@ __global__ void __launch_bounds__(S::THREADS, S::MINB) col_mid_tma_kernel(const 
     fence_mbar_init();
   }
   __syncthreads();
-  const int tiles_x = a.Nx / C;
+  const int xt0 = a.x_lo / C;  // column tiles xt0 .. xt0 + tiles_x - 1
+  const int tiles_x = (a.x_hi > 0 ? a.x_hi : a.Nx) / C - xt0;
   const int ntiles = tiles_x * a.G;
   const int mine = (int)blockIdx.x < ntiles ? (ntiles - 1 - (int)blockIdx.x) / (int)gridDim.x + 1 : 0;
 
   auto load = [&](int k) {  // this CTA's k-th tile into stage k & 1
     const int tile = blockIdx.x + k * gridDim.x;
-    const int p = tile % a.G, xt = tile / a.G;
+    const int p = tile % a.G, xt = xt0 + tile / a.G;
     float2* dst = stage + (k & 1) * STAGE;
     uint64_t* bar = &full[k & 1];
     mbar_expect_tx(bar, (uint32_t)(STAGE * sizeof(float2)));
@@ -282,7 +290,7 @@ __global__ void __launch_bounds__(S::THREADS, S::MINB) col_mid_tma_kernel(const 
   if (tid == 0)
     for (; loaded < 2 && loaded < mine; ++loaded) load(loaded);
   // this column's propagator factor and mask band, fetched one tile ahead
-  auto column_of = [&](int k) { return ((int)(blockIdx.x + k * gridDim.x) / a.G) * C + c; };
+  auto column_of = [&](int k) { return (xt0 + (int)(blockIdx.x + k * gridDim.x) / a.G) * C + c; };
   float2 px_next = make_float2(0.f, 0.f);
   int2 bd_next = make_int2(1, 0);
   if (mine > 0) {
@@ -292,7 +300,7 @@ __global__ void __launch_bounds__(S::THREADS, S::MINB) col_mid_tma_kernel(const 
   for (int k = 0; k < mine; ++k) {
     const int s = k & 1;
     const int tile = blockIdx.x + k * gridDim.x;
-    const int p = tile % a.G, xt = tile / a.G;
+    const int p = tile % a.G, xt = xt0 + tile / a.G;
     const int x = xt * C + c;
     const float2 px = px_next;
     const int2 bd = bd_next;

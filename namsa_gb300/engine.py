@@ -57,6 +57,21 @@ def supported_size(n):
     return bool(lib().msx_supported_size(int(n)))
 
 
+def col_tile(n, index):
+    """Columns per tile of schedule `index`'s column pass for line length n."""
+    v = ctypes.c_int()
+    _lib.check(lib().msx_schedule_col_tile(int(n), int(index), ctypes.byref(v)))
+    return v.value
+
+
+def band_columns(nx, kmax, k_band, tile):
+    """[x_lo, x_hi): the columns the persistent passes keep from the second slice on."""
+    lo, hi = ctypes.c_int(), ctypes.c_int()
+    _lib.check(lib().msx_band_columns(int(nx), float(kmax), float(k_band), int(tile), ctypes.byref(lo),
+                                      ctypes.byref(hi)))
+    return lo.value, hi.value
+
+
 def schedules(n):
     """Names of the compiled FFT schedules for line length n."""
     out = []

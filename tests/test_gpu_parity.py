@@ -209,6 +209,40 @@ def test_host_buffer_multislice_matches_device_call(pinned):
     plan.close()
 
 
+def test_band_limited_passes_with_an_aperture_wider_than_the_band():
+    """From the second slice on the persistent passes skip the columns beyond the
+    bandwidth mask.  With a probe aperture wider than the mask (k_semi > k_band)
+    the first slice still covers every column: the result equals the plain
+    full-grid passes and the FP64 oracle."""
+    rng = np.random.default_rng(21)
+    n, S, P = 128, 6, 3
+    kmax = n / 20.0
+    g = geom_of(n, n, kmax, 0.025)
+    g.semi_ang = 0.08  # k_semi = 3.2 / Angstrom > k_band = kmax / 3 = 2.13
+    pd = {'smooth_apert': True, 'spherical_phase': True, 'aberration_dict': {'C1': 5., 'C3': 1e4, 'C5': 0.},
+          'scherzer': False}
+    psik, _, _ = O.probe_gpu(g, pd)
+    psik = psik.astype(np.complex64)
+    norm = float(np.sum(np.abs(np.fft.ifft2(psik.astype(np.complex128)) * n * n) ** 2))
+    trans = np.exp(0.3j * rng.standard_normal((S, n, n))).astype(np.complex64)
+    pos = rng.uniform(-6, 6, size=(P, 2)).astype(np.float32)
+    st = 1.5
+    args = (torch.from_numpy(trans).to(DEV), torch.from_numpy(psik).to(DEV),
+            torch.tensor([norm], dtype=torch.float64, device=DEV), torch.from_numpy(pos).to(DEV),
+            np.float32(kmax), 0.025, st, np.float32(kmax / 3))
+    lo, hi = engine.band_columns(n, np.float32(kmax), np.float32(kmax / 3), engine.col_tile(n, 0))
+    assert hi - lo < n  # the band really excludes columns here
+    plan = engine.Plan(n, n)
+    got = plan.multislice(*args).cpu().numpy()
+    plan.set_tma(False)
+    full = plan.multislice(*args).cpu().numpy()
+    plan.check()
+    plan.close()
+    assert np.abs(got - full).max() <= 1e-6 * np.abs(full).max()
+    ref = oracle_cbed(g, trans, psik, norm, pos, st, 1 / 3)
+    assert O.rel_l2(got, ref).max() < 2e-5
+
+
 def test_failed_workspace_allocation_keeps_the_plan_usable():
     """Host-side allocation failure: a 65535-wave group of 1024^2 waves (512 GiB)
     cannot be allocated.  set_schedule reports MSX_ERR_ALLOC and the plan keeps its

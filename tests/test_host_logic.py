@@ -135,3 +135,26 @@ def test_warp_column_layout_is_bank_conflict_free(n, rads):
                 for m in range(E):
                     assert _col_wavefronts([addr(perm(t + T * m), c) for t, c in lanes]) == 2
             ns *= R
+
+
+def test_band_columns_contain_every_column_the_mask_keeps():
+    """msx_band_columns: every column with a row that passes the float32 mask test
+    (|k| on the centred grid, as the device computes it) lies inside [x_lo, x_hi);
+    the range is tile-aligned and inside the grid."""
+    from namsa_gb300 import engine
+    rng = np.random.default_rng(5)
+    for _ in range(60):
+        nx = int(rng.choice([64, 128, 256, 384, 512, 768, 1024]))
+        ny = int(rng.choice([64, 256, 512]))
+        tile = int(rng.choice([8, 16, 32]))
+        kmax = np.float32(rng.uniform(2, 40))
+        k_band = np.float32(kmax * rng.uniform(0.05, 0.6))
+        lo, hi = engine.band_columns(nx, kmax, k_band, tile)
+        assert 0 <= lo < hi <= nx and lo % tile == 0 and (hi % tile == 0 or hi == nx)
+        km = np.float64(kmax)
+        kx = np.arange(nx, dtype=np.float64) * km / (nx - 1) - km / 2.0
+        ky = np.arange(ny, dtype=np.float64) * km / (ny - 1) - km / 2.0
+        k = np.sqrt(kx[None, :] * kx[None, :] + ky[:, None] * ky[:, None]).astype(np.float32)
+        kept = np.nonzero((k < k_band).any(axis=0))[0]
+        if kept.size:
+            assert lo <= kept.min() and kept.max() < hi, (nx, tile, lo, hi, kept.min(), kept.max())
