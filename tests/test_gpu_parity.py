@@ -215,10 +215,10 @@ def test_band_limited_passes_with_an_aperture_wider_than_the_band():
     the first slice still covers every column: the result equals the plain
     full-grid passes and the FP64 oracle."""
     rng = np.random.default_rng(21)
-    n, S, P = 128, 6, 3
+    n, S, P = 256, 6, 3
     kmax = n / 20.0
     g = geom_of(n, n, kmax, 0.025)
-    g.semi_ang = 0.08  # k_semi = 3.2 / Angstrom > k_band = kmax / 3 = 2.13
+    g.semi_ang = 0.12  # k_semi = 4.8 / Angstrom > k_band = kmax / 3 = 4.27
     pd = {'smooth_apert': True, 'spherical_phase': True, 'aberration_dict': {'C1': 5., 'C3': 1e4, 'C5': 0.},
           'scherzer': False}
     psik, _, _ = O.probe_gpu(g, pd)
