@@ -145,7 +145,6 @@ __global__ void __launch_bounds__(S::THREADS, S::MINB) row_pass_tma_kernel(TmaPa
   const int pchunks = (a.G + L - 1) / L;
   const int ntiles = a.Ny * pchunks;
   const int mine = (int)blockIdx.x < ntiles ? (ntiles - 1 - (int)blockIdx.x) / (int)gridDim.x + 1 : 0;
-  const int xlo = a.x_lo, xhi = a.x_hi > 0 ? a.x_hi : NX;  // columns outside are zero on entry
 
   auto issue = [&](int k) {  // this CTA's k-th tile into stage k % NS
     const int tile = blockIdx.x + k * gridDim.x;
@@ -154,11 +153,9 @@ __global__ void __launch_bounds__(S::THREADS, S::MINB) row_pass_tma_kernel(TmaPa
     const int nl = min(L, a.G - p0);
     float2* dst = stage + (k % NS) * STAGE;
     uint64_t* bar = &full[k % NS];
-    // only the column range can be non-zero: copy that segment of each row
-    const uint32_t seg = (uint32_t)((xhi - xlo) * sizeof(float2));
-    mbar_expect_tx(bar, (uint32_t)nl * seg + (uint32_t)(NX * sizeof(float2)));
+    mbar_expect_tx(bar, (uint32_t)((nl + 1) * NX * sizeof(float2)));
     for (int i = 0; i < nl; ++i)
-      bulk_g2s(dst + i * NX + xlo, a.psi + ((size_t)(p0 + i) * a.Ny + y) * NX + xlo, seg, bar);
+      bulk_g2s(dst + i * NX, a.psi + ((size_t)(p0 + i) * a.Ny + y) * NX, NX * sizeof(float2), bar);
     bulk_g2s(dst + L * NX, a.trans + (size_t)y * NX, NX * sizeof(float2), bar);
   };
 
@@ -195,16 +192,14 @@ __global__ void __launch_bounds__(S::THREADS, S::MINB) row_pass_tma_kernel(TmaPa
     SwizzledLine<ilog2(E)> buf{line};
     float2 v[E];
 #pragma unroll
-    for (int m = 0; m < E; ++m) {
-      const int xk = t + T * m;
-      v[m] = (xk >= xlo && xk < xhi) ? line[xk] : make_float2(0.f, 0.f);
-    }
+    for (int m = 0; m < E; ++m) v[m] = line[t + T * m];
     S::FFT::template run<true, false>(v, buf, tw, t);
 #pragma unroll
     for (int m = 0; m < E; ++m) v[m] = cmul(v[m], trow[t + T * m]);
     S::FFT::template run<false, false>(v, buf, tw, t);
     if (slot < nl) {
       float2* out = a.psi + ((size_t)(p0 + slot) * a.Ny + y) * NX;
+      const int xlo = a.x_lo, xhi = a.x_hi > 0 ? a.x_hi : NX;
 #pragma unroll
       for (int m = 0; m < E; ++m) {
         const int xk = t + T * m;
