@@ -380,4 +380,111 @@ struct LineFFT<N, T, Radices<Rs...>> {
   }
 };
 
+// ----------------------------------------------------------------- paired radix-2 line transform
+// Lines of 512 held by one warp (32 threads x 16 values, thread t holding
+// elements t + 32 m) with the radices (16, 2, 16) of LineFFT and its twiddle
+// table, but with the radix-2 stage done across lane pairs instead of through
+// shared memory.  After the first radix-16 stage, the Stockham butterfly
+// j = 16 t' + r (t' < 16) of the radix-2 stage combines output r of lane t'
+// (value a) with output r of lane t' + 16 (value b), and its twiddle W_32^r
+// depends on r alone.  Lane t' computes the butterflies r < 8, lane t' + 16
+// those with r >= 8, and each sends the other the eight values it needs (two
+// 32-bit shuffles apiece).  So that both lanes send the same register, the
+// upper lane negates its odd inputs, which moves output (r + 8) mod 16 of its
+// radix-16 DFT into register r: lane t' then sends a[8 + I] and lane t' + 16
+// sends b[I] from register 8 + I.  Butterfly outputs y0 = a + W b and
+// y1 = a - W b land at 32 t' + r and 32 t' + 16 + r; the last stage reads
+// t + 32 m.  Bank-conflict-free through the swizzle p ^ ((p >> 5) & 15): a
+// store of one register by a half warp covers 32 t' + c for sixteen t' and one
+// c < 32, a load 32 m + t for sixteen consecutive t.  One exchange through
+// shared memory per transform instead of two.
+struct PairedFFT512 {
+  static constexpr int N = 512, T = 32, E = 16;
+  using Base = LineFFT<512, 32, Radices<16, 2, 16>>;
+  static constexpr int kStage2Tw = 16;  // offset of the last stage's twiddles in Base's table
+  struct Line {
+    float2* base;
+    __host__ __device__ __forceinline__ float2& operator[](int i) const { return base[i ^ ((i >> 5) & 15)]; }
+  };
+  // first radix-16 stage of thread t (upper lane: h = t >= 16)
+  template <bool INV>
+  static __host__ __device__ __forceinline__ void first(float2 (&v)[E], bool h) {
+    const float sg = h ? -1.f : 1.f;
+#pragma unroll
+    for (int r = 1; r < 16; r += 2) v[r] = cscale(v[r], sg);
+    Dft<16, INV>::run(v);
+  }
+  // radix-2 butterfly I (< 8) of this lane; `recv` is the partner's register 8 + I
+  template <bool INV, int I>
+  static __host__ __device__ __forceinline__ void pair(float2 (&v)[E], float2 recv, bool h) {
+    const float2 a = h ? recv : v[I];
+    float2 b = twc<32, I, INV>(h ? v[I] : recv);
+    const float2 b8 = twc<4, 1, INV>(b);  // the upper lane's butterfly is I + 8: one more W_32^8
+    b = h ? b8 : b;
+    v[I] = cadd(a, b);
+    v[8 + I] = csub(a, b);
+  }
+  // line position of register m of thread t after the radix-2 stage
+  static __host__ __device__ __forceinline__ int pos(int m, int t) {
+    return 32 * (t & 15) + 8 * (t >> 4) + m + (m >= 8 ? 8 : 0);
+  }
+  template <bool INV, int... Is>
+  static __device__ __forceinline__ void pairs(float2 (&v)[E], bool h, std::integer_sequence<int, Is...>) {
+    (pair<INV, Is>(v, make_float2(__shfl_xor_sync(0xffffffffu, v[8 + Is].x, 16),
+                                  __shfl_xor_sync(0xffffffffu, v[8 + Is].y, 16)), h), ...);
+  }
+  // In-place transform of the line held by the warp (unnormalised); `line` is
+  // the warp's 512-word exchange buffer, whose earlier readers must be this
+  // warp's own threads.
+  template <bool INV>
+  static __device__ __forceinline__ void run(float2 (&v)[E], float2* line, const float2* tw, int t) {
+    const bool h = t >= 16;
+    first<INV>(v, h);
+    pairs<INV>(v, h, std::make_integer_sequence<int, 8>{});
+    const Line buf{line};
+    __syncwarp();  // earlier reads of the buffer are done
+#pragma unroll
+    for (int m = 0; m < E; ++m) buf[pos(m, t)] = v[m];
+    __syncwarp();
+#pragma unroll
+    for (int m = 0; m < E; ++m) v[m] = buf[t + T * m];
+    float2 out[E];
+    Base::template butterflies<16, 32, kStage2Tw, INV>(v, out, tw, t);
+#pragma unroll
+    for (int m = 0; m < E; ++m) v[m] = out[m];
+  }
+
+  // Host emulation of run() on a whole line (natural order), for the host-side
+  // check of the lane arithmetic; the shuffles become reads of the partner's
+  // registers.
+  template <bool INV, int... Is>
+  static void host_pairs(float2 (*v)[E], std::integer_sequence<int, Is...>) {
+    auto one = [&](auto ic) {
+      constexpr int I = decltype(ic)::value;
+      float2 recv[T];
+      for (int t = 0; t < T; ++t) recv[t] = v[t ^ 16][8 + I];
+      for (int t = 0; t < T; ++t) pair<INV, I>(v[t], recv[t], t >= 16);
+    };
+    (one(std::integral_constant<int, Is>{}), ...);
+  }
+  template <bool INV>
+  static void host_run(float2* data, const float2* tw) {
+    static float2 v[T][E];
+    static float2 scratch[N];
+    const Line buf{scratch};
+    for (int t = 0; t < T; ++t) for (int m = 0; m < E; ++m) v[t][m] = data[t + T * m];
+    for (int t = 0; t < T; ++t) first<INV>(v[t], t >= 16);
+    host_pairs<INV>(v, std::make_integer_sequence<int, 8>{});
+    for (int t = 0; t < T; ++t) for (int m = 0; m < E; ++m) buf[pos(m, t)] = v[t][m];
+    for (int t = 0; t < T; ++t) {
+      for (int m = 0; m < E; ++m) v[t][m] = buf[t + T * m];
+      float2 out[E];
+      Base::template butterflies<16, 32, kStage2Tw, INV>(v[t], out, tw, t);
+      for (int m = 0; m < E; ++m) data[t + T * m] = out[m];
+    }
+  }
+  static constexpr int tw_words() { return Base::tw_words(); }
+  static void host_twiddles(float2* tw) { Base::host_twiddles(tw); }
+};
+
 }  // namespace msx

@@ -10,6 +10,7 @@ int schedules_512(const SchedOps** out) {
     SchedImpl<Sched<512, 32, 16, 1, 16, 16, 2>>::ops("t32_r16x16x2_c16"),
     SchedImpl<Sched<512, 32, 16, 1, 8, 8, 8>>::ops("t32_r8x8x8_c16"),
     SchedImpl<Sched<512, 32, 8, 2, 16, 2, 16>>::ops("t32_r16x2x16"),
+    SchedImpl<PairedRow<Sched<512, 32, 8, 2, 16, 2, 16>>>::ops("t32_r16x2x16_pair"),
   };
   *out = table;
   return (int)(sizeof(table) / sizeof(table[0]));

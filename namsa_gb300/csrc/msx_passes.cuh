@@ -18,6 +18,7 @@
 #pragma once
 #include "msx_fft.cuh"
 #include <cuda_runtime.h>
+#include <type_traits>
 
 namespace msx {
 
@@ -47,6 +48,16 @@ struct Sched {
   static constexpr size_t col_smem() { return sizeof(float2) * (TW_PAD + (size_t)C * N) + sizeof(float) * N; }
   static_assert(THREADS == 256 || THREADS == 512, "CTA of 256 or 512 threads");
   static_assert(T <= 32 && 32 % T == 0, "a row line must live inside one warp");
+  static constexpr bool PAIRED = false;  // persistent row pass uses PairedFFT512
+};
+
+// The same schedule with the persistent row pass transforming through
+// PairedFFT512 (radix-2 stage across lane pairs); every other pass unchanged.
+template <class S>
+struct PairedRow : S {
+  static_assert(std::is_same_v<typename S::FFT, LineFFT<512, 32, Radices<16, 2, 16>>>,
+                "paired row transform: lines of 512, 32 threads, radices 16 x 2 x 16");
+  static constexpr bool PAIRED = true;
 };
 
 template <int TW>

@@ -189,14 +189,21 @@ __global__ void __launch_bounds__(S::THREADS, S::MINB) row_pass_tma_kernel(TmaPa
     const int nl = min(L, a.G - p0);
     float2* line = stage + s * STAGE + slot * NX;
     const float2* trow = stage + s * STAGE + L * NX;
-    SwizzledLine<ilog2(E)> buf{line};
     float2 v[E];
 #pragma unroll
     for (int m = 0; m < E; ++m) v[m] = line[t + T * m];
-    S::FFT::template run<true, false>(v, buf, tw, t);
+    if constexpr (S::PAIRED) {
+      PairedFFT512::run<true>(v, line, tw, t);
 #pragma unroll
-    for (int m = 0; m < E; ++m) v[m] = cmul(v[m], trow[t + T * m]);
-    S::FFT::template run<false, false>(v, buf, tw, t);
+      for (int m = 0; m < E; ++m) v[m] = cmul(v[m], trow[t + T * m]);
+      PairedFFT512::run<false>(v, line, tw, t);
+    } else {
+      SwizzledLine<ilog2(E)> buf{line};
+      S::FFT::template run<true, false>(v, buf, tw, t);
+#pragma unroll
+      for (int m = 0; m < E; ++m) v[m] = cmul(v[m], trow[t + T * m]);
+      S::FFT::template run<false, false>(v, buf, tw, t);
+    }
     if (slot < nl) {
       float2* out = a.psi + ((size_t)(p0 + slot) * a.Ny + y) * NX;
       const int xlo = a.x_lo, xhi = a.x_hi > 0 ? a.x_hi : NX;

@@ -35,8 +35,41 @@ template <class F, int N> double check() {
   printf("N=%4d T=%2d E=%2d rel err %.3e\n", N, N / F::E, F::E, worst);
   return worst;
 }
+// The exchange of PairedFFT512: every half warp's store of one register and
+// every half warp's load of one element touch sixteen distinct bank pairs
+// (a float2 spans two 4-byte banks), and the swizzle is a permutation.
+bool paired_banks_ok() {
+  using P = PairedFFT512;
+  auto sw = [](int i) { return i ^ ((i >> 5) & 15); };
+  bool seen[512] = {};
+  for (int i = 0; i < 512; ++i) {
+    if (seen[sw(i)]) return false;
+    seen[sw(i)] = true;
+  }
+  for (int m = 0; m < 16; ++m)
+    for (int half = 0; half < 2; ++half) {
+      bool st[16] = {}, ld[16] = {};
+      for (int l = 0; l < 16; ++l) {
+        const int t = 16 * half + l;
+        const int bs = sw(P::pos(m, t)) & 15, bl = sw(t + 32 * m) & 15;
+        if (st[bs] || ld[bl]) return false;
+        st[bs] = ld[bl] = true;
+      }
+    }
+  // every position is written exactly once
+  bool hit[512] = {};
+  for (int t = 0; t < 32; ++t)
+    for (int m = 0; m < 16; ++m) {
+      if (hit[P::pos(m, t)]) return false;
+      hit[P::pos(m, t)] = true;
+    }
+  return true;
+}
 int main() {
   double w = 0;
+  const bool banks = paired_banks_ok();
+  printf("paired exchange conflict-free: %s\n", banks ? "yes" : "NO");
+  if (!banks) return 1;
   w = fmax(w, check<LineFFT<64, 8, Radices<8, 8>>, 64>());
   w = fmax(w, check<LineFFT<128, 8, Radices<16, 8>>, 128>());
   w = fmax(w, check<LineFFT<256, 16, Radices<16, 16>>, 256>());
@@ -46,6 +79,7 @@ int main() {
   w = fmax(w, check<LineFFT<512, 32, Radices<16, 16, 2>>, 512>());
   w = fmax(w, check<LineFFT<512, 32, Radices<8, 8, 8>>, 512>());
   w = fmax(w, check<LineFFT<512, 32, Radices<16, 2, 16>>, 512>());
+  w = fmax(w, check<PairedFFT512, 512>());
   w = fmax(w, check<LineFFT<768, 32, Radices<8, 8, 12>>, 768>());
   w = fmax(w, check<LineFFT<1024, 32, Radices<32, 32>>, 1024>());
   w = fmax(w, check<LineFFT<1024, 32, Radices<16, 8, 8>>, 1024>());
