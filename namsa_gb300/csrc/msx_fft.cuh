@@ -181,8 +181,68 @@ template <bool INV> struct Dft<6, INV> {
 template <bool INV> struct Dft<12, INV> {
   static __host__ __device__ __forceinline__ void run(float2 (&v)[12]) { dft_ct<4, 3, INV>(v); }
 };
+// 16-point DFT as 4 x 4 (X[ka + 4 kb] over inner DFTs of x[b + 4 a]) with the
+// twiddle scales folded into fused multiply-adds.  With s = -1 forward, +1
+// inverse, h = cos(pi/4), C = cos(pi/8) and tau = tan(pi/8):
+//   W^2 = h (1 + s i), W^4 = s i, W^6 = h (-1 + s i),
+//   W^1 = C (1 + s i tau), W^3 = C (tau + s i), W^9 = -C (1 + s i tau),
+// so in the outer DFTs of columns ka = 1, 2, 3 the pairs (z1, z3) and z2 carry
+// the common scales C and h, which are applied by the butterflies' FMAs:
+// 144 operations against 160 with the twiddles multiplied out.
+template <bool INV>
+__host__ __device__ __forceinline__ void dft16_outer(float2 u0, float2 z2h, float2 q1, float2 q3, float hs, float cs,
+                                                     float2& y0, float2& y1, float2& y2, float2& y3) {
+  // inputs z0 = u0, z2 = hs * z2h, z1 = cs * q1, z3 = cs * q3; outputs Y_kb of the 4-point DFT
+  constexpr float s = INV ? 1.f : -1.f;
+  const float2 a = make_float2(fmaf(hs, z2h.x, u0.x), fmaf(hs, z2h.y, u0.y));
+  const float2 b = make_float2(fmaf(-hs, z2h.x, u0.x), fmaf(-hs, z2h.y, u0.y));
+  const float2 P = cadd(q1, q3), Q = csub(q1, q3);
+  y0 = make_float2(fmaf(cs, P.x, a.x), fmaf(cs, P.y, a.y));
+  y2 = make_float2(fmaf(-cs, P.x, a.x), fmaf(-cs, P.y, a.y));
+  y1 = make_float2(fmaf(-s * cs, Q.y, b.x), fmaf(s * cs, Q.x, b.y));
+  y3 = make_float2(fmaf(s * cs, Q.y, b.x), fmaf(-s * cs, Q.x, b.y));
+}
 template <bool INV> struct Dft<16, INV> {
-  static __host__ __device__ __forceinline__ void run(float2 (&v)[16]) { dft_ct<4, 4, INV>(v); }
+  static __host__ __device__ __forceinline__ void run(float2 (&v)[16]) {
+    constexpr float s = INV ? 1.f : -1.f;
+    constexpr float h = 0.70710678118654752440f;    // cos(pi/4)
+    constexpr float C = 0.92387953251128675613f;    // cos(pi/8)
+    constexpr float tau = 0.41421356237309504880f;  // tan(pi/8)
+    float2 U[4][4];  // U[b][ka]: inner 4-point DFTs of x[b + 4 a]
+#pragma unroll
+    for (int b = 0; b < 4; ++b) {
+      float2 u[4] = {v[b], v[b + 4], v[b + 8], v[b + 12]};
+      Dft<4, INV>::run(u);
+#pragma unroll
+      for (int k = 0; k < 4; ++k) U[b][k] = u[k];
+    }
+    {  // ka = 0: no twiddles
+      float2 z[4] = {U[0][0], U[1][0], U[2][0], U[3][0]};
+      Dft<4, INV>::run(z);
+      v[0] = z[0]; v[4] = z[1]; v[8] = z[2]; v[12] = z[3];
+    }
+    {  // ka = 1: z1 = C q1, z2 = h p2, z3 = C q3
+      const float2 u1 = U[1][1], u2 = U[2][1], u3 = U[3][1];
+      const float2 q1 = make_float2(fmaf(-s * tau, u1.y, u1.x), fmaf(s * tau, u1.x, u1.y));  // u1 (1 + s i tau)
+      const float2 p2 = make_float2(u2.x - s * u2.y, u2.y + s * u2.x);                        // u2 (1 + s i)
+      const float2 q3 = make_float2(fmaf(tau, u3.x, -s * u3.y), fmaf(tau, u3.y, s * u3.x));  // u3 (tau + s i)
+      dft16_outer<INV>(U[0][1], p2, q1, q3, h, C, v[1], v[5], v[9], v[13]);
+    }
+    {  // ka = 2: z1 = h p1, z2 = s i u2, z3 = h p3 (the common scale h goes with z1, z3)
+      const float2 u1 = U[1][2], u2 = U[2][2], u3 = U[3][2];
+      const float2 p1 = make_float2(u1.x - s * u1.y, u1.y + s * u1.x);   // u1 (1 + s i)
+      const float2 z2 = make_float2(-s * u2.y, s * u2.x);                // s i u2
+      const float2 p3 = make_float2(-u3.x - s * u3.y, s * u3.x - u3.y);  // u3 (-1 + s i)
+      dft16_outer<INV>(U[0][2], z2, p1, p3, 1.f, h, v[2], v[6], v[10], v[14]);
+    }
+    {  // ka = 3: z1 = C q1, z2 = h p2, z3 = C q3
+      const float2 u1 = U[1][3], u2 = U[2][3], u3 = U[3][3];
+      const float2 q1 = make_float2(fmaf(tau, u1.x, -s * u1.y), fmaf(tau, u1.y, s * u1.x));    // u1 (tau + s i)
+      const float2 p2 = make_float2(-u2.x - s * u2.y, s * u2.x - u2.y);                         // u2 (-1 + s i)
+      const float2 q3 = make_float2(fmaf(s * tau, u3.y, -u3.x), fmaf(-s * tau, u3.x, -u3.y));  // -u3 (1 + s i tau)
+      dft16_outer<INV>(U[0][3], p2, q1, q3, h, C, v[3], v[7], v[11], v[15]);
+    }
+  }
 };
 template <bool INV> struct Dft<24, INV> {
   static __host__ __device__ __forceinline__ void run(float2 (&v)[24]) { dft_ct<8, 3, INV>(v); }
