@@ -202,47 +202,49 @@ __host__ __device__ __forceinline__ void dft16_outer(float2 u0, float2 z2h, floa
   y1 = make_float2(fmaf(-s * cs, Q.y, b.x), fmaf(s * cs, Q.x, b.y));
   y3 = make_float2(fmaf(s * cs, Q.y, b.x), fmaf(-s * cs, Q.x, b.y));
 }
-template <bool INV> struct Dft<16, INV> {
-  static __host__ __device__ __forceinline__ void run(float2 (&v)[16]) {
-    constexpr float s = INV ? 1.f : -1.f;
-    constexpr float h = 0.70710678118654752440f;    // cos(pi/4)
-    constexpr float C = 0.92387953251128675613f;    // cos(pi/8)
-    constexpr float tau = 0.41421356237309504880f;  // tan(pi/8)
-    float2 U[4][4];  // U[b][ka]: inner 4-point DFTs of x[b + 4 a]
+// `odd` (1 or -1) multiplies the odd-indexed inputs: they feed the inner DFTs
+// b = 1, 3, i.e. the pairs (z1, z3) of every outer DFT, whose scale it joins.
+template <bool INV>
+__host__ __device__ __forceinline__ void dft16(float2 (&v)[16], float odd) {
+  constexpr float s = INV ? 1.f : -1.f;
+  constexpr float h = 0.70710678118654752440f;    // cos(pi/4)
+  constexpr float C = 0.92387953251128675613f;    // cos(pi/8)
+  constexpr float tau = 0.41421356237309504880f;  // tan(pi/8)
+  float2 U[4][4];  // U[b][ka]: inner 4-point DFTs of x[b + 4 a]
 #pragma unroll
-    for (int b = 0; b < 4; ++b) {
-      float2 u[4] = {v[b], v[b + 4], v[b + 8], v[b + 12]};
-      Dft<4, INV>::run(u);
+  for (int b = 0; b < 4; ++b) {
+    float2 u[4] = {v[b], v[b + 4], v[b + 8], v[b + 12]};
+    Dft<4, INV>::run(u);
 #pragma unroll
-      for (int k = 0; k < 4; ++k) U[b][k] = u[k];
-    }
-    {  // ka = 0: no twiddles
-      float2 z[4] = {U[0][0], U[1][0], U[2][0], U[3][0]};
-      Dft<4, INV>::run(z);
-      v[0] = z[0]; v[4] = z[1]; v[8] = z[2]; v[12] = z[3];
-    }
-    {  // ka = 1: z1 = C q1, z2 = h p2, z3 = C q3
-      const float2 u1 = U[1][1], u2 = U[2][1], u3 = U[3][1];
-      const float2 q1 = make_float2(fmaf(-s * tau, u1.y, u1.x), fmaf(s * tau, u1.x, u1.y));  // u1 (1 + s i tau)
-      const float2 p2 = make_float2(u2.x - s * u2.y, u2.y + s * u2.x);                        // u2 (1 + s i)
-      const float2 q3 = make_float2(fmaf(tau, u3.x, -s * u3.y), fmaf(tau, u3.y, s * u3.x));  // u3 (tau + s i)
-      dft16_outer<INV>(U[0][1], p2, q1, q3, h, C, v[1], v[5], v[9], v[13]);
-    }
-    {  // ka = 2: z1 = h p1, z2 = s i u2, z3 = h p3 (the common scale h goes with z1, z3)
-      const float2 u1 = U[1][2], u2 = U[2][2], u3 = U[3][2];
-      const float2 p1 = make_float2(u1.x - s * u1.y, u1.y + s * u1.x);   // u1 (1 + s i)
-      const float2 z2 = make_float2(-s * u2.y, s * u2.x);                // s i u2
-      const float2 p3 = make_float2(-u3.x - s * u3.y, s * u3.x - u3.y);  // u3 (-1 + s i)
-      dft16_outer<INV>(U[0][2], z2, p1, p3, 1.f, h, v[2], v[6], v[10], v[14]);
-    }
-    {  // ka = 3: z1 = C q1, z2 = h p2, z3 = C q3
-      const float2 u1 = U[1][3], u2 = U[2][3], u3 = U[3][3];
-      const float2 q1 = make_float2(fmaf(tau, u1.x, -s * u1.y), fmaf(tau, u1.y, s * u1.x));    // u1 (tau + s i)
-      const float2 p2 = make_float2(-u2.x - s * u2.y, s * u2.x - u2.y);                         // u2 (-1 + s i)
-      const float2 q3 = make_float2(fmaf(s * tau, u3.y, -u3.x), fmaf(-s * tau, u3.x, -u3.y));  // -u3 (1 + s i tau)
-      dft16_outer<INV>(U[0][3], p2, q1, q3, h, C, v[3], v[7], v[11], v[15]);
-    }
+    for (int k = 0; k < 4; ++k) U[b][k] = u[k];
   }
+  const float hodd = h * odd, codd = C * odd;
+  // ka = 0: no twiddles
+  dft16_outer<INV>(U[0][0], U[2][0], U[1][0], U[3][0], 1.f, odd, v[0], v[4], v[8], v[12]);
+  {  // ka = 1: z1 = C q1, z2 = h p2, z3 = C q3
+    const float2 u1 = U[1][1], u2 = U[2][1], u3 = U[3][1];
+    const float2 q1 = make_float2(fmaf(-s * tau, u1.y, u1.x), fmaf(s * tau, u1.x, u1.y));  // u1 (1 + s i tau)
+    const float2 p2 = make_float2(u2.x - s * u2.y, u2.y + s * u2.x);                        // u2 (1 + s i)
+    const float2 q3 = make_float2(fmaf(tau, u3.x, -s * u3.y), fmaf(tau, u3.y, s * u3.x));  // u3 (tau + s i)
+    dft16_outer<INV>(U[0][1], p2, q1, q3, h, codd, v[1], v[5], v[9], v[13]);
+  }
+  {  // ka = 2: z1 = h p1, z2 = s i u2, z3 = h p3 (the common scale h goes with z1, z3)
+    const float2 u1 = U[1][2], u2 = U[2][2], u3 = U[3][2];
+    const float2 p1 = make_float2(u1.x - s * u1.y, u1.y + s * u1.x);   // u1 (1 + s i)
+    const float2 z2 = make_float2(-s * u2.y, s * u2.x);                // s i u2
+    const float2 p3 = make_float2(-u3.x - s * u3.y, s * u3.x - u3.y);  // u3 (-1 + s i)
+    dft16_outer<INV>(U[0][2], z2, p1, p3, 1.f, hodd, v[2], v[6], v[10], v[14]);
+  }
+  {  // ka = 3: z1 = C q1, z2 = h p2, z3 = C q3
+    const float2 u1 = U[1][3], u2 = U[2][3], u3 = U[3][3];
+    const float2 q1 = make_float2(fmaf(tau, u1.x, -s * u1.y), fmaf(tau, u1.y, s * u1.x));    // u1 (tau + s i)
+    const float2 p2 = make_float2(-u2.x - s * u2.y, s * u2.x - u2.y);                         // u2 (-1 + s i)
+    const float2 q3 = make_float2(fmaf(s * tau, u3.y, -u3.x), fmaf(-s * tau, u3.x, -u3.y));  // -u3 (1 + s i tau)
+    dft16_outer<INV>(U[0][3], p2, q1, q3, h, codd, v[3], v[7], v[11], v[15]);
+  }
+}
+template <bool INV> struct Dft<16, INV> {
+  static __host__ __device__ __forceinline__ void run(float2 (&v)[16]) { dft16<INV>(v, 1.f); }
 };
 template <bool INV> struct Dft<24, INV> {
   static __host__ __device__ __forceinline__ void run(float2 (&v)[24]) { dft_ct<8, 3, INV>(v); }
@@ -466,23 +468,31 @@ struct PairedFFT512 {
     float2* base;
     __host__ __device__ __forceinline__ float2& operator[](int i) const { return base[i ^ ((i >> 5) & 15)]; }
   };
-  // first radix-16 stage of thread t (upper lane: h = t >= 16)
+  // first radix-16 stage of thread t (upper lane: h = t >= 16, odd inputs negated)
   template <bool INV>
   static __host__ __device__ __forceinline__ void first(float2 (&v)[E], bool h) {
-    const float sg = h ? -1.f : 1.f;
-#pragma unroll
-    for (int r = 1; r < 16; r += 2) v[r] = cscale(v[r], sg);
-    Dft<16, INV>::run(v);
+    dft16<INV>(v, h ? -1.f : 1.f);
   }
-  // radix-2 butterfly I (< 8) of this lane; `recv` is the partner's register 8 + I
+  // radix-2 butterfly I (< 8) of this lane; `recv` is the partner's register 8 + I.
+  // W_32^I = (c, s sn) is applied as a scale times (1 + i s t) or (t + i s)
+  // with t <= 1, the scale going into the butterfly's FMAs.
   template <bool INV, int I>
   static __host__ __device__ __forceinline__ void pair(float2 (&v)[E], float2 recv, bool h) {
+    constexpr float s = INV ? 1.f : -1.f;
+    constexpr double cw = ce_trig2pi(I, 32, false), sw = ce_trig2pi(I, 32, true);
+    constexpr bool by_cos = cw >= sw;
+    constexpr float scale = (float)(by_cos ? cw : sw);
+    constexpr float t = (float)(by_cos ? sw / cw : cw / sw);
     const float2 a = h ? recv : v[I];
-    float2 b = twc<32, I, INV>(h ? v[I] : recv);
-    const float2 b8 = twc<4, 1, INV>(b);  // the upper lane's butterfly is I + 8: one more W_32^8
-    b = h ? b8 : b;
-    v[I] = cadd(a, b);
-    v[8 + I] = csub(a, b);
+    const float2 b = h ? v[I] : recv;
+    float2 q;
+    if constexpr (I == 0) q = b;
+    else if constexpr (by_cos) q = make_float2(fmaf(-s * t, b.y, b.x), fmaf(s * t, b.x, b.y));  // b (1 + i s t)
+    else q = make_float2(fmaf(t, b.x, -s * b.y), fmaf(t, b.y, s * b.x));                         // b (t + i s)
+    const float2 q8 = make_float2(-s * q.y, s * q.x);  // the upper lane's butterfly is I + 8: times W_32^8 = s i
+    q = h ? q8 : q;
+    v[I] = make_float2(fmaf(scale, q.x, a.x), fmaf(scale, q.y, a.y));
+    v[8 + I] = make_float2(fmaf(-scale, q.x, a.x), fmaf(-scale, q.y, a.y));
   }
   // line position of register m of thread t after the radix-2 stage
   static __host__ __device__ __forceinline__ int pos(int m, int t) {
