@@ -584,6 +584,8 @@ int msx_plan_check(msx_plan* p) {
   MSX_CUDA(cudaMemcpy(&h, p->err, sizeof(int), cudaMemcpyDeviceToHost), "reading the plan error word");
   if (h) {
     MSX_CUDA(cudaMemset(p->err, 0, sizeof(int)), "clearing the plan error word");
+    if (h & 2)  // bit 1: the paired row pass found its shared memory misaligned and did nothing
+      return fail(MSX_ERR_CUDA, "the paired row pass found its shared memory misaligned (error word 0x%x)", h);
     return fail(MSX_ERR_TIMEOUT, "a pipelined pass gave up waiting for its tile copy (error word 0x%x)", h);
   }
   return MSX_OK;

@@ -460,6 +460,15 @@ struct LineFFT<N, T, Radices<Rs...>> {
 // store of one register by a half warp covers 32 t' + c for sixteen t' and one
 // c < 32, a load 32 m + t for sixteen consecutive t.  One exchange through
 // shared memory per transform instead of two.
+__device__ __forceinline__ void sts64(unsigned addr, float2 v) {
+  asm volatile("st.shared.v2.f32 [%0], {%1, %2};" ::"r"(addr), "f"(v.x), "f"(v.y) : "memory");
+}
+__device__ __forceinline__ float2 lds64(unsigned addr) {
+  float2 v;
+  asm volatile("ld.shared.v2.f32 {%0, %1}, [%2];" : "=f"(v.x), "=f"(v.y) : "r"(addr) : "memory");
+  return v;
+}
+
 struct PairedFFT512 {
   static constexpr int N = 512, T = 32, E = 16;
   using Base = LineFFT<512, 32, Radices<16, 2, 16>>;
@@ -498,26 +507,40 @@ struct PairedFFT512 {
   static __host__ __device__ __forceinline__ int pos(int m, int t) {
     return 32 * (t & 15) + 8 * (t >> 4) + m + (m >= 8 ? 8 : 0);
   }
+  // The same exchange as byte offsets in a 256-byte-aligned line, in a form
+  // with one logic operation per access: the store of register m is
+  // st_base(t) ^ 8 c_m (c_m = m + 8 [m >= 8]) and the load of element
+  // t + 32 m is ((8 t) ^ (8 m)) + 256 m, both equal to 8 Line-index.
+  static __host__ __device__ __forceinline__ unsigned st_base(int t) {
+    return 256u * (t & 15) + 8u * ((8 * (t >> 4)) ^ (t & 15));
+  }
+  static __host__ __device__ __forceinline__ unsigned st_off(int m, int t) {
+    return st_base(t) ^ (8u * (m + (m >= 8 ? 8 : 0)));
+  }
+  static __host__ __device__ __forceinline__ unsigned ld_off(int m, int t) {
+    return ((8u * t) ^ (8u * m)) + 256u * m;
+  }
   template <bool INV, int... Is>
   static __device__ __forceinline__ void pairs(float2 (&v)[E], bool h, std::integer_sequence<int, Is...>) {
     (pair<INV, Is>(v, make_float2(__shfl_xor_sync(0xffffffffu, v[8 + Is].x, 16),
                                   __shfl_xor_sync(0xffffffffu, v[8 + Is].y, 16)), h), ...);
   }
   // In-place transform of the line held by the warp (unnormalised); `line` is
-  // the warp's 512-word exchange buffer, whose earlier readers must be this
-  // warp's own threads.
+  // the shared-memory address of the warp's 512-word exchange buffer, 256-byte
+  // aligned, whose earlier readers must be this warp's own threads.
   template <bool INV>
-  static __device__ __forceinline__ void run(float2 (&v)[E], float2* line, const float2* tw, int t) {
+  static __device__ __forceinline__ void run(float2 (&v)[E], unsigned line, const float2* tw, int t) {
     const bool h = t >= 16;
     first<INV>(v, h);
     pairs<INV>(v, h, std::make_integer_sequence<int, 8>{});
-    const Line buf{line};
     __syncwarp();  // earlier reads of the buffer are done
+    const unsigned q = line + st_base(t);
 #pragma unroll
-    for (int m = 0; m < E; ++m) buf[pos(m, t)] = v[m];
+    for (int m = 0; m < E; ++m) sts64(q ^ (8u * (m + (m >= 8 ? 8 : 0))), v[m]);
     __syncwarp();
+    const unsigned r = line + 8u * t;
 #pragma unroll
-    for (int m = 0; m < E; ++m) v[m] = buf[t + T * m];
+    for (int m = 0; m < E; ++m) v[m] = lds64((r ^ (8u * m)) + 256u * m);
     float2 out[E];
     Base::template butterflies<16, 32, kStage2Tw, INV>(v, out, tw, t);
 #pragma unroll

@@ -88,7 +88,7 @@ struct TmaPassArgs {
   const float2* tw;       // twiddles of the line schedule
   const float2* pyx;      // py[Ny] then px[Nx] (column pass)
   const int2* band;       // [lo, hi] ky band per column (column pass)
-  int* err;               // bit 0: a bounded wait gave up
+  int* err;               // bit 0: a bounded wait gave up; bit 1: misaligned shared memory
   int G, Ny, Nx;
   // columns [x_lo, x_hi) written by the row pass and processed by the column
   // pass (x_hi == 0: all); the columns outside hold zeros that stay zero
@@ -133,6 +133,12 @@ __global__ void __launch_bounds__(S::THREADS, S::MINB) row_pass_tma_kernel(TmaPa
   uint64_t* full = reinterpret_cast<uint64_t*>(tw + S::TW_PAD);
   uint64_t* empty = full + NS;
   const int tid = threadIdx.x;
+  if constexpr (S::PAIRED) {  // the paired exchange addresses need 256-byte-aligned lines
+    if (smem_u32(smem) & 255u) {
+      if (tid == 0) atomicOr(a.err, 2);
+      return;
+    }
+  }
   for (int i = tid; i < S::TW; i += blockDim.x) tw[i] = a.tw[i];
   if (tid == 0) {
     for (int s = 0; s < NS; ++s) {
@@ -193,10 +199,11 @@ __global__ void __launch_bounds__(S::THREADS, S::MINB) row_pass_tma_kernel(TmaPa
 #pragma unroll
     for (int m = 0; m < E; ++m) v[m] = line[t + T * m];
     if constexpr (S::PAIRED) {
-      PairedFFT512::run<true>(v, line, tw, t);
+      const unsigned la = smem_u32(line);
+      PairedFFT512::run<true>(v, la, tw, t);
 #pragma unroll
       for (int m = 0; m < E; ++m) v[m] = cmul(v[m], trow[t + T * m]);
-      PairedFFT512::run<false>(v, line, tw, t);
+      PairedFFT512::run<false>(v, la, tw, t);
     } else {
       SwizzledLine<ilog2(E)> buf{line};
       S::FFT::template run<true, false>(v, buf, tw, t);

@@ -56,6 +56,17 @@ bool paired_banks_ok() {
         st[bs] = ld[bl] = true;
       }
     }
+  // the byte-offset forms of the device code: for a 256-byte-aligned line L,
+  // (L + st_base(t)) ^ 8 c_m and ((L + 8 t) ^ 8 m) + 256 m address the same
+  // words as the swizzled indices
+  for (unsigned L : {0u, 256u, 0x9100u, 0x2a700u})
+    for (int t = 0; t < 32; ++t)
+      for (int m = 0; m < 16; ++m) {
+        const unsigned cm = 8u * (m + (m >= 8 ? 8 : 0));
+        if (P::st_off(m, t) != 8u * sw(P::pos(m, t)) || P::ld_off(m, t) != 8u * sw(t + 32 * m)) return false;
+        if (((L + P::st_base(t)) ^ cm) != L + P::st_off(m, t)) return false;
+        if ((((L + 8u * t) ^ (8u * m)) + 256u * m) != L + P::ld_off(m, t)) return false;
+      }
   // every position is written exactly once
   bool hit[512] = {};
   for (int t = 0; t < 32; ++t)
