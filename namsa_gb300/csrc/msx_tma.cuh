@@ -4,8 +4,9 @@
 // wave).  While it transforms tile i out of one shared-memory stage, the bulk
 // copy engine (cp.async.bulk for rows, cp.async.bulk.tensor for column tiles)
 // fills the next stage(s) with the following tiles; one mbarrier per stage
-// tracks the bytes in flight.  Results go straight from registers to global
-// memory.
+// tracks the bytes in flight.  Row results go straight from registers to
+// global memory; column results go back into their stage and out by a tiled
+// bulk store.
 //
 // The row pass exchanges Stockham stages in place inside the staged rows, with
 // an XOR swizzle of the element index (bits [S, S+4) folded into bits [0, 4))
@@ -70,6 +71,20 @@ __device__ __forceinline__ void tma2d_g2s(void* dst, const CUtensorMap* map, int
       "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(smem_u32(bar))
       : "memory");
 }
+
+// Tiled bulk store of a shared-memory box to the tensor; completion is tracked
+// by bulk groups of the issuing thread.
+__device__ __forceinline__ void tma2d_s2g(const CUtensorMap* map, int x, int y, const void* src) {
+  asm volatile("cp.async.bulk.tensor.2d.global.shared::cta.bulk_group [%0, {%1, %2}], [%3];" ::"l"(
+                   reinterpret_cast<uint64_t>(map)),
+               "r"(x), "r"(y), "r"(smem_u32(src))
+               : "memory");
+}
+__device__ __forceinline__ void bulk_commit() { asm volatile("cp.async.bulk.commit_group;" ::: "memory"); }
+// the issuing thread's bulk stores have read their shared memory
+__device__ __forceinline__ void bulk_wait_read_all() { asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory"); }
+// the issuing thread's bulk stores are complete
+__device__ __forceinline__ void bulk_wait_all() { asm volatile("cp.async.bulk.wait_group 0;" ::: "memory"); }
 
 // Row line inside a staged, densely packed row: element i lives at
 // i ^ ((i >> SH) & 15).  SH = log2(elements per thread) makes the first
@@ -244,8 +259,13 @@ __global__ void __launch_bounds__(S::THREADS, S::MINB) row_pass_tma_kernel(TmaPa
 // Where a third tile-sized buffer does not fit beside the two stages without
 // costing occupancy, both transforms exchange in the stage and each scatter is
 // preceded by a barrier as well.
-// Thread 0 refills the previous tile's stage with tile k+1 right after #0
-// (that stage was last written by generic stores, fenced before #0).
+// Results: every thread writes its outputs back into the tile's stage, at the
+// words its own final gather read (so no barrier is needed before), and fences
+// them for the async proxy; after the next tile's #0, thread 0 issues the
+// tiled bulk store of the tile.  Thread 0 refills that stage with tile k+1
+// after the forward transform of tile k (past #1), once the store has read
+// the stage; after the last tile the CTA synchronises, stores it and waits
+// for the store to complete.
 template <class S>
 struct ColTma {
   static constexpr int NY = S::N;
@@ -288,15 +308,42 @@ __global__ void __launch_bounds__(S::THREADS, S::MINB) col_mid_tma_kernel(const 
   const int tiles_x = (a.x_hi > 0 ? a.x_hi : a.Nx) / C - xt0;
   const int ntiles = tiles_x * a.G;
   const int mine = (int)blockIdx.x < ntiles ? (ntiles - 1 - (int)blockIdx.x) / (int)gridDim.x + 1 : 0;
+  // Tile order: the tiles xt = 2j and 2j + 1 of one wave share the 256-byte L2
+  // fills of the tensor map, so they are taken one after the other (by
+  // neighbouring CTAs); a tile whose partner lies outside the range (at most
+  // one at each end) is ordered on its own.
+  const int lead = xt0 & 1, npairs = (tiles_x - lead) >> 1;
+  auto coords = [&](int u, int& p, int& xt) {
+    const int G = a.G;
+    if (u < lead * G) {
+      p = u; xt = xt0;
+      return;
+    }
+    u -= lead * G;
+    if (u < npairs * 2 * G) {
+      const int q = u / (2 * G), r = u - q * 2 * G;
+      p = r >> 1; xt = xt0 + lead + 2 * q + (r & 1);
+      return;
+    }
+    p = u - npairs * 2 * G; xt = xt0 + tiles_x - 1;
+  };
 
   auto load = [&](int k) {  // this CTA's k-th tile into stage k & 1
-    const int tile = blockIdx.x + k * gridDim.x;
-    const int p = tile % a.G, xt = xt0 + tile / a.G;
+    int p, xt;
+    coords(blockIdx.x + k * gridDim.x, p, xt);
     float2* dst = stage + (k & 1) * STAGE;
     uint64_t* bar = &full[k & 1];
     mbar_expect_tx(bar, (uint32_t)(STAGE * sizeof(float2)));
 #pragma unroll
     for (int b = 0; b < NBOX; ++b) tma2d_g2s(dst + b * BOXR * C, &map, xt * C, p * NY + b * BOXR, bar);
+  };
+  auto store = [&](int k) {  // the k-th tile's results, staged in stage k & 1, back to the workspace
+    int p, xt;
+    coords(blockIdx.x + k * gridDim.x, p, xt);
+    const float2* src = stage + (k & 1) * STAGE;
+#pragma unroll
+    for (int b = 0; b < NBOX; ++b) tma2d_s2g(&map, xt * C, p * NY + b * BOXR, src + b * BOXR * C);
+    bulk_commit();
   };
 
   const int c = tid % C, t = tid / C;
@@ -304,7 +351,11 @@ __global__ void __launch_bounds__(S::THREADS, S::MINB) col_mid_tma_kernel(const 
   if (tid == 0)
     for (; loaded < 2 && loaded < mine; ++loaded) load(loaded);
   // this column's propagator factor and mask band, fetched one tile ahead
-  auto column_of = [&](int k) { return (xt0 + (int)(blockIdx.x + k * gridDim.x) / a.G) * C + c; };
+  auto column_of = [&](int k) {
+    int p, xt;
+    coords(blockIdx.x + k * gridDim.x, p, xt);
+    return xt * C + c;
+  };
   float2 px_next = make_float2(0.f, 0.f);
   int2 bd_next = make_int2(1, 0);
   if (mine > 0) {
@@ -313,9 +364,6 @@ __global__ void __launch_bounds__(S::THREADS, S::MINB) col_mid_tma_kernel(const 
   }
   for (int k = 0; k < mine; ++k) {
     const int s = k & 1;
-    const int tile = blockIdx.x + k * gridDim.x;
-    const int p = tile % a.G, xt = xt0 + tile / a.G;
-    const int x = xt * C + c;
     const float2 px = px_next;
     const int2 bd = bd_next;
     if (k + 1 < mine) {
@@ -326,11 +374,12 @@ __global__ void __launch_bounds__(S::THREADS, S::MINB) col_mid_tma_kernel(const 
     if (!__syncthreads_and(ok)) {  // #0
       if (tid == 0) {
         atomicOr(a.err, 1);
+        bulk_wait_all();  // stores in flight read the stages
         for (int j = k; j < loaded; ++j) mbar_wait_bounded(&full[j & 1], (j >> 1) & 1);
       }
       return;
     }
-    if (tid == 0 && k >= 1 && loaded < mine) load(loaded++);  // tile k+1 into the stage of tile k-1
+    if (tid == 0 && k >= 1) store(k - 1);  // written back into its stage and fenced before #0
     float2* st = stage + s * STAGE;
     InterleavedLine<C> in{st + c};
     float2 v[E];
@@ -344,6 +393,10 @@ __global__ void __launch_bounds__(S::THREADS, S::MINB) col_mid_tma_kernel(const 
       S::FFT::template run_alt<false, true, 0>(v, scr, in, tw, t);  // #1 (and one per further exchange)
     else
       S::FFT::template run<false, true, InterleavedLine<C>, true>(v, in, tw, t);
+    if (tid == 0 && k >= 1 && loaded < mine) {  // tile k+1 into the stage of tile k-1, once its store has read it
+      bulk_wait_read_all();
+      load(loaded++);
+    }
 #pragma unroll
     for (int m = 0; m < E; ++m) {
       const int ky = t + T * m;
@@ -354,10 +407,16 @@ __global__ void __launch_bounds__(S::THREADS, S::MINB) col_mid_tma_kernel(const 
       S::FFT::template run_alt<true, true, NXCH % 2>(v, scr, in, tw, t);  // #2 ...
     else
       S::FFT::template run<true, true, InterleavedLine<C>, true>(v, in, tw, t);
-    float2* col = a.psi + (size_t)p * NY * a.Nx + x;
+    // results back into the stage, at the words this thread read last (the final
+    // gather is from the stage), for the bulk store issued after the next #0
 #pragma unroll
-    for (int m = 0; m < E; ++m) col[(t + T * m) * a.Nx] = v[m];
-    fence_proxy_async();  // the inverse exchange wrote the stage that the copy engine refills next
+    for (int m = 0; m < E; ++m) in[t + T * m] = v[m];
+    fence_proxy_async();  // these writes precede the bulk store and the refill of the stage
+  }
+  __syncthreads();
+  if (tid == 0 && mine > 0) {
+    store(mine - 1);
+    bulk_wait_all();
   }
 }
 
