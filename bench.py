@@ -46,7 +46,7 @@ WORKLOAD = 'Si[001] 8x8x50 cells, 512x512 c64, 199 slices (t=a/4), 200 keV, 30 m
 NCU_TRAFFIC = {
     ('row', 512, 5, 512): 1.076697e9 + 0.684955e9,   # row_pass_tma_kernel t32_r16x2x16
     ('row', 512, 6, 512): 1.076570e9 + 0.684825e9,   # row_pass_tma_kernel t32_r16x2x16_pair
-    ('col', 512, 0, 512): 0.848855e9 + 0.682400e9,   # col_mid_tma_kernel t16_r32x16
+    ('col', 512, 0, 512): 0.771863e9 + 0.682320e9,   # col_mid_tma_kernel t16_r32x16
 }
 
 
