@@ -266,6 +266,26 @@ __global__ void __launch_bounds__(S::THREADS, S::MINB) row_pass_tma_kernel(TmaPa
 // after the forward transform of tile k (past #1), once the store has read
 // the stage; after the last tile the CTA synchronises, stores it and waits
 // for the store to complete.
+// Order of a column pass's tiles: tile u of G waves x tiles_x column tiles
+// starting at xt0 -> (wave p, column tile xt).  The tiles xt = 2j and 2j + 1 of
+// one wave share the tensor map's 256-byte L2 fills, so they are taken one
+// after the other (by neighbouring CTAs); a tile whose partner lies outside the
+// range (at most one at each end) is ordered on its own.
+__host__ __device__ __forceinline__ void col_tile_order(int u, int G, int xt0, int tiles_x, int& p, int& xt) {
+  const int lead = xt0 & 1, npairs = (tiles_x - lead) >> 1;
+  if (u < lead * G) {
+    p = u; xt = xt0;
+    return;
+  }
+  u -= lead * G;
+  if (u < npairs * 2 * G) {
+    const int q = u / (2 * G), r = u - q * 2 * G;
+    p = r >> 1; xt = xt0 + lead + 2 * q + (r & 1);
+    return;
+  }
+  p = u - npairs * 2 * G; xt = xt0 + tiles_x - 1;
+}
+
 template <class S>
 struct ColTma {
   static constexpr int NY = S::N;
@@ -308,25 +328,7 @@ __global__ void __launch_bounds__(S::THREADS, S::MINB) col_mid_tma_kernel(const 
   const int tiles_x = (a.x_hi > 0 ? a.x_hi : a.Nx) / C - xt0;
   const int ntiles = tiles_x * a.G;
   const int mine = (int)blockIdx.x < ntiles ? (ntiles - 1 - (int)blockIdx.x) / (int)gridDim.x + 1 : 0;
-  // Tile order: the tiles xt = 2j and 2j + 1 of one wave share the 256-byte L2
-  // fills of the tensor map, so they are taken one after the other (by
-  // neighbouring CTAs); a tile whose partner lies outside the range (at most
-  // one at each end) is ordered on its own.
-  const int lead = xt0 & 1, npairs = (tiles_x - lead) >> 1;
-  auto coords = [&](int u, int& p, int& xt) {
-    const int G = a.G;
-    if (u < lead * G) {
-      p = u; xt = xt0;
-      return;
-    }
-    u -= lead * G;
-    if (u < npairs * 2 * G) {
-      const int q = u / (2 * G), r = u - q * 2 * G;
-      p = r >> 1; xt = xt0 + lead + 2 * q + (r & 1);
-      return;
-    }
-    p = u - npairs * 2 * G; xt = xt0 + tiles_x - 1;
-  };
+  auto coords = [&](int u, int& p, int& xt) { col_tile_order(u, a.G, xt0, tiles_x, p, xt); };
 
   auto load = [&](int k) {  // this CTA's k-th tile into stage k & 1
     int p, xt;

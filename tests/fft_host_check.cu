@@ -4,6 +4,7 @@
 // evaluated in double precision.  Prints one line per schedule and exits
 // non-zero when a relative L2 error exceeds 5e-7.
 #include "msx_fft.cuh"
+#include "msx_tma.cuh"
 #include <cstdio>
 #include <cmath>
 #include <vector>
@@ -76,8 +77,34 @@ bool paired_banks_ok() {
     }
   return true;
 }
+// The column pass's tile order visits every (wave, column tile) of the range
+// exactly once, and the two tiles of each aligned pair inside the range
+// consecutively.
+bool col_tile_order_ok() {
+  for (int G : {1, 2, 3, 7, 64})
+    for (int xt0 = 0; xt0 < 9; ++xt0)
+      for (int tx = 1; tx < 14; ++tx) {
+        std::vector<char> seen(G * tx, 0);
+        int prev_p = -1, prev_xt = -1;
+        for (int u = 0; u < G * tx; ++u) {
+          int p = -1, xt = -1;
+          col_tile_order(u, G, xt0, tx, p, xt);
+          if (p < 0 || p >= G || xt < xt0 || xt >= xt0 + tx) return false;
+          char& s = seen[p * tx + (xt - xt0)];
+          if (s) return false;
+          s = 1;
+          // an odd tile whose even partner is in the range follows it directly
+          if ((xt & 1) && xt - 1 >= xt0 && (prev_p != p || prev_xt != xt - 1)) return false;
+          prev_p = p; prev_xt = xt;
+        }
+      }
+  return true;
+}
 int main() {
   double w = 0;
+  const bool order = col_tile_order_ok();
+  printf("column tile order: %s\n", order ? "yes" : "NO");
+  if (!order) return 1;
   const bool banks = paired_banks_ok();
   printf("paired exchange conflict-free: %s\n", banks ? "yes" : "NO");
   if (!banks) return 1;
