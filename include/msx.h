@@ -156,9 +156,10 @@ MSX_API int msx_plan_get_schedule(const msx_plan* plan, int* row_schedule, int* 
 MSX_API int msx_plan_set_tma(msx_plan* plan, int enable);
 
 /* Synchronises the device and reports whether a pipelined pass of this plan
- * gave up on a bounded wait since the last check (MSX_ERR_TIMEOUT; the error
- * word is then cleared).  Kernels never trap: a stuck copy makes the pass
- * return early and flag the plan instead. */
+ * gave up on a bounded wait since the last check (MSX_ERR_TIMEOUT), or found
+ * its shared memory misaligned for the paired row transform and did nothing
+ * (MSX_ERR_CUDA); the error word is then cleared.  Kernels never trap: a
+ * stuck copy makes the pass return early and flag the plan instead. */
 MSX_API int msx_plan_check(msx_plan* plan);
 
 /* 1 = record the launch sequence of msx_multislice in a CUDA graph and
