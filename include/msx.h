@@ -199,7 +199,10 @@ MSX_API int msx_multislice(msx_plan* plan, const float* trans_dev, int num_slice
  * the next group computes.  Stream-ordered like msx_multislice: `stream` waits
  * for the last download, so the host buffers must stay valid until then; they
  * should be page-locked for the copies to overlap.  The plan holds the device
- * copies of the inputs and of the CBED stack.
+ * copies of the inputs and of the CBED stack.  With page-locked buffers (and
+ * graphs enabled) the call is recorded as one CUDA graph and replayed while
+ * the arguments, buffer addresses included, repeat; the copies read and write
+ * the host buffers' contents at each replay.
  */
 MSX_API int msx_multislice_host(msx_plan* plan, const float* trans_host, int num_slices, const float* psi_k_host,
                                 double normalization, const float* positions_host, int num_probes, float kmax,

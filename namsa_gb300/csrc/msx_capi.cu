@@ -96,6 +96,8 @@ struct msx_plan {
   bool use_graph = true;
   cudaGraphExec_t gexec = nullptr;
   std::vector<unsigned char> gkey;
+  cudaGraphExec_t gexec_host = nullptr;  // msx_multislice_host, page-locked buffers
+  std::vector<unsigned char> gkey_host;
   // persistent TMA-pipelined passes
   bool use_tma = true;
   int* err = nullptr;            // device error word of the bounded waits
@@ -198,6 +200,9 @@ void drop_graph(msx_plan* p) {
   if (p->gexec) cudaGraphExecDestroy(p->gexec);
   p->gexec = nullptr;
   p->gkey.clear();
+  if (p->gexec_host) cudaGraphExecDestroy(p->gexec_host);
+  p->gexec_host = nullptr;
+  p->gkey_host.clear();
 }
 
 int auto_group(int ny, int nx) {
@@ -782,9 +787,52 @@ int msx_multislice_host(msx_plan* p, const float* trans_host, int num_slices, co
   if (rc != MSX_OK) return rc;
 
   cudaStream_t caller = (cudaStream_t)stream, w = p->work, cp = p->copy;
+  // The whole call is captured into a CUDA graph and replayed while its
+  // arguments (host and device buffers included) repeat, when every host buffer
+  // is page-locked: copies from pageable memory stay outside graphs.
+  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+  MSX_CUDA(cudaStreamIsCapturing(caller, &cap), "cudaStreamIsCapturing");
+  auto locked = [](const void* q) {
+    cudaPointerAttributes at{};
+    if (cudaPointerGetAttributes(&at, q) != cudaSuccess) {
+      cudaGetLastError();
+      return false;
+    }
+    return at.type == cudaMemoryTypeHost;
+  };
+  const bool graph = p->use_graph && cap == cudaStreamCaptureStatusNone && locked(psi_k_host) &&
+                     locked(positions_host) && locked(cbed_host) && (num_slices == 0 || locked(trans_host));
+  struct HostKey {
+    const void *trans, *psik, *pos, *cbed, *d_trans, *d_psik, *d_pos, *d_norm, *d_cbed;
+    double normalization, lambda, slice_t;
+    float kmax, k_band;
+    int num_slices, num_probes, crop_y, crop_x, group, row_sched, col_sched, tma;
+  } hk;
+  std::memset(&hk, 0, sizeof(hk));  // the struct is the cache key: no stray padding bytes
+  hk.trans = trans_host; hk.psik = psi_k_host; hk.pos = positions_host; hk.cbed = cbed_host;
+  hk.d_trans = p->io_trans; hk.d_psik = p->io_psik; hk.d_pos = p->io_pos; hk.d_norm = p->io_norm;
+  hk.d_cbed = p->io_cbed; hk.normalization = normalization; hk.lambda = lambda; hk.slice_t = slice_t;
+  hk.kmax = kmax; hk.k_band = k_band; hk.num_slices = num_slices; hk.num_probes = num_probes; hk.crop_y = crop_y;
+  hk.crop_x = crop_x; hk.group = p->group; hk.row_sched = p->row_sched; hk.col_sched = p->col_sched;
+  hk.tma = p->use_tma ? 1 : 0;
+  std::vector<unsigned char> key(sizeof(hk));
+  std::memcpy(key.data(), &hk, sizeof(hk));
   // everything here follows the caller's earlier work and this plan's earlier calls
   MSX_CUDA(cudaEventRecord(p->ev_in, caller), "cudaEventRecord");
   MSX_CUDA(cudaStreamWaitEvent(w, p->ev_in, 0), "cudaStreamWaitEvent");
+  if (graph && p->gexec_host && key == p->gkey_host) {
+    MSX_CUDA(cudaGraphLaunch(p->gexec_host, w), "cudaGraphLaunch");
+    MSX_CUDA(cudaEventRecord(p->ev_out, w), "cudaEventRecord");
+    MSX_CUDA(cudaStreamWaitEvent(caller, p->ev_out, 0), "cudaStreamWaitEvent");
+    return MSX_OK;
+  }
+  if (graph) {
+    if (p->gexec_host) cudaGraphExecDestroy(p->gexec_host);
+    p->gexec_host = nullptr;
+    p->gkey_host.clear();
+    MSX_CUDA(cudaStreamBeginCapture(w, cudaStreamCaptureModeThreadLocal), "cudaStreamBeginCapture");
+  }
+  // the copy stream forks from the work stream (joining the capture, if any)
   MSX_CUDA(cudaEventRecord(p->ev_out, w), "cudaEventRecord");
   MSX_CUDA(cudaStreamWaitEvent(cp, p->ev_out, 0), "cudaStreamWaitEvent");
 
@@ -825,13 +873,36 @@ int msx_multislice_host(msx_plan* p, const float* trans_host, int num_slices, co
     HostPipe hp{cp, chunk, &chunk_ev, &group_ev, cbed_host, pattern};
     int r = enqueue_multislice(p, a, w, &hp);
     if (r != MSX_OK) return r;
+    // the copy stream joins back: the work stream (and through it the caller) waits for the downloads
     MSX_CUDA(cudaEventRecord(p->ev_copy, cp), "cudaEventRecord");
-    MSX_CUDA(cudaStreamWaitEvent(caller, p->ev_copy, 0), "cudaStreamWaitEvent");
+    MSX_CUDA(cudaStreamWaitEvent(w, p->ev_copy, 0), "cudaStreamWaitEvent");
     return MSX_OK;
   };
   rc = run();
-  release();
-  return rc;
+  if (graph) {
+    cudaGraph_t g = nullptr;
+    const cudaError_t e = cudaStreamEndCapture(w, &g);
+    release();
+    if (rc != MSX_OK) {
+      if (g) cudaGraphDestroy(g);
+      return rc;
+    }
+    if (e != cudaSuccess) return cuda_fail(e, "cudaStreamEndCapture");
+    const cudaError_t e2 = cudaGraphInstantiate(&p->gexec_host, g, 0);
+    cudaGraphDestroy(g);
+    if (e2 != cudaSuccess) {
+      p->gexec_host = nullptr;
+      return cuda_fail(e2, "cudaGraphInstantiate");
+    }
+    p->gkey_host = key;
+    MSX_CUDA(cudaGraphLaunch(p->gexec_host, w), "cudaGraphLaunch");
+  } else {
+    release();
+  }
+  if (rc != MSX_OK) return rc;
+  MSX_CUDA(cudaEventRecord(p->ev_out, w), "cudaEventRecord");
+  MSX_CUDA(cudaStreamWaitEvent(caller, p->ev_out, 0), "cudaStreamWaitEvent");
+  return MSX_OK;
 }
 
 int msx_plan_profile(msx_plan* p, const float* trans_dev, int num_slices, const float* psi_k_dev,

@@ -201,11 +201,28 @@ def test_host_buffer_multislice_matches_device_call(pinned):
                            torch.tensor([norm], dtype=torch.float64, device=DEV), torch.from_numpy(pos).to(DEV),
                            np.float32(kmax), lam, st, np.float32(kmax / 3), crop=96).cpu().numpy()
     host = (lambda a: torch.from_numpy(a).pin_memory()) if pinned else torch.from_numpy
-    got = plan.multislice_host(host(trans), host(psik), norm, host(pos), np.float32(kmax), lam, st,
-                               np.float32(kmax / 3), crop=96)
+    h_trans, h_psik, h_pos = host(trans), host(psik), host(pos)
+    got = plan.multislice_host(h_trans, h_psik, norm, h_pos, np.float32(kmax), lam, st, np.float32(kmax / 3), crop=96)
     torch.cuda.synchronize()
     plan.check()
     np.testing.assert_array_equal(got.numpy(), want)
+    # the same buffers with new contents: a repeated call (a graph replay when the
+    # buffers are page-locked) reads the host memory again
+    pos2 = (pos[::-1] + np.float32(0.37)).copy()
+    h_pos.copy_(torch.from_numpy(pos2))
+    want2 = plan.multislice(torch.from_numpy(trans).to(DEV), torch.from_numpy(psik).to(DEV),
+                            torch.tensor([norm], dtype=torch.float64, device=DEV), torch.from_numpy(pos2).to(DEV),
+                            np.float32(kmax), lam, st, np.float32(kmax / 3), crop=96).cpu().numpy()
+    out = torch.empty_like(got)
+    if pinned:
+        out = out.pin_memory()
+    for _ in range(2):
+        got2 = plan.multislice_host(h_trans, h_psik, norm, h_pos, np.float32(kmax), lam, st, np.float32(kmax / 3),
+                                    crop=96, out=out)
+        torch.cuda.synchronize()
+        plan.check()
+        np.testing.assert_array_equal(got2.numpy(), want2)
+    assert not np.array_equal(want2, want)
     plan.close()
 
 
