@@ -832,10 +832,6 @@ int msx_multislice_host(msx_plan* p, const float* trans_host, int num_slices, co
     p->gkey_host.clear();
     MSX_CUDA(cudaStreamBeginCapture(w, cudaStreamCaptureModeThreadLocal), "cudaStreamBeginCapture");
   }
-  // the copy stream forks from the work stream (joining the capture, if any)
-  MSX_CUDA(cudaEventRecord(p->ev_out, w), "cudaEventRecord");
-  MSX_CUDA(cudaStreamWaitEvent(cp, p->ev_out, 0), "cudaStreamWaitEvent");
-
   const int chunk = 8;
   const int nchunks = (num_slices + chunk - 1) / chunk;
   const int ngroups = (num_probes + p->group - 1) / p->group;
@@ -844,11 +840,16 @@ int msx_multislice_host(msx_plan* p, const float* trans_host, int num_slices, co
     for (cudaEvent_t e : chunk_ev) if (e) cudaEventDestroy(e);
     for (cudaEvent_t e : group_ev) if (e) cudaEventDestroy(e);
   };
-  for (auto& e : chunk_ev)
-    if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) { release(); return fail(MSX_ERR_CUDA, "cudaEventCreate"); }
-  for (auto& e : group_ev)
-    if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) { release(); return fail(MSX_ERR_CUDA, "cudaEventCreate"); }
+  // everything between the start and the end of a capture: any failure returns
+  // through here, so that the capture is always ended
   auto run = [&]() -> int {
+    for (auto& e : chunk_ev)
+      if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) return fail(MSX_ERR_CUDA, "cudaEventCreate");
+    for (auto& e : group_ev)
+      if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) return fail(MSX_ERR_CUDA, "cudaEventCreate");
+    // the copy stream forks from the work stream (joining the capture, if any)
+    MSX_CUDA(cudaEventRecord(p->ev_out, w), "cudaEventRecord");
+    MSX_CUDA(cudaStreamWaitEvent(cp, p->ev_out, 0), "cudaStreamWaitEvent");
     MSX_CUDA(cudaMemcpyAsync(p->io_psik, psi_k_host, sizeof(float2) * wave, cudaMemcpyHostToDevice, cp), "probe upload");
     MSX_CUDA(cudaMemcpyAsync(p->io_pos, positions_host, sizeof(float) * 2 * num_probes, cudaMemcpyHostToDevice, cp),
              "position upload");
