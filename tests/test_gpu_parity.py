@@ -129,6 +129,20 @@ def test_multislice_every_size_and_schedule(n):
             assert err.max() < 2e-5, (n, k, tma, err)
 
 
+@pytest.mark.parametrize('ny,nx,bandwidth,P', [(512, 512, 0.45, 13), (512, 512, 1.0, 13), (384, 512, 1 / 3, 9)])
+def test_paired_row_schedule(ny, nx, bandwidth, P):
+    """The paired 512 row transform (its radix-2 stage by warp shuffles, schedule
+    t32_r16x2x16_pair) against the FP64 oracle: groups that fill the last tile of 8
+    rows only in part, a wide band and no band limit, and a rectangular grid whose
+    rows are 512 long."""
+    k = engine.schedules(512).index('t32_r16x2x16_pair')
+    g, trans, psik, norm, pos, kmax, lam, st = random_case(ny, nx, S=4, P=P, seed=ny + P)
+    ref = oracle_cbed(g, trans, psik, norm, pos, st, bandwidth)
+    got = engine_cbed(trans, psik, norm, pos, kmax, lam, st, bandwidth, group=P, sched=(k, 0))
+    err = O.rel_l2(got, ref)
+    assert err.max() < 2e-5, err
+
+
 @pytest.mark.parametrize('ny,nx', [(256, 512), (384, 768), (128, 64)])
 def test_multislice_rectangular(ny, nx):
     g, trans, psik, norm, pos, kmax, lam, st = random_case(ny, nx, S=4, P=2, seed=ny + nx)
