@@ -135,9 +135,11 @@ MSX_API int msx_build_probe(int ny, int nx, float kmax, double lambda, float k_s
 
 /*
  * Multislice plan for an (ny, nx) grid.  `group` is the number of probe
- * wavefunctions kept resident per group (0 = pick by size).  Replaces the
- * per-batch cuFFT plans and allocations of MSAGPU.multislice
- * (namsa/msa.py:843-881) and plan_simulation's batching
+ * wavefunctions kept resident per group (0 = about 1 GiB of waves, 4 to 512);
+ * the workspace for it is allocated here.  The plan starts with the schedules
+ * the autotuner picks on GB300 for the grid (msx_plan_autotune refines both
+ * for given inputs).  Replaces the per-batch cuFFT plans and allocations of
+ * MSAGPU.multislice (namsa/msa.py:843-881) and plan_simulation's batching
  * (namsa/msa.py:445-461).
  */
 MSX_API int msx_plan_create(int ny, int nx, int group, msx_plan** plan);

@@ -206,14 +206,30 @@ void drop_graph(msx_plan* p) {
 }
 
 int auto_group(int ny, int nx) {
-  // Keep a group's waves (complex64) within about 48 MiB so that the row and
-  // column passes of one slice find them in L2.
+  // A resident group of about 1 GiB of waves (complex64), 4 to 512 waves: the
+  // persistent passes run faster per wave on large groups than on groups small
+  // enough to stay in L2 (tiles flow without launch tails); the plan autotuner
+  // picks the same on GB300 for every supported grid.
   const size_t wave = sizeof(float2) * (size_t)ny * nx;
-  size_t g = (48u << 20) / wave;
+  size_t g = ((size_t)1 << 30) / wave;
   if (g < 4) g = 4;
   if (g > 512) g = 512;
   return (int)g;
 }
+
+// Schedules a plan starts with: the plan autotuner's choice on GB300 (random
+// inputs, bandwidth 1/3, the groups above) -- the paired row transform for
+// rows of 512, 16-column tiles for columns of 768, the first schedule
+// elsewhere.
+int schedule_index(int n, const char* name) {
+  const SchedOps* ops = nullptr;
+  const int k = schedule_table(n, &ops);
+  for (int i = 0; i < k; ++i)
+    if (std::strcmp(ops[i].name, name) == 0) return i;
+  return 0;
+}
+int default_row_schedule(int nx) { return nx == 512 ? schedule_index(512, "t32_r16x2x16_pair") : 0; }
+int default_col_schedule(int ny) { return ny == 768 ? schedule_index(768, "t32_r8x8x12_c16") : 0; }
 
 struct MsArgs {
   const float* trans; int num_slices; const float* psik; const double* norm; const float* pos; int num_probes;
@@ -484,7 +500,8 @@ int msx_plan_create(int ny, int nx, int group, msx_plan** out) {
   p->ny = ny;
   p->nx = nx;
   p->device = device;
-  int rc = msx_plan_set_schedule(p, 0, 0, group > 0 ? group : auto_group(ny, nx));
+  int rc = msx_plan_set_schedule(p, default_row_schedule(nx), default_col_schedule(ny),
+                                 group > 0 ? group : auto_group(ny, nx));
   if (rc == MSX_OK) {
     cudaError_t e = cudaMalloc(&p->ptab, sizeof(float2) * (size_t)ny * nx);
     if (e == cudaSuccess) e = cudaMalloc(&p->pyx, sizeof(float2) * (size_t)(ny + nx));
