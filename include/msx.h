@@ -321,7 +321,7 @@ MSX_API int msx_batch_set_schedule(msx_batch* batch, int ny, int nx, int row_sch
 MSX_API int msx_batch_run(msx_batch* batch, const msx_job* jobs, int njobs, void* stream);
 /* msx_plan_autotune for every grid size of the job list, on the job of that
  * size with the most positions (`iters` slices per candidate, workspace up to
- * the batch's 512 MiB per plan); the winners become the batch's schedules.
+ * the batch's 1 GiB per plan); the winners become the batch's schedules.
  * Synchronises `stream`. */
 MSX_API int msx_batch_autotune(msx_batch* batch, const msx_job* jobs, int njobs, int iters, void* stream);
 /* msx_plan_check over every plan of the batch. */

@@ -1099,17 +1099,21 @@ msx_plan* batch_plan(msx_batch* b, int branch, int ny, int nx, int* rc) {
   const long long key = ((long long)ny << 32) | (unsigned)nx;
   for (auto& kv : b->plans[branch])
     if (kv.first == key) return kv.second;
-  // Persistent passes amortise their start-up over large groups: up to 512 MiB
+  // Persistent passes amortise their start-up over large groups: up to 1 GiB
   // of waves per branch (the jobs of a branch run one after another).
-  int group = (int)(((size_t)512 << 20) / (sizeof(float2) * (size_t)ny * nx));
+  int group = (int)(((size_t)1 << 30) / (sizeof(float2) * (size_t)ny * nx));
   if (group < 2) group = 2;
   int r = 0, c = 0;
+  bool tuned = false;  // schedules set for this grid (else the plan's defaults)
   for (auto& kv : b->sched)
-    if (kv.first == key) { r = kv.second[0]; c = kv.second[1]; if (kv.second[2] > 0) group = kv.second[2]; }
+    if (kv.first == key) {
+      r = kv.second[0]; c = kv.second[1]; tuned = true;
+      if (kv.second[2] > 0) group = kv.second[2];
+    }
   msx_plan* p = nullptr;
   *rc = msx_plan_create(ny, nx, group, &p);
   if (*rc != MSX_OK) return nullptr;
-  if (r || c) {
+  if (tuned) {
     *rc = msx_plan_set_schedule(p, r, c, group);
     if (*rc != MSX_OK) { msx_plan_destroy(p); return nullptr; }
   }
@@ -1204,9 +1208,9 @@ int msx_batch_autotune(msx_batch* b, const msx_job* jobs, int njobs, int iters, 
     msx_plan* p = nullptr;
     int rc = msx_plan_create(j.ny, j.nx, 0, &p);
     if (rc != MSX_OK) return rc;
-    // the batch keeps at most 512 MiB of waves per plan and branch
+    // the batch keeps at most 1 GiB of waves per plan and branch
     rc = msx_plan_autotune(p, j.trans_dev, j.num_slices, j.psi_k_dev, j.normalization_dev, j.positions_dev,
-                           j.num_probes, j.kmax, j.lambda, j.slice_t, j.k_band, iters, (size_t)512 << 20, nullptr,
+                           j.num_probes, j.kmax, j.lambda, j.slice_t, j.k_band, iters, (size_t)1 << 30, nullptr,
                            stream);
     int row = 0, col = 0, group = 0;
     if (rc == MSX_OK) rc = msx_plan_get_schedule(p, &row, &col, &group);
