@@ -7,8 +7,8 @@ driven in MSAGPU's order (oracle/refgpu_harness.cu), on identical inputs.
   (probe_kernels.cu:196-206); at the edge its slope is 40 per 1/Angstrom, so float
   rounding of k moves it by up to ~1e-5.  The engine evaluates it in double.
 * CBED: relative L2 <= 1e-4 per pattern (FP32 engine vs FP32 reference path), for
-  the single-probe Si 256^2 case, 64 positions of the Si 512^2 1024-position scan
-  a three-species SrTiO3 256^2 case at 300 keV with defocus and Cs, and a rectangular
+  the single-probe Si 256^2 case, all 1024 positions of the Si 512^2 scan, a
+  three-species SrTiO3 256^2 case at 300 keV with defocus and Cs, and a rectangular
   256 x 384 SrTiO3 grid
 
 The harness libraries are built by oracle/build_ref.py from kernels rendered where
@@ -106,11 +106,12 @@ def test_cbed_single_probe_si256_matches_reference_gpu_path():
     assert 0.9 < want.sum() <= 1.0 + 1e-4
 
 
-def test_cbed_scan_si512_sampled_matches_reference_gpu_path():
+def test_cbed_scan_si512_matches_reference_gpu_path():
+    """Every one of the 1024 patterns of the Si 512^2 scan (199 slices)."""
     ii, jj = np.meshgrid(np.arange(32), np.arange(32), indexing='ij')
-    pos = np.stack([ii.ravel() * A_SI / 32, jj.ravel() * A_SI / 32], 1)[::16]
+    pos = np.stack([ii.ravel() * A_SI / 32, jj.ravel() * A_SI / 32], 1)
     err, got, want = _cbed_parity('c2', PROBE_C2, pos)
-    assert err.shape == (64,)
+    assert err.shape == (1024,)
     assert err.max() <= 1e-4, (err.mean(), err.max())
 
 
