@@ -44,8 +44,8 @@ struct Sched {
   static constexpr int ROW_LINES = LPW * WARPS;      // row lines per CTA
   static constexpr int ROW_LINE_WORDS = PaddedLine::words(N);
   static constexpr size_t row_smem() { return sizeof(float2) * (TW_PAD + (size_t)ROW_LINES * ROW_LINE_WORDS); }
-  // plain column pass: twiddles, the exchange buffer and (probe formation) one float per row
-  static constexpr size_t col_smem() { return sizeof(float2) * (TW_PAD + (size_t)C * N) + sizeof(float) * N; }
+  // plain column pass: twiddles, the exchange buffer and (probe formation) one complex factor per row
+  static constexpr size_t col_smem() { return sizeof(float2) * (TW_PAD + (size_t)C * N + N); }
   static_assert(THREADS == 256 || THREADS == 512, "CTA of 256 or 512 threads");
   static_assert(T <= 32 && 32 % T == 0, "a row line must live inside one warp");
   static constexpr bool PAIRED = false;  // persistent row pass uses PairedFFT512
@@ -149,30 +149,30 @@ __global__ void __launch_bounds__(S::THREADS, S::MINB) col_pass_kernel(ColArgs a
 
   if constexpr (MODE == COL_INIT || MODE == COL_INIT_FINAL) {
     // psi_k * exp(2 pi i (-kx x_p - ky y_p)) * (-1)^(kx_idx + ky_idx); k on the centred
-    // grid j*kmax/(N-1) - kmax/2 (probe_kernels.cu:11-16, 37-57, 239-253).  The two
-    // phase terms (in turns) are formed in double and reduced modulo one turn
-    // separately -- the row terms once per CTA into shared memory, the column term
-    // per thread -- and summed, reduced and evaluated in float.
-    float* ay = reinterpret_cast<float*>(smem + S::TW_PAD + S::C * NY);
+    // grid j*kmax/(N-1) - kmax/2 (probe_kernels.cu:11-16, 37-57, 239-253).  The ramp
+    // factors into exp(-2 pi i ky y_p) exp(-2 pi i kx x_p): each phase (in turns) is
+    // formed in double and reduced modulo one turn, then evaluated in float -- the
+    // row factors once per CTA into shared memory, the column factor per thread --
+    // and the element takes their product.
+    float2* ey = smem + S::TW_PAD + S::C * NY;
     const double km = (double)a.kmax;
     const double py = (double)a.pos_yx[2 * p], px = (double)a.pos_yx[2 * p + 1];
     for (int i = threadIdx.x; i < NY; i += blockDim.x) {
       const double ky = (double)i * km / (double)(NY - 1) - km * 0.5;
       const double ph = -ky * py;
-      ay[i] = (float)(ph - rint(ph));
+      float sn, cs;
+      sincospif(2.0f * (float)(ph - rint(ph)), &sn, &cs);
+      ey[i] = make_float2(cs, sn);
     }
     __syncthreads();
     const double kx = (double)x * km / (double)(a.Nx - 1) - km * 0.5;
     const double phx = -kx * px;
-    const float bx = (float)(phx - rint(phx));
+    float2 ex;
+    sincospif(2.0f * (float)(phx - rint(phx)), &ex.y, &ex.x);
 #pragma unroll
     for (int m = 0; m < S::E; ++m) {
       const int ky_i = t + S::T * m;
-      float ph = ay[ky_i] + bx;
-      ph -= rintf(ph);
-      float sn, cs;
-      sincospif(2.0f * ph, &sn, &cs);
-      float2 val = cmul(__ldg(a.psik + ky_i * Nx + x), make_float2(cs, sn));
+      float2 val = cmul(__ldg(a.psik + ky_i * Nx + x), cmul(ey[ky_i], ex));
       if ((x + ky_i) & 1) val = make_float2(-val.x, -val.y);
       v[m] = val;
     }
