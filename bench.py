@@ -403,7 +403,8 @@ def run_ours(args):
     hbm_peak = hbm_peak or 6800.0
     achieved = alg_bytes / (dom_ms / 1e3) / 1e9
     sm_clock = (clk.get('sm_mhz') or 1900.0)
-    fp32_peak = 152 * 128 * 2 * sm_clock * 1e6 / 1e12
+    sm_count = torch.cuda.get_device_properties(torch.cuda.current_device()).multi_processor_count
+    fp32_peak = sm_count * 128 * 2 * sm_clock * 1e6 / 1e12
     roof = {'bound': 'hbm', 'achieved': achieved, 'peak': hbm_peak, 'unit': 'GB/s', 'frac': achieved / hbm_peak,
             'traffic': NCU_TRAFFIC.get((dom, 512, plan.schedule[0] if dom == 'row' else plan.schedule[1], gw)),
             'kernel': f'{dom}_pass_kernel (512, {gw} waves per launch)', 'peak_source': f'{peak_src} hbm_gbs',
@@ -411,7 +412,7 @@ def run_ours(args):
             'launch_ms': dom_ms, 'row_pass_ms': row_ms, 'col_pass_ms': col_ms,
             'fp32': {'achieved_tflops': alg_flops / (dom_ms / 1e3) / 1e12, 'peak_tflops': fp32_peak,
                      'frac': alg_flops / (dom_ms / 1e3) / 1e12 / fp32_peak,
-                     'peak_source': f'nominal 152 SM x 128 FP32 lanes x 2 at the sampled {sm_clock:.0f} MHz'}}
+                     'peak_source': f'nominal {sm_count} SM x 128 FP32 lanes x 2 at the sampled {sm_clock:.0f} MHz'}}
 
     groups = math.ceil(P / plan.schedule[2])
     launches = args.steps * (1 + groups * (1 + 2 * sim.num_slices))

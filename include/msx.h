@@ -221,11 +221,18 @@ MSX_API int msx_multislice_host(msx_plan* plan, const float* trans_host, int num
  *  msx_plan_probe_waves: fftshift(ifft2_u(psi_k * ramp)) per position (msa.py:959-964).
  *  msx_plan_step_waves:  in place, psi <- ifft2_u(ptab * fft2_u(t * psi)), one slice.
  *  msx_plan_cbed_waves:  |fft2_u(psi)|^2 / N / norm, cropped; the waves are overwritten.
+ *  msx_plan_probe_stack: the probe stack of multislice(transmit=False)
+ *                        (msa.py:959-964 then the division at msa.py:914-915):
+ *                        fftshift(ifft2_u(psi_k * ramp)) / sqrt(norm) per position into
+ *                        probes_out (num_probes, ny, nx) complex64, no propagation.
  */
 MSX_API int msx_propagator_table(int ny, int nx, float kmax, double lambda, double slice_t, float k_band,
                                  float* ptab_out_dev, void* stream);
 MSX_API int msx_plan_probe_waves(msx_plan* plan, const float* psi_k_dev, const float* positions_dev, int num_probes,
                                  float kmax, float* waves_out_dev, void* stream);
+MSX_API int msx_plan_probe_stack(msx_plan* plan, const float* psi_k_dev, const double* normalization_dev,
+                                 const float* positions_dev, int num_probes, float kmax, float* probes_out_dev,
+                                 void* stream);
 MSX_API int msx_plan_step_waves(msx_plan* plan, float* waves_dev, int num_waves, const float* trans_dev,
                                 const float* ptab_dev, void* stream);
 MSX_API int msx_plan_cbed_waves(msx_plan* plan, float* waves_dev, int num_waves, const double* normalization_dev,
@@ -258,9 +265,13 @@ MSX_API int msx_multislice_detect(msx_plan* plan, const float* trans_dev, int nu
  * library; every GPU that loads the library holds it until the process exits.
  * A grid needs (2048 + 2*ny*nx) complex64 words of it at least, so every
  * supported size fits (1024 x 1024 runs 2 waves at a time); larger requests
- * return MSX_ERR_INVALID.  The first call on a device looks up the array's
- * device address (cudaGetSymbolAddress) with that device current; make that
- * first call before any stream capture.  All calls share the array and it keeps
+ * return MSX_ERR_INVALID, and so do complex inputs, positions or the
+ * normalisation that are not 8-byte aligned.  The first call on a device looks
+ * up the array's device address (cudaGetSymbolAddress) with that device
+ * current and keeps it for the life of the process; make that first call
+ * before any stream capture.  A cudaDeviceReset on that device invalidates the
+ * kept address, so this entry point must not be called on a device after it
+ * was reset.  All calls share the array and it keeps
  * the last call's contents (nothing in it needs to start at zero): calls whose
  * work overlaps on the GPU -- on different streams, or from different host
  * threads -- race on it and must be serialised by the caller.  Uses the first

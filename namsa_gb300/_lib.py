@@ -50,6 +50,7 @@ SIGNATURES = [
     ('msx_propagator_table', _c.c_int, [_c.c_int, _c.c_int, _c.c_float, _c.c_double, _c.c_double, _c.c_float, _vp,
                                         _vp]),
     ('msx_plan_probe_waves', _c.c_int, [_vp, _vp, _vp, _c.c_int, _c.c_float, _vp, _vp]),
+    ('msx_plan_probe_stack', _c.c_int, [_vp, _vp, _vp, _vp, _c.c_int, _c.c_float, _vp, _vp]),
     ('msx_plan_step_waves', _c.c_int, [_vp, _vp, _c.c_int, _vp, _vp, _vp]),
     ('msx_plan_cbed_waves', _c.c_int, [_vp, _vp, _c.c_int, _vp, _vp, _c.c_int, _c.c_int, _vp]),
     ('msx_multislice_detect', _c.c_int, [_vp, _vp, _c.c_int, _vp, _vp, _vp, _c.c_int, _c.c_float, _c.c_double,

@@ -737,6 +737,24 @@ int msx_plan_probe_waves(msx_plan* p, const float* psi_k_dev, const float* posit
   return MSX_OK;
 }
 
+int msx_plan_probe_stack(msx_plan* p, const float* psi_k_dev, const double* normalization_dev,
+                         const float* positions_dev, int num_probes, float kmax, float* probes_out_dev, void* stream) {
+  if (!p || num_probes < 0 || !psi_k_dev || !normalization_dev || !positions_dev || !probes_out_dev || !(kmax > 0))
+    return fail(MSX_ERR_INVALID, "probe stack: bad arguments");
+  if (!aligned(psi_k_dev, 8) || !aligned(normalization_dev, 8) || !aligned(positions_dev, 8) ||
+      !aligned(probes_out_dev, 8))
+    return fail(MSX_ERR_INVALID, "probe stack: arrays must be 8-byte aligned");
+  if (num_probes == 0) return MSX_OK;
+  cudaStream_t st = (cudaStream_t)stream;
+  ColArgs c{};
+  c.psi = reinterpret_cast<float2*>(probes_out_dev); c.psik = reinterpret_cast<const float2*>(psi_k_dev);
+  c.pos_yx = positions_dev; c.tw = p->tw_col; c.G = num_probes; c.Nx = p->nx; c.kmax = kmax; c.x_begin = 0;
+  c.ncols = p->nx; c.init_norm = normalization_dev;
+  MSX_CUDA(p->col_ops->col(COL_INIT, c, st), "probe formation pass");
+  MSX_CUDA(p->row_ops->row_mode(ROW_I, c.psi, nullptr, p->tw_row, num_probes, p->ny, st), "inverse row transform");
+  return MSX_OK;
+}
+
 int msx_plan_step_waves(msx_plan* p, float* waves_dev, int num_waves, const float* trans_dev, const float* ptab_dev,
                         void* stream) {
   if (!p || num_waves < 0 || !waves_dev || !trans_dev || !ptab_dev) return fail(MSX_ERR_INVALID, "step waves: bad arguments");

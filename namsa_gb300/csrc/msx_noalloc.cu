@@ -6,8 +6,10 @@
 #include "msx_internal.h"
 
 #include <cstdarg>
+#include <cstdint>
 #include <cstdio>
 #include <cstring>
+#include <mutex>
 #include <string>
 
 using namespace msx;
@@ -23,10 +25,14 @@ static __device__ __align__(256) float2 g_scratch[kScratchWords];
 
 // Host-side cache of the scratch's device address, one per device.  The name
 // g_scratch in host code is only a host-side stand-in; the device address
-// comes from cudaGetSymbolAddress with that device current.
+// comes from cudaGetSymbolAddress with that device current.  The mutex makes
+// the first call on a device safe from several host threads at once.
 constexpr int kMaxDev = 64;
 float2* g_scratch_dev[kMaxDev];
 bool g_scratch_ready[kMaxDev];
+std::mutex g_scratch_mutex;
+
+bool aligned_to(const void* p, size_t a) { return (reinterpret_cast<uintptr_t>(p) % a) == 0; }
 
 int fail(int code, const char* fmt, ...) {
   char buf[512];
@@ -78,6 +84,7 @@ __global__ void twiddle_fill_kernel(Rad rd, float2* __restrict__ tw) {
 
 int ensure_scratch(int dev, float2** out) {
   if (dev < 0 || dev >= kMaxDev) return fail(MSX_ERR_INVALID, "device %d out of range", dev);
+  std::lock_guard<std::mutex> lock(g_scratch_mutex);
   if (!g_scratch_ready[dev]) {
     void* p = nullptr;
     cudaError_t e = cudaGetSymbolAddress(&p, g_scratch);
@@ -112,6 +119,10 @@ extern "C" MSX_API int msx_multislice_noalloc(const float* trans_dev, int num_sl
     return fail(MSX_ERR_INVALID, "crop %d x %d outside the %d x %d grid", crop_y, crop_x, ny, nx);
   if (!psi_k_dev || !normalization_dev || !positions_dev || !cbed_out_dev || (num_slices > 0 && !trans_dev))
     return fail(MSX_ERR_INVALID, "null pointer");
+  if (!aligned_to(trans_dev, 8) || !aligned_to(psi_k_dev, 8) || !aligned_to(positions_dev, 8) ||
+      !aligned_to(normalization_dev, 8) || !aligned_to(cbed_out_dev, 4))
+    return fail(MSX_ERR_INVALID, "complex inputs, positions and the normalisation must be 8-byte aligned, "
+                "the output 4-byte aligned");
   if (!(kmax > 0) || !(lambda > 0) || !(slice_t >= 0) || !(k_band >= 0))
     return fail(MSX_ERR_INVALID, "kmax, lambda must be positive; slice thickness and k_band non-negative");
   size_t g = (kScratchWords - fixed) / wave;

@@ -127,6 +127,7 @@ struct ColArgs {
   const float* det;        // (ndet, Ny, Nx) detector weights over the CBED grid (detect)
   int ndet;
   float* partial;          // (G, Nx / C, ndet) per-tile detector sums (detect)
+  const double* init_norm; // init: when set, the probe is scaled by 1/sqrt(*init_norm)
 };
 
 template <class S, int MODE>
@@ -169,6 +170,10 @@ __global__ void __launch_bounds__(S::THREADS, S::MINB) col_pass_kernel(ColArgs a
     const double phx = -kx * px;
     float2 ex;
     sincospif(2.0f * (float)(phx - rint(phx)), &ex.y, &ex.x);
+    if (a.init_norm) {  // unit-norm probe stack (msa.py:915): the scale folds into the column factor
+      const float sc = (float)(1.0 / sqrt(*a.init_norm));
+      ex = make_float2(ex.x * sc, ex.y * sc);
+    }
 #pragma unroll
     for (int m = 0; m < S::E; ++m) {
       const int ky_i = t + S::T * m;

@@ -306,6 +306,23 @@ class Plan:
                                               float(kmax), _ptr(out), _stream()))
         return out
 
+    def probe_stack(self, psik, norm, positions, kmax, out=None):
+        """Unit-norm real-space probes (P, ny, nx) complex64 at each position, no
+        propagation: fftshift(ifft2_u(psi_k * ramp)) / sqrt(norm)."""
+        _need(psik, torch.complex64, 'psi_k', 2)
+        _need(norm, torch.float64, 'normalization', 1)
+        _need(positions, torch.float32, 'positions', 2)
+        P = positions.shape[0]
+        if out is None:
+            out = torch.empty((P, self.ny, self.nx), dtype=torch.complex64, device=psik.device)
+        else:
+            _need(out, torch.complex64, 'out', 3)
+            if tuple(out.shape) != (P, self.ny, self.nx):
+                raise ValueError('out has the wrong shape')
+        _lib.check(lib().msx_plan_probe_stack(self.handle, _ptr(psik), _ptr(norm), _ptr(positions), P, float(kmax),
+                                              _ptr(out), _stream()))
+        return out
+
     def step_waves(self, waves, trans, ptab):
         """One slice in place on real-space waves (G, ny, nx): psi <- ifft2(ptab * fft2(t * psi))."""
         _need(waves, torch.complex64, 'waves', 3)

@@ -189,10 +189,11 @@ class MSAGPU:
         self.num_probes = 0
         self._plan = None
         self._probes_host = None
-        self.print_verbose('Simulation Parameters:\nSupercell dimensions xyz:%s (A)\nReal, Reciprocal space pixel sizes:'
-                           '%s A, %s 1/A\nMax angle: %2.2f (rad)\nSampling: %s pixels' %
-                           (np.round(self.dims, 3), np.round(self.pix_size, 3), np.round(self.kpix_size, 3),
-                            self.max_ang, self.sampling))
+        self._last = None
+        self.probe_stack = None
+        self.print_verbose(f'grid {self.sampling[0]} x {self.sampling[1]} px over a {self.dims[0]:.3f} x '
+                           f'{self.dims[1]:.3f} x {self.dims[2]:.3f} A cell; pixel {self.pix_size[0]:.4f} A, '
+                           f'k pixel {self.kpix_size[0]:.4f} 1/A; largest angle {self.max_ang * 1e3:.1f} mrad')
 
     # ------------------------------------------------------------------ utilities
     def print_debug(self, *args, **kwargs):
@@ -358,29 +359,39 @@ class MSAGPU:
         None keeps the full grid like the reference.  ``unified_mem`` and
         ``batch_size`` are accepted for compatibility; batching is the plan's.
         The result stays on the device in ``self.cbed``; ``self.probes`` is
-        its host copy."""
+        its host copy.  With ``transmit=False`` no slice is applied: the result
+        is the unit-norm complex64 probe stack at every position
+        (``self.probe_stack``; msa.py:970, 914-915)."""
         if self.trans is None:
             raise RuntimeError('Potential slices must be calculated first: call build_potential_slices().')
         if getattr(self, 'psi_k_dev', None) is None:
             raise RuntimeError('Probe must be initiated first: call build_probe().')
         if self.probe_positions is None:
             raise RuntimeError('Probe positions must be set first: call generate_probe_positions().')
-        if not transmit:
-            raise NotImplementedError('transmit=False (probe wavefunctions only) is not provided')
         dev = self._dev()
         self.bandwidth = bandwidth
         pos = torch.from_numpy(np.ascontiguousarray(np.asarray(self.probe_positions, np.float32))).to(dev)
+        self._probes_host = None
+        if not transmit:
+            # probe wavefunctions only (msa.py:970, 914-915): the unit-norm real-space
+            # probe stack, complex64, with no slice applied
+            self.probe_stack = self.plan().probe_stack(self.psi_k_dev, self.norm_dev, pos, np.float32(self.kmax))
+            self._last = self.probe_stack
+            return None
         self.cbed = self.plan().multislice(self.trans, self.psi_k_dev, self.norm_dev, pos, np.float32(self.kmax),
                                            self.Lambda, self.slice_t, np.float32(bandwidth * self.kmax), crop=crop)
-        self._probes_host = None
+        self._last = self.cbed
         return None
 
     @property
     def probes(self):
-        if self.cbed is None:
+        """Host copy of the last multislice result: the float32 CBED stack, or with
+        transmit=False the complex64 probe stack."""
+        last = getattr(self, '_last', None)
+        if last is None:
             return None
         if self._probes_host is None:
-            self._probes_host = self.cbed.cpu().numpy()
+            self._probes_host = last.cpu().numpy()
         return self._probes_host
 
     @probes.setter

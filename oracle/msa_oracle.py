@@ -335,20 +335,65 @@ def multislice_gpu(t, psi_k, P, positions_yx, normalization, geom, crop=None, dt
     (msa.py:985-990, 905).  ``crop`` keeps rows/cols N/2-crop/2 .. N/2+crop/2-1.
     ``t`` is (S, Ny, Nx); all FFTs are unnormalised like cuFFT's C2C.
     """
+    import scipy.fft as sfft  # pocketfft, as numpy.fft, with threads over the rows
     ct = np.complex128 if dtype == np.float64 else np.complex64
+    fft2 = lambda a: sfft.fft2(a, workers=-1)
+    ifft2 = lambda a: sfft.ifft2(a, workers=-1)
     S, Ny, Nx = t.shape
     N = Ny * Nx
     out = []
+    Pc = P.astype(ct)
     for pos in np.asarray(positions_yx):
-        psi = np.fft.fftshift(np.fft.ifft2(psi_k.astype(ct) * probe_ramp_gpu(geom, pos, (Ny, Nx)).astype(ct)) * N)
+        psi = np.fft.fftshift(ifft2(psi_k.astype(ct) * probe_ramp_gpu(geom, pos, (Ny, Nx)).astype(ct)) * N)
         for i in range(S):
             psi = psi * t[i].astype(ct) / N
-            psi = np.fft.ifft2(np.fft.fft2(psi) * P.astype(ct)) * N
-        I = np.abs(np.fft.fft2(psi / N) * np.sqrt(N)) ** 2 / normalization
+            psi = ifft2(fft2(psi) * Pc) * N
+        I = np.abs(fft2(psi / N) * np.sqrt(N)) ** 2 / normalization
         if crop is not None and crop < min(Ny, Nx):
             I = I[Ny // 2 - crop // 2:Ny // 2 + crop // 2, Nx // 2 - crop // 2:Nx // 2 + crop // 2]
         out.append(I.astype(np.float64 if dtype == np.float64 else np.float32))
     return np.array(out)
+
+
+def probe_stack_gpu(psi_k, positions_yx, normalization, geom):
+    """Probe stack of ``multislice(transmit=False)`` (namsa/msa.py:959-964, 970, 914-915).
+
+    For each position fftshift(ifft2_u(psi_k * ramp)) / sqrt(normalization),
+    complex128: the probes are formed and shifted, no slice is applied, and
+    the stack is divided by the square root of the normalisation."""
+    Ny, Nx = psi_k.shape
+    out = []
+    for pos in np.asarray(positions_yx):
+        psi = np.fft.fftshift(np.fft.ifft2(psi_k.astype(np.complex128) * probe_ramp_gpu(geom, pos, (Ny, Nx))) * Ny * Nx)
+        out.append(psi / np.sqrt(normalization))
+    return np.array(out)
+
+
+def bandwidth_limit_mask(shape, radius):
+    """Disc of pixel radius max(shape)*radius about the centre (namsa/msa.py:246-251)."""
+    gx, gy = np.mgrid[-shape[0] // 2:shape[0] // 2, -shape[1] // 2:shape[1] // 2]
+    r = np.sqrt(gx ** 2 + gy ** 2)
+    return np.heaviside(max(shape[0], shape[1]) * radius - r, 0).astype(np.float32)
+
+
+def annular_detector(sampling, kpix_size, lam, inner_angle, outer_angle):
+    """Annular detector of ``integrate_cbed`` (namsa/msa.py:428-435): the radii are
+    angle / (kpix * lambda * N) / 2 per axis, the first axis's is used, and the
+    annulus is where the outer and inner discs differ."""
+    sampling = np.asarray(sampling)
+    inner = inner_angle / (np.asarray(kpix_size) * lam * sampling) / 2
+    outer = outer_angle / (np.asarray(kpix_size) * lam * sampling) / 2
+    inner_seg = bandwidth_limit_mask(sampling, inner[0]).astype(bool)
+    outer_seg = bandwidth_limit_mask(sampling, outer[0]).astype(bool)
+    return np.logical_not(outer_seg == inner_seg)
+
+
+def integrate_cbed(cbed, grid_steps, detector):
+    """STEM image of ``integrate_cbed`` (namsa/msa.py:436-439): the CBED stack
+    reshaped to (grid_steps..., Ny, Nx) and summed over each pattern times the
+    detector, in float64."""
+    stack = np.asarray(cbed, np.float64).reshape(list(grid_steps) + list(np.shape(cbed)[-2:]))
+    return np.sum(stack * np.asarray(detector, np.float64), axis=(-2, -1))
 
 
 def exit_wave_cpu(V, sigma, psi0, Pmask):

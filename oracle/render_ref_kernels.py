@@ -12,14 +12,17 @@ workloads the parity tests use, and writes the rendered sources into
   c2  Si 8x8x50 cells (face-inclusive), 512^2, 200 keV, t = a/4 (199 slices)
   c4  SrTiO3 12x12x16 cells, 256^2, 300 keV, t = a/2 (three species)
   c5  SrTiO3 18x12x8 cells (x, y, z), a rectangular 256 x 384 (y, x) grid, 200 keV
+  c6  Si 12x12x20 cells (face-inclusive), 768^2, 300 keV, t = a/4 (80 slices)
+  c7  SrTiO3 40x40x12 cells, 1024^2, 300 keV, t = a/2 (24 slices)
 
 plus ``oracle/_ref/workloads.json`` with the rendered parameters.  The sources
 are then compiled against the stand-in header ``oracle/pycuda-complex.hpp`` and
 the harness ``oracle/refgpu_harness.cu`` by ``oracle/build_ref.py``.
 
-The rendering needs the reference checkout (``/root/reference`` by default, or
-the ``NAMSA_REFERENCE`` environment variable); machines without it use the
-rendered files already present in ``oracle/_ref/``.
+The rendering needs a reference checkout, named by the ``NAMSA_REFERENCE``
+environment variable or the first argument (``python oracle/render_ref_kernels.py
+CHECKOUT``); machines without one use the rendered files already present in
+``oracle/_ref/``.
 """
 from __future__ import annotations
 
@@ -32,7 +35,7 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(HERE)
 OUT = os.path.join(HERE, '_ref')
-REFERENCE = os.environ.get('NAMSA_REFERENCE', '/root/reference')
+REFERENCE = os.environ.get('NAMSA_REFERENCE')
 
 A_SI = 5.431
 A_STO = 3.905
@@ -41,6 +44,8 @@ WORKLOADS = {
     'c2': dict(crystal='si', cells=(8, 8, 50), n=512, kv=200.0, semi=30e-3, slice_t=A_SI / 4),
     'c4': dict(crystal='srtio3', cells=(12, 12, 16), n=256, kv=300.0, semi=25e-3, slice_t=A_STO / 2),
     'c5': dict(crystal='srtio3', cells=(18, 12, 8), n=(256, 384), kv=200.0, semi=25e-3, slice_t=A_STO / 2),
+    'c6': dict(crystal='si', cells=(12, 12, 20), n=768, kv=300.0, semi=25e-3, slice_t=A_SI / 4),
+    'c7': dict(crystal='srtio3', cells=(40, 40, 12), n=1024, kv=300.0, semi=25e-3, slice_t=A_STO / 2),
 }
 
 
@@ -69,8 +74,11 @@ def workload_params(tag):
                 crystal=w['crystal'], cells=list(w['cells']), kv=w['kv'], semi=w['semi'], slice_t=t)
 
 
-def render(reference=REFERENCE, out=OUT):
+def render(reference=None, out=OUT):
     from jinja2 import Template
+    reference = reference or REFERENCE
+    if not reference:
+        raise RuntimeError('no reference checkout: set NAMSA_REFERENCE or pass its path')
     os.makedirs(out, exist_ok=True)
     with open(os.path.join(reference, 'namsa', 'probe_kernels.cu')) as f:
         probe_t = Template(f.read())
@@ -95,9 +103,10 @@ def render(reference=REFERENCE, out=OUT):
     return meta
 
 
-def available(reference=REFERENCE):
-    return os.path.exists(os.path.join(reference, 'namsa', 'probe_kernels.cu'))
+def available(reference=None):
+    reference = reference or REFERENCE
+    return bool(reference) and os.path.exists(os.path.join(reference, 'namsa', 'probe_kernels.cu'))
 
 
 if __name__ == '__main__':
-    print(json.dumps(render(), indent=1))
+    print(json.dumps(render(*sys.argv[1:2]), indent=1))

@@ -1,7 +1,7 @@
 """Generate the golden fixtures in this folder from the reference's own CPU code.
 
-Run in a container where the reference checkout is available (the path is the
-first argument, default ``/root/reference``).  The reference package imports
+Run where a checkout of the reference is available; its path is the first
+argument or the environment variable ``NAMSA_REFERENCE``.  The reference package imports
 pycuda/skcuda/mpi4py/h5py/pymatgen at module load; none of these is used by
 the ``MSA`` CPU class, so they are replaced by empty stub modules, and the
 NumPy aliases removed in NumPy 2 (``np.int``, ``np.float``, ``np.bool``) are
@@ -23,6 +23,13 @@ Fixtures written (all ``.npz``):
                          on a seeded 3-D potential.  SciPy 1.14 removed
                          ``integrate.trapz``; it is aliased to ``trapezoid``
                          (the same rule) for this call.
+* ``detector.npz``    -- ``MSA.integrate_cbed`` (namsa/msa.py:426-439) on a seeded
+                         CBED stack: the default 50-100 mrad annulus it builds and a
+                         20-60 mrad one, with the integrated signals.
+* ``cif.npz``         -- the reference's own CIF test inputs and expected unit
+                         cells (cif_files/mvc-9418.cif with mvc-9418_P_1_1_1.xyz,
+                         the golden of tests/supercell_tests.py:8-21, and
+                         cif_files/Si.cif), read as text.
 """
 import os
 import sys
@@ -67,7 +74,41 @@ def import_reference_utils(ref_root):
     return ref_utils
 
 
-def main(ref_root='/root/reference'):
+def detector_fixture(msa, rng):
+    """integrate_cbed of the reference CPU class on a seeded CBED stack."""
+    m = msa.MSA(200, 30e-3, si_supercell(2, 2, 1), sampling=np.array([64, 64]), debye_waller=False)
+    m.grid_steps = np.array([3, 2])
+    cbed = rng.gamma(0.8, 1e-3, size=(6, 64, 64)).astype(np.float32)
+    out = {'cbed': cbed, 'grid_steps': m.grid_steps, 'sampling': m.sampling, 'kpix_size': m.kpix_size,
+           'Lambda': m.Lambda, 'max_ang': m.max_ang}
+    for tag, params in [('default', {'inner_angle': 50e-3, 'outer_angle': 100e-3}),
+                        ('narrow', {'inner_angle': 20e-3, 'outer_angle': 60e-3})]:
+        m.probes = cbed.copy()
+        sig, det = m.integrate_cbed(detector_params=params)
+        out[tag + '_inner'] = params['inner_angle']
+        out[tag + '_outer'] = params['outer_angle']
+        out[tag + '_detector'] = det
+        out[tag + '_signal'] = sig
+    return out
+
+
+def cif_fixture(ref_root):
+    """The reference's CIF test inputs and expected P1 unit cell, as text and arrays."""
+    d = os.path.join(ref_root, 'cif_files')
+    with open(os.path.join(d, 'mvc-9418.cif')) as f:
+        mvc = f.read()
+    with open(os.path.join(d, 'Si.cif')) as f:
+        si = f.read()
+    xyz = np.loadtxt(os.path.join(d, 'mvc-9418_P_1_1_1.xyz'), skiprows=2,
+                     dtype=[('atom_type', '|U16'), ('x', 'f'), ('y', 'f'), ('z', 'f')])
+    return {'mvc_cif': np.array(mvc), 'si_cif': np.array(si), 'mvc_types': xyz['atom_type'],
+            'mvc_xyz': np.column_stack([xyz['x'], xyz['y'], xyz['z']])}
+
+
+def main(ref_root=None):
+    ref_root = ref_root or os.environ.get('NAMSA_REFERENCE')
+    if not ref_root:
+        raise SystemExit('usage: make_golden.py REFERENCE_CHECKOUT (or set NAMSA_REFERENCE)')
     msa, optics = import_reference(ref_root)
     volts = np.array([80e3, 100e3, 120e3, 200e3, 300e3])
     np.savez_compressed(os.path.join(HERE, 'optics.npz'), volts=volts,
@@ -143,6 +184,9 @@ def main(ref_root='/root/reference'):
     out = m3.integrate_potential_slices(pot, (zc, yc, xc), 2.5, output=True)
     np.savez_compressed(os.path.join(HERE, 'integrated.npz'), pot=pot, z=zc, y=yc, x=xc, slice_t=2.5,
                         slices=out, sigma=m3.sigma, sampling=m3.sampling, dims=m3.dims)
+
+    np.savez_compressed(os.path.join(HERE, 'detector.npz'), **detector_fixture(msa, np.random.default_rng(11)))
+    np.savez_compressed(os.path.join(HERE, 'cif.npz'), **cif_fixture(ref_root))
     print('golden fixtures written to', HERE)
 
 

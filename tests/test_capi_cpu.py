@@ -85,3 +85,21 @@ def test_reference_gpu_harness_exports_and_site_layout():
         n = len(want[s])
         np.testing.assert_array_equal(trip[:n], want[s].astype(np.float32))
         assert np.all(trip[n:, 0] == 1)
+
+
+def test_noalloc_rejects_misaligned_pointers(libmsx):
+    """The allocation-free entry point checks the alignment its kernels need
+    (8 bytes for complex64 and float64, as msx_multislice does) before any device
+    work, so a pointer into the middle of a caller's pool returns an error status
+    instead of faulting on the GPU."""
+    from namsa_gb300 import _lib
+    vp = ctypes.c_void_p
+    good, odd = 0x10000, 0x10004
+
+    def call(trans, psik, norm, pos, out):
+        return libmsx.msx_multislice_noalloc(vp(trans), 2, vp(psik), vp(norm), vp(pos), 3, 256, 256, 12.8, 0.025,
+                                             1.5, 4.0, vp(out), 128, 128, None)
+    for args in [(odd, good, good, good, good), (good, odd, good, good, good), (good, good, odd, good, good),
+                 (good, good, good, odd, good), (good, good, good, good, odd + 2)]:
+        assert call(*args) == _lib.MSX_ERR_INVALID
+        assert 'aligned' in _lib.last_error()

@@ -383,21 +383,30 @@ def test_config2_scan_sampled_vs_fp64():
     assert err.max() < 1e-4, err
 
 
-def test_detector_signals_match_cbed_sums():
-    """Fused detector epilogue (msx_multislice_detect) against the CBED stack
-    summed with the same weights in float64 (MSA.integrate_cbed, msa.py:426-439)."""
-    g, trans, psik, norm, pos, kmax, lam, st = random_case(256, 256, S=4, P=5, seed=21)
-    cbed = engine_cbed(trans, psik, norm, pos, kmax, lam, st, 0.45)
-    det = np.stack([M.annular_detector(np.array([256, 256]), np.array([kmax, kmax]) / 256, lam, a, b)
-                    for a, b in [(0.02, 0.05), (0.05, 0.09), (0.0, 0.02)]]).astype(np.float32)
-    ref = np.einsum('pyx,dyx->pd', cbed.astype(np.float64), det.astype(np.float64))
+def test_detector_signals_match_oracle():
+    """Fused detector epilogue (msx_multislice_detect) against the oracle's
+    integrate_cbed (namsa/msa.py:426-439, pinned to the reference class by
+    tests/golden/detector.npz) applied to the FP64 oracle's CBED stack of the same
+    inputs, with the reference's own annuli and a smooth weight map."""
+    g, trans, psik, norm, pos, kmax, lam, st = random_case(256, 256, S=4, P=6, seed=21)
+    kpix = np.array([kmax, kmax]) / 256
+    det = [O.annular_detector(np.array([256, 256]), kpix, lam, a, b) for a, b in [(0.02, 0.05), (0.05, 0.09),
+                                                                                   (0.0, 0.02)]]
+    ky, kx = np.mgrid[-128:128, -128:128]
+    det.append(np.exp(-(kx ** 2 + ky ** 2) / 900.0))
+    det = np.stack(det).astype(np.float32)
+    P, _ = O.propagator_gpu(g, st, 0.45)
+    cbed = O.multislice_gpu(trans.astype(np.complex128), psik.astype(np.complex128), P, pos, norm, g)
+    ref = np.stack([O.integrate_cbed(cbed, (6,), d) for d in det], axis=1)
     plan = engine.Plan(256, 256, 2)
     sig = plan.detect(torch.from_numpy(trans).to(DEV), torch.from_numpy(psik).to(DEV),
                       torch.tensor([norm], dtype=torch.float64, device=DEV), torch.from_numpy(pos).to(DEV),
                       np.float32(kmax), lam, st, np.float32(0.45 * kmax), torch.from_numpy(det).to(DEV)).cpu().numpy()
     plan.close()
-    assert sig.shape == (5, 3)
+    assert sig.shape == (6, 4)
     assert np.abs(sig - ref).max() <= 2e-5 * np.abs(ref).max()
+    # the facade's stored-stack form agrees with the fused one
+    assert np.abs(sig[:, :3] - np.einsum('pyx,dyx->pd', cbed, det[:3].astype(np.float64))).max() <= 2e-5 * np.abs(ref).max()
 
 
 def test_real_space_stepping_matches_multislice():
@@ -415,3 +424,33 @@ def test_real_space_stepping_matches_multislice():
     got = plan.cbed_waves(w, d_norm).cpu().numpy()
     plan.close()
     assert O.rel_l2(got, ref).max() < 2e-6
+
+
+@pytest.mark.parametrize('ny,nx', [(256, 256), (256, 384)])
+def test_probe_stack_without_transmission(ny, nx):
+    """multislice(transmit=False) returns the unit-norm complex64 probe stack of
+    every position with no slice applied (namsa/msa.py:959-964, 970, 914-915),
+    checked against the FP64 oracle's probe formation."""
+    sc = O.srtio3_supercell(6, 6, 2)
+    pd = {'smooth_apert': True, 'apert_smooth': 50, 'spherical_phase': True,
+          'aberration_dict': {'C1': 25., 'C3': 2e4, 'C5': 0.}, 'scherzer': False}
+    sim = M.MSAGPU(200, 25e-3, sc, sampling=np.array([ny, nx]), debye_waller=False)
+    sim.setup_device(0)
+    sim.calc_atomic_potentials()
+    sim.build_potential_slices(3.905 / 2)
+    sim.build_probe(pd)
+    sim.generate_probe_positions(grid_steps=np.array([3, 4]))
+    sim.multislice(transmit=False)
+    got = sim.probes
+    assert got.dtype == np.complex64 and got.shape == (12, ny, nx)
+
+    geom = crystal_geom(sc, 200., 25e-3, (ny, nx))
+    psik, _, norm = O.probe_gpu(geom, pd)
+    ref = O.probe_stack_gpu(psik, sim.probe_positions.astype(np.float32), norm, geom)  # the engine's float32 positions
+    err = np.linalg.norm((got - ref).reshape(12, -1), axis=1) / np.linalg.norm(ref.reshape(12, -1), axis=1)
+    assert err.max() < 5e-6, err
+    np.testing.assert_allclose(np.sum(np.abs(got.astype(np.complex128)) ** 2, axis=(1, 2)), 1.0, rtol=1e-5)
+    # a CBED run afterwards still returns the float32 stack
+    sim.multislice(crop=128)
+    assert sim.probes.dtype == np.float32 and sim.probes.shape == (12, 128, 128)
+    sim.close()

@@ -8,8 +8,9 @@ driven in MSAGPU's order (oracle/refgpu_harness.cu), on identical inputs.
   rounding of k moves it by up to ~1e-5.  The engine evaluates it in double.
 * CBED: relative L2 <= 1e-4 per pattern (FP32 engine vs FP32 reference path), for
   the single-probe Si 256^2 case, all 1024 positions of the Si 512^2 scan, a
-  three-species SrTiO3 256^2 case at 300 keV with defocus and Cs, and a rectangular
-  256 x 384 SrTiO3 grid
+  three-species SrTiO3 256^2 case at 300 keV with defocus and Cs, a rectangular
+  256 x 384 SrTiO3 grid, a Si 768^2 grid (three-stage radix schedules) and a
+  SrTiO3 1024^2 grid, the line lengths of the uneven batch and the precision study
 
 The harness libraries are built by oracle/build_ref.py from kernels rendered where
 the reference checkout exists; without them these tests skip with that reason.
@@ -57,7 +58,7 @@ def _case(tag):
     return ref, sim, geom, win
 
 
-@pytest.mark.parametrize('tag', ['c1', 'c2', 'c4', 'c5'])
+@pytest.mark.parametrize('tag', ['c1', 'c2', 'c4', 'c5', 'c6', 'c7'])
 def test_transmission_bit_identical_to_reference_kernel(tag):
     ref, sim, geom, win = _case(tag)
     t_ref = ref.build_potential(geom, ref.meta['slice_t'], win)
@@ -67,7 +68,8 @@ def test_transmission_bit_identical_to_reference_kernel(tag):
     sim.close()
 
 
-@pytest.mark.parametrize('tag,pd', [('c1', PROBE_C1), ('c2', PROBE_C2), ('c4', PROBE_C4), ('c5', PROBE_C2)])
+@pytest.mark.parametrize('tag,pd', [('c1', PROBE_C1), ('c2', PROBE_C2), ('c4', PROBE_C4), ('c5', PROBE_C2),
+                                    ('c6', PROBE_C4), ('c7', PROBE_C2)])
 def test_probe_matches_reference_kernels(tag, pd):
     ref, sim, geom, _ = _case(tag)
     sim.build_probe(pd)
@@ -125,4 +127,20 @@ def test_cbed_rectangular_grid_matches_reference_gpu_path():
     pos = np.array([[0., 0.], [1.3, -2.1]])
     err, got, want = _cbed_parity('c5', PROBE_C2, pos)
     assert got.shape == (2, 256, 384)
+    assert err.max() <= 1e-4, err
+
+
+def test_cbed_si768_matches_reference_gpu_path():
+    """768^2 grid (radices 8.8.12), Si 12x12x20 cells, 80 slices, 300 keV, hard aperture."""
+    pos = np.array([[0., 0.], [1.4, 2.7], [-2.6, -0.9]])
+    err, got, want = _cbed_parity('c6', PROBE_C4, pos)
+    assert got.shape == (3, 768, 768)
+    assert err.max() <= 1e-4, err
+
+
+def test_cbed_srtio3_1024_matches_reference_gpu_path():
+    """1024^2 grid, SrTiO3 40x40x12 cells, 24 slices, 300 keV, Cs 1 um."""
+    pos = np.array([[0., 0.], [1.9, -1.0]])
+    err, got, want = _cbed_parity('c7', PROBE_C2, pos)
+    assert got.shape == (2, 1024, 1024)
     assert err.max() <= 1e-4, err

@@ -110,3 +110,27 @@ def test_integrated_potential_matches_reference():
     out = O.integrate_potential_slices(g['pot'], g['z'], float(g['slice_t']))
     assert out.shape == g['slices'].shape
     np.testing.assert_allclose(out, g['slices'], rtol=2e-6, atol=2e-6)
+
+
+def test_integrate_cbed_against_reference():
+    """Detector epilogue oracle (integrate_cbed, namsa/msa.py:426-439) against the
+    reference class's own output: the annulus it builds from the angles, bit for
+    bit, and the integrated signals of a seeded CBED stack."""
+    g = np.load(os.path.join(G, 'detector.npz'))
+    for tag in ('default', 'narrow'):
+        det = O.annular_detector(g['sampling'], g['kpix_size'], float(g['Lambda']), float(g[tag + '_inner']),
+                                 float(g[tag + '_outer']))
+        np.testing.assert_array_equal(det, g[tag + '_detector'])
+        sig = O.integrate_cbed(g['cbed'], g['grid_steps'], det)
+        assert sig.shape == tuple(g['grid_steps'])
+        np.testing.assert_allclose(sig, g[tag + '_signal'], rtol=2e-6)
+
+
+def test_facade_detector_matches_reference():
+    """The MSAGPU surface builds the same annulus as the reference (host code, no GPU)."""
+    from namsa_gb300 import msa as M
+    g = np.load(os.path.join(G, 'detector.npz'))
+    for tag in ('default', 'narrow'):
+        det = M.annular_detector(g['sampling'], g['kpix_size'], float(g['Lambda']), float(g[tag + '_inner']),
+                                 float(g[tag + '_outer']))
+        np.testing.assert_array_equal(det, g[tag + '_detector'])
