@@ -360,6 +360,19 @@ MSX_API int msx_tc_set_compensation(int enable);
 MSX_API int msx_tc_check(void);
 
 /*
+ * General BF16 tensor-core GEMM (no reference counterpart), the contraction
+ * engine of the learned corrector: c (m x n) = a (m x k) . b (n x k)^T (+ bias[n])
+ * with a and b rounded to bfloat16 and FP32 accumulation on tcgen05; with
+ * accumulate = 1 the product is added to c.  a, b, c are FP32 row-major with
+ * leading dimensions lda, ldb, ldc (elements); n <= 4096.  Operand images are
+ * held per host thread and grow with the largest call.  msx_gemm_check
+ * synchronises and reports MSX_ERR_TIMEOUT if a bounded wait gave up.
+ */
+MSX_API int msx_gemm_bf16(const float* a_dev, int lda, const float* b_dev, int ldb, int m, int n, int k, float* c_dev,
+                          int ldc, const float* bias_dev, int accumulate, void* stream);
+MSX_API int msx_gemm_check(void);
+
+/*
  * Self-test of the bounded in-kernel wait (no reference counterpart).  One CTA
  * waits on an mbarrier with a limit of 2^limit_log2 cycles (10..31); with
  * arrive = 0 nothing arrives, so the wait runs out and the call returns
@@ -370,30 +383,66 @@ MSX_API int msx_tc_check(void);
 MSX_API int msx_selftest_wait(int arrive, int limit_log2, void* stream);
 
 /*
- * Learned coarse-slice corrector (no counterpart in the reference): a
- * spectral-convolution network mapping the wave after one thick slice and
- * that slice's transmission t_c to the wave of the equivalent fine slices.
- * channels <= 32 (C), layers L, 8 x 8 retained Fourier modes per layer.
- * Waves and transmissions are (batch, ny, nx) complex64; waves are expected
- * scaled by sqrt(ny*nx).  Parameters, gradients and Adam moments are four
- * consecutive float32 arrays of `count` values (msx_corrector_params); the
- * layout is documented in namsa_gb300/csrc/msx_corrector.cu.  Parameters
- * start at zero: the caller writes its initialisation.
- *  msx_corrector_forward:   pred = psi_c + net(psi_c, t_c)
- *  msx_corrector_loss_grad: loss = sum_b w_b sum |pred_b - psi_f_b|^2 / denom (to
- *                           *loss_out_dev; w_b = sample_weights_dev[b], or 1 when NULL)
- *                           and the gradient of every parameter (overwritten)
- *  msx_corrector_adam:      one Adam step on the stored gradient
+ * Learned coarse-slice corrector (no counterpart in the reference).  A
+ * spectral-convolution network maps the potentials of the `ratio` fine slices
+ * inside one coarse slice to two per-pixel complex maps A, B of the corrected
+ * coarse step
+ *     psi <- (1 + A) . ifft2( P_c . fft2( (1 + B) . t_c . psi ) )
+ * (P_c the coarse propagator, t_c the coarse transmission).  The maps depend on
+ * the crystal only: the network runs once per coarse slice and the corrected
+ * multislice of every probe costs what the plain coarse one costs.
+ *
+ * Network: lift of `in_channels` inputs to C channels, L spectral layers
+ * (per-mode C x C complex mixing on modes kx in [0, modes_x), ky in
+ * [-modes_y/2, modes_y/2), plus a pointwise C x C layer, gelu), pointwise MLP
+ * head C -> C -> 4.  Every contraction (lift, pointwise layers, head, their
+ * weight gradients, the partial DFT stages) runs as a bfloat16 GEMM with FP32
+ * accumulation on the tensor cores; activations are FP32, pixel-major
+ * (samples, ny, nx, channels).  Parameters, gradients and Adam moments are
+ * four consecutive float32 arrays of `count` values; msx_corrector_layout
+ * gives the offsets of W0 (C x in), b0, then per layer R (modes_x * modes_y *
+ * C * C complex, mode-major), W (C x C), b, then P1 (C x C), c1, P2 (4 x C), c2.
+ * Parameters start at zero: the caller writes its initialisation.
+ *  msx_corrector_forward:  features (S, ny, nx, in_channels) -> maps (S, ny, nx, 4) =
+ *                          (Re A, Im A, Re B, Im B); keeps what the backward needs
+ *  msx_corrector_backward: d loss / d maps (S, ny, nx, 4) -> parameter gradients
+ *                          (overwritten), for the S samples of the last forward
+ *  msx_corrector_adam:     one Adam step on the stored gradients
+ *  msx_corrector_check:    synchronises; MSX_ERR_TIMEOUT if a GEMM wait gave up
+ *  msx_corrector_features: inputs of S coarse slices from the fine potential
+ *                          slices pot (S * ratio, ny, nx): sigma V of each fine
+ *                          slice, their sum and the constant tval (in_channels =
+ *                          ratio + 2)
+ * Rollout helpers on complex64 waves (num, ny, nx) with one map set (ny, nx, 4):
+ *  msx_corrector_apply_map:  waves *= (1 + M) (conj: its conjugate), M = A (which 0) or B (1)
+ *  msx_corrector_mul_plane:  waves *= plane (conj: its conjugate) for one complex (ny, nx) plane
+ *  msx_corrector_map_trans:  out = trans (1 + M) for one (ny, nx) plane
+ *  msx_corrector_map_grad:   dmaps[.., M] (+)= 2 sum_b conj(u_b) g_b (d loss / d Re M, d Im M
+ *                            for a map that multiplied u, g the adjoint of the product)
+ *  msx_corrector_residual:   adjoint (+)= weight (psi - target); *loss_out = weight sum |psi - target|^2
  */
-MSX_API int msx_corrector_create(int ny, int nx, int channels, int layers, int max_batch, msx_corrector** corrector);
+MSX_API int msx_corrector_create(int ny, int nx, int in_channels, int channels, int layers, int modes_x, int modes_y,
+                                 int max_samples, msx_corrector** corrector);
 MSX_API int msx_corrector_destroy(msx_corrector* corrector);
 MSX_API int msx_corrector_params(msx_corrector* corrector, float** params_dev, float** grads_dev, size_t* count);
-MSX_API int msx_corrector_forward(msx_corrector* corrector, const float* psi_c_dev, const float* tc_dev, int batch,
-                                  float* pred_out_dev, void* stream);
-MSX_API int msx_corrector_loss_grad(msx_corrector* corrector, const float* psi_c_dev, const float* tc_dev,
-                                    const float* psi_f_dev, int batch, double denom, const float* sample_weights_dev,
-                                    float* loss_out_dev, void* stream);
+MSX_API int msx_corrector_layout(const msx_corrector* corrector, size_t* offsets, int n);
+MSX_API int msx_corrector_forward(msx_corrector* corrector, const float* features_dev, int samples, float* maps_out_dev,
+                                  void* stream);
+MSX_API int msx_corrector_backward(msx_corrector* corrector, const float* dmaps_dev, void* stream);
 MSX_API int msx_corrector_adam(msx_corrector* corrector, float lr, float beta1, float beta2, float eps, void* stream);
+MSX_API int msx_corrector_check(msx_corrector* corrector);
+MSX_API int msx_corrector_features(const float* pot_dev, int samples, int ratio, int ny, int nx, float sigma,
+                                   float tval, float* features_out_dev, void* stream);
+MSX_API int msx_corrector_apply_map(float* waves_dev, int num, int ny, int nx, const float* maps_dev, int which,
+                                    int conj, void* stream);
+MSX_API int msx_corrector_mul_plane(float* waves_dev, int num, int ny, int nx, const float* plane_dev, int conj,
+                                    void* stream);
+MSX_API int msx_corrector_map_trans(const float* trans_dev, int ny, int nx, const float* maps_dev, int which,
+                                    float* out_dev, void* stream);
+MSX_API int msx_corrector_map_grad(const float* u_dev, const float* g_dev, int num, int ny, int nx, int which,
+                                   int accumulate, float* dmaps_dev, void* stream);
+MSX_API int msx_corrector_residual(const float* psi_dev, const float* target_dev, int num, int ny, int nx, float weight,
+                                   int accumulate, float* adjoint_dev, float* loss_out_dev, void* stream);
 
 /*
  * Autotuner: times every (row schedule, column schedule, group size) of the

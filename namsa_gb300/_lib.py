@@ -67,17 +67,31 @@ SIGNATURES = [
     ('msx_batch_run', _c.c_int, [_vp, _vp, _c.c_int, _vp]),
     ('msx_batch_autotune', _c.c_int, [_vp, _vp, _c.c_int, _c.c_int, _vp]),
     ('msx_batch_check', _c.c_int, [_vp]),
+    ('msx_gemm_bf16', _c.c_int, [_vp, _c.c_int, _vp, _c.c_int, _c.c_int, _c.c_int, _c.c_int, _vp, _c.c_int, _vp,
+                                 _c.c_int, _vp]),
+    ('msx_gemm_check', _c.c_int, []),
     ('msx_tc_dft', _c.c_int, [_vp, _c.c_int, _c.c_int, _c.c_int, _vp, _vp]),
     ('msx_step_waves_tc', _c.c_int, [_vp, _c.c_int, _c.c_int, _vp, _vp, _vp]),
     ('msx_tc_set_compensation', _c.c_int, [_c.c_int]),
     ('msx_tc_check', _c.c_int, []),
     ('msx_selftest_wait', _c.c_int, [_c.c_int, _c.c_int, _c.c_void_p]),
-    ('msx_corrector_create', _c.c_int, [_c.c_int, _c.c_int, _c.c_int, _c.c_int, _c.c_int, _c.POINTER(_vp)]),
+    ('msx_corrector_create', _c.c_int, [_c.c_int, _c.c_int, _c.c_int, _c.c_int, _c.c_int, _c.c_int, _c.c_int,
+                                        _c.c_int, _c.POINTER(_vp)]),
     ('msx_corrector_destroy', _c.c_int, [_vp]),
     ('msx_corrector_params', _c.c_int, [_vp, _c.POINTER(_vp), _c.POINTER(_vp), _c.POINTER(_c.c_size_t)]),
-    ('msx_corrector_forward', _c.c_int, [_vp, _vp, _vp, _c.c_int, _vp, _vp]),
-    ('msx_corrector_loss_grad', _c.c_int, [_vp, _vp, _vp, _vp, _c.c_int, _c.c_double, _vp, _vp, _vp]),
+    ('msx_corrector_layout', _c.c_int, [_vp, _c.POINTER(_c.c_size_t), _c.c_int]),
+    ('msx_corrector_forward', _c.c_int, [_vp, _vp, _c.c_int, _vp, _vp]),
+    ('msx_corrector_backward', _c.c_int, [_vp, _vp, _vp]),
     ('msx_corrector_adam', _c.c_int, [_vp, _c.c_float, _c.c_float, _c.c_float, _c.c_float, _vp]),
+    ('msx_corrector_check', _c.c_int, [_vp]),
+    ('msx_corrector_features', _c.c_int, [_vp, _c.c_int, _c.c_int, _c.c_int, _c.c_int, _c.c_float, _c.c_float, _vp,
+                                          _vp]),
+    ('msx_corrector_apply_map', _c.c_int, [_vp, _c.c_int, _c.c_int, _c.c_int, _vp, _c.c_int, _c.c_int, _vp]),
+    ('msx_corrector_mul_plane', _c.c_int, [_vp, _c.c_int, _c.c_int, _c.c_int, _vp, _c.c_int, _vp]),
+    ('msx_corrector_map_trans', _c.c_int, [_vp, _c.c_int, _c.c_int, _vp, _c.c_int, _vp, _vp]),
+    ('msx_corrector_map_grad', _c.c_int, [_vp, _vp, _c.c_int, _c.c_int, _c.c_int, _c.c_int, _c.c_int, _vp, _vp]),
+    ('msx_corrector_residual', _c.c_int, [_vp, _vp, _c.c_int, _c.c_int, _c.c_int, _c.c_float, _c.c_int, _vp, _vp,
+                                          _vp]),
     ('msx_plan_autotune', _c.c_int, [_vp, _vp, _c.c_int, _vp, _vp, _vp, _c.c_int, _c.c_float, _c.c_double,
                                      _c.c_double, _c.c_float, _c.c_int, _c.c_size_t, _c.POINTER(_c.c_float), _vp]),
     ('msx_plan_profile', _c.c_int, [_vp, _vp, _c.c_int, _vp, _vp, _vp, _c.c_int, _c.c_float, _c.c_double,

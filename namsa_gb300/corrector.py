@@ -1,16 +1,29 @@
-"""Learned coarse-slice corrector: training data, training and corrected multislice.
+"""Learned coarse-slice corrector: data, rollout training and corrected multislice.
 
-A coarse step propagates through one slice four times as thick as the fine
-one (the transmission of four fine slices and the Fresnel propagator of
-their summed thickness).  It is four times cheaper but its splitting error
-grows with the thickness.  The corrector network (``engine.Corrector``,
-kernels in csrc/msx_corrector.cu) maps the wave after a coarse step, together
-with that step's transmission, to the wave after the four fine steps.  Plain
-fine-slice multislice generates the training pairs on the device and judges
-the corrected result.
+A coarse step propagates through one slice ``ratio`` (4) times as thick as the
+fine one: the transmission of the fine slices it contains and the Fresnel
+propagator of their summed thickness.  It costs a quarter of the fine steps
+but its splitting error grows with the thickness.  The corrected coarse step is
 
-Waves handed to the network are scaled to unit mean intensity per pixel
-(multiplied by sqrt(N / norm), norm = sum |psi_0|^2).
+    psi <- (1 + A_k) ifft2(P_c fft2((1 + B_k) t_k psi))
+
+with per-pixel complex maps A_k, B_k that the corrector network
+(``engine.Corrector``, csrc/msx_corrector.cu) computes from the potentials of
+the fine slices inside coarse slice k.  The maps depend on the crystal only, so
+they fold into the transmission slices of a plain multislice run:
+
+    t'_0 = (1 + B_0) t_0,  t'_k = (1 + A_{k-1})(1 + B_k) t_k,  t'_S = 1 + A_{S-1}
+
+(the extra last slice only multiplies; its propagator phase does not change
+the CBED).  The corrected multislice of every probe position therefore runs
+through ``Plan.multislice`` at the cost of a coarse-slice run.
+
+Training follows the corrector's own rollouts: a window of K corrected coarse
+steps from a fine-slice wave, loss = sum over steps of the relative squared
+error against the fine-slice waves at the same depth, back-propagated through
+the engine's slice step (``Plan.step_waves``; the adjoint step is the same
+transform with the conjugate propagator) into the maps and the network.
+Plain fine-slice multislice generates the targets and judges the result.
 """
 from __future__ import annotations
 
@@ -25,153 +38,217 @@ from .msa import MSAGPU
 
 PROBE = {'smooth_apert': True, 'apert_smooth': 50, 'spherical_phase': True,
          'aberration_dict': {'C1': 0., 'C3': 0., 'C5': 0.}, 'scherzer': False}
+RATIO = 4
 
 
-def init_params(C, L, seed=0, K=8):
-    """Seeded initial parameters in the library's layout: fan-in scaled linear
-    maps, spectral weights ~ 1/C, and a zero output layer (the untrained
-    network returns the coarse wave exactly)."""
+def init_params(net, seed=0, out_scale=1e-2, spec_scale=0.5):
+    """Seeded initial parameters in the library's layout (engine.Corrector.views):
+    fan-in scaled weights, spectral weights ~ spec_scale / C, zero biases and a
+    small output layer, so the untrained maps are close to zero."""
     rng = np.random.default_rng(seed)
-    parts = [rng.standard_normal((C, 4)) / 2.0, np.zeros(C)]
-    for _ in range(L):
-        parts += [rng.standard_normal((K, K, C, C)) / C, rng.standard_normal((K, K, C, C)) / C,
-                  rng.standard_normal((C, C)) / math.sqrt(C), np.zeros(C)]
-    parts += [rng.standard_normal((C, C)) / math.sqrt(C), np.zeros(C),
-              np.zeros((2, C)), np.zeros(2)]
-    return np.concatenate([p.ravel() for p in parts]).astype(np.float32)
+    flat = np.zeros(net.count, np.float32)
+    v = net.views(torch.from_numpy(flat))
+    C, Ci = net.channels, net.in_channels
+    for name, t in v.items():
+        if name[0] in 'bc':
+            continue
+        if name == 'W0':
+            val = rng.standard_normal(t.shape) / math.sqrt(Ci)
+        elif name.startswith('R'):
+            val = rng.standard_normal(t.shape) * spec_scale / C
+        elif name == 'P2':
+            val = rng.standard_normal(t.shape) * out_scale / math.sqrt(C)
+        else:
+            val = rng.standard_normal(t.shape) / math.sqrt(C)
+        t.copy_(torch.from_numpy(val.astype(np.float32)))
+    return flat
 
 
 class Crystal:
-    """A crystal prepared at fine and coarse slicing on one grid."""
+    """A crystal prepared at fine and coarse slicing on one grid, with the fine
+    potentials the corrector reads."""
 
-    def __init__(self, sites, n, slice_t, kv=200, semi_angle=20e-3, device=None, ratio=4):
+    def __init__(self, sites, n, slice_t, kv=200, semi_angle=20e-3, device=None, ratio=RATIO):
         self.sim = MSAGPU(kv, semi_angle, sites, sampling=np.array([n, n]), debye_waller=False)
         dev = device or torch.device('cuda', torch.cuda.current_device())
         self.sim.setup_device(dev.index if dev.index is not None else 0)
         self.sim.calc_atomic_potentials()
         self.sim.build_potential_slices(ratio * slice_t)
         self.trans_coarse = self.sim.trans
-        self.sim.build_potential_slices(slice_t)
+        self.sim.build_potential_slices(slice_t, keep_potential=True)
         self.trans_fine = self.sim.trans
+        self.pot_fine = self.sim.potential
         self.sim.build_probe(PROBE)
         self.n, self.ratio, self.slice_t = n, ratio, slice_t
-        self.coarse_steps = self.trans_coarse.shape[0]
+        self.coarse_steps = min(self.trans_coarse.shape[0], self.trans_fine.shape[0] // ratio)
         kmax = np.float32(self.sim.kmax)
         kband = np.float32(self.sim.kmax / 3)
-        self.kmax = kmax
+        self.kmax, self.kband = kmax, kband
         self.ptab_fine = engine.propagator_table(n, n, kmax, self.sim.Lambda, slice_t, kband)
         self.ptab_coarse = engine.propagator_table(n, n, kmax, self.sim.Lambda, ratio * slice_t, kband)
-        self.scale = math.sqrt(n * n / self.sim.normalization)
+        self.ptab_coarse_adj = torch.conj(self.ptab_coarse).contiguous()
+        self.ones = torch.ones((n, n), dtype=torch.complex64, device=self.trans_fine.device)
         self.plan = engine.Plan(n, n)
+        self._features = None
+
+    def features(self):
+        """Network inputs of every coarse slice (S, n, n, ratio + 2): sigma V of its fine
+        slices, their sum, and the fine slice thickness in Angstrom / 2."""
+        if self._features is None:
+            pot = self.pot_fine[:self.ratio * self.coarse_steps].contiguous()
+            self._features = engine.corrector_features(pot, self.ratio, float(self.sim.sigma), self.slice_t / 2.0)
+        return self._features
 
     def waves(self, positions):
         pos = torch.as_tensor(np.asarray(positions, np.float32), device=self.trans_fine.device)
         return self.plan.probe_waves(self.sim.psi_k_dev, pos, self.kmax)
 
-    def pairs(self, positions, steps=None):
-        """(psi_coarse, psi_fine, coarse-slice index) for every coarse step of every
-        position, scaled to unit mean intensity."""
-        w = self.waves(positions)
+    def trajectory(self, positions, steps=None):
+        """Fine-slice waves at every coarse boundary: (steps + 1, P, n, n) complex64."""
         steps = self.coarse_steps if steps is None else min(steps, self.coarse_steps)
-        out_c, out_f, idx = [], [], []
+        w = self.waves(positions)
+        out = torch.empty((steps + 1,) + tuple(w.shape), dtype=torch.complex64, device=w.device)
+        out[0] = w
         for k in range(steps):
-            c = w.clone()
-            self.plan.step_waves(c, self.trans_coarse[k], self.ptab_coarse)
             for j in range(self.ratio * k, self.ratio * (k + 1)):
                 self.plan.step_waves(w, self.trans_fine[j], self.ptab_fine)
-            out_c.append(c * self.scale)
-            out_f.append(w * self.scale)
-            idx.append(torch.full((w.shape[0],), k, dtype=torch.long, device=w.device))
-        return torch.cat(out_c), torch.cat(out_f), torch.cat(idx)
+            out[k + 1] = w
+        return out
+
+    def effective_slices(self, maps):
+        """Transmission slices of the corrected multislice (S + 1, n, n) from the maps (S, n, n, 4)."""
+        S = maps.shape[0]
+        out = torch.empty((S + 1, self.n, self.n), dtype=torch.complex64, device=maps.device)
+        for k in range(S):
+            engine.map_trans(self.trans_coarse[k], maps[k], 1, out=out[k])
+            if k > 0:
+                engine.map_trans(out[k].clone(), maps[k - 1], 0, out=out[k])
+        engine.map_trans(self.ones, maps[S - 1], 0, out=out[S])
+        return out
 
 
-def training_crystals(n=256, seed=0, random_count=6):
-    """Si [001], SrTiO3 [001] and seeded random cubic crystals on an n x n grid,
-    about 1000 Angstrom thick."""
-    rng = np.random.default_rng(seed)
-    cells = max(1, int(round(n * 0.085 / 5.431)))
-    out = [('Si[001]', structures.silicon((cells, cells, 184)), 5.431 / 4, 5.431)]
-    cs = max(1, int(round(n * 0.085 / 3.905)))
-    out.append(('SrTiO3[001]', structures.srtio3((cs, cs, 256)), 3.905 / 2, 3.905))
-    for i in range(random_count):
-        basis, species, a = structures.random_cubic(rng)
-        m = max(1, int(round(n * 0.1 / a)))
-        nz = int(math.ceil(1000.0 / a))
-        out.append((f'random{i}', structures.tile(basis, species, (m, m, nz), a), float(rng.uniform(1.0, 2.0)), a))
+def crystal_maps(net, crystal):
+    """Correction maps of every coarse slice of a crystal (the network runs once per slice)."""
+    f = crystal.features()
+    S = f.shape[0]
+    out = torch.empty((S, crystal.n, crystal.n, 4), dtype=torch.float32, device=f.device)
+    for s0 in range(0, S, net.max_samples):
+        net.forward(f[s0:s0 + net.max_samples].contiguous(), out=out[s0:s0 + net.max_samples])
     return out
 
 
-def train(net, data_c, data_f, data_t, steps, batch, lr=1e-3, seed=0, log=None):
-    """Adam on random batches of pairs; every pair is weighted by the inverse of its
-    own coarse error, so the loss is the mean ratio (corrected error / coarse error)
-    and 1 means no gain.  Returns the per-step losses."""
-    g = torch.Generator(device='cpu').manual_seed(seed)
-    n = data_c.shape[0]
-    losses = []
-    for s in range(steps):
-        idx = torch.randint(0, n, (batch,), generator=g).to(data_c.device)
-        c, f, t = data_c[idx].contiguous(), data_f[idx].contiguous(), data_t[idx].contiguous()
-        w = 1.0 / (f - c).abs().pow(2).sum((1, 2)).clamp_min(1e-20).float()
-        loss = net.loss_grad(c, t, f, float(batch), weights=w.contiguous())
-        net.adam(lr=lr * (0.5 * (1 + math.cos(math.pi * s / steps))))
-        losses.append(float(loss.item()))
-        if log and s % 100 == 0:
-            log(f'step {s} loss {losses[-1]:.4f}')
-    return losses
-
-
-def rollout_pairs(net, crystal, positions, steps=None):
-    """Pairs taken along the corrector's own trajectory: at every coarse step the
-    target is four fine steps from the current corrected wave.  Training on them
-    teaches the network the states it meets when it is applied repeatedly."""
-    w = crystal.waves(positions)
-    steps = crystal.coarse_steps if steps is None else min(steps, crystal.coarse_steps)
-    out_c, out_f, idx = [], [], []
-    B = w.shape[0]
-    for k in range(steps):
-        c = w.clone()
-        crystal.plan.step_waves(c, crystal.trans_coarse[k], crystal.ptab_coarse)
-        f = w.clone()
-        for j in range(crystal.ratio * k, crystal.ratio * (k + 1)):
-            crystal.plan.step_waves(f, crystal.trans_fine[j], crystal.ptab_fine)
-        cs, fs = c * crystal.scale, f * crystal.scale
-        out_c.append(cs)
-        out_f.append(fs)
-        idx.append(torch.full((B,), k, dtype=torch.long, device=w.device))
-        nxt = torch.empty_like(cs)
-        for b0 in range(0, B, net.max_batch):
-            chunk = cs[b0:b0 + net.max_batch].contiguous()
-            tc = crystal.trans_coarse[k].expand(chunk.shape[0], -1, -1).contiguous()
-            nxt[b0:b0 + net.max_batch] = net.forward(chunk, tc)
-        w = (nxt / crystal.scale).contiguous()
-    return torch.cat(out_c), torch.cat(out_f), torch.cat(idx)
-
-
-def corrected_multislice(net, crystal, positions, steps=None, use_net=True):
-    """CBED of coarse-step multislice with (or without) the corrector."""
-    w = crystal.waves(positions) * crystal.scale
+def corrected_multislice(net, crystal, positions, steps=None, maps=None, trans=None):
+    """CBED of the corrected coarse-slice multislice through `steps` coarse slices,
+    run by Plan.multislice on the effective transmission slices."""
     steps = crystal.coarse_steps if steps is None else steps
-    B = w.shape[0]
-    for k in range(steps):
-        crystal.plan.step_waves(w, crystal.trans_coarse[k], crystal.ptab_coarse)
-        if use_net:
-            for b0 in range(0, B, net.max_batch):
-                chunk = w[b0:b0 + net.max_batch].contiguous()
-                tc = crystal.trans_coarse[k].expand(chunk.shape[0], -1, -1).contiguous()
-                w[b0:b0 + net.max_batch] = net.forward(chunk, tc)
-    w = (w / crystal.scale).contiguous()
-    return crystal.plan.cbed_waves(w, crystal.sim.norm_dev)
+    if trans is None:
+        maps = crystal_maps(net, crystal) if maps is None else maps
+        trans = crystal.effective_slices(maps[:steps].contiguous())
+    sim = crystal.sim
+    pos = torch.as_tensor(np.asarray(positions, np.float32), device=crystal.trans_fine.device)
+    return crystal.plan.multislice(trans, sim.psi_k_dev, sim.norm_dev, pos, crystal.kmax, sim.Lambda,
+                                   crystal.ratio * crystal.slice_t, crystal.kband)
+
+
+def coarse_multislice(crystal, positions, steps=None):
+    """CBED of plain coarse-slice multislice through `steps` coarse slices."""
+    steps = crystal.coarse_steps if steps is None else steps
+    sim = crystal.sim
+    pos = torch.as_tensor(np.asarray(positions, np.float32), device=crystal.trans_fine.device)
+    return crystal.plan.multislice(crystal.trans_coarse[:steps].contiguous(), sim.psi_k_dev, sim.norm_dev, pos,
+                                   crystal.kmax, sim.Lambda, crystal.ratio * crystal.slice_t, crystal.kband)
 
 
 def fine_multislice(crystal, positions, steps=None):
-    """CBED of plain fine-slice multislice (the fused engine path) through the
-    same thickness as `steps` coarse steps."""
+    """CBED of plain fine-slice multislice (the error reference) through the same
+    thickness as `steps` coarse steps."""
     steps = crystal.coarse_steps if steps is None else steps
     sim = crystal.sim
     pos = torch.as_tensor(np.asarray(positions, np.float32), device=crystal.trans_fine.device)
     trans = crystal.trans_fine[:crystal.ratio * steps].contiguous()
     return crystal.plan.multislice(trans, sim.psi_k_dev, sim.norm_dev, pos, crystal.kmax, sim.Lambda,
-                                   crystal.slice_t, np.float32(sim.kmax / 3))
+                                   crystal.slice_t, crystal.kband)
+
+
+class RolloutTrainer:
+    """Windowed rollout training of a corrector over a set of crystals."""
+
+    def __init__(self, net, crystals, trajectories, window=8, waves=8, seed=0):
+        self.net, self.crystals, self.traj = net, crystals, trajectories
+        self.K, self.B = window, waves
+        self.rng = np.random.default_rng(seed)
+        n = crystals[0].n
+        dev = crystals[0].trans_fine.device
+        self.loss_buf = torch.zeros(1, dtype=torch.float32, device=dev)
+        self.n = n
+
+    def step(self, lr, windows=2):
+        """One Adam step on `windows` random rollout windows; returns the mean relative error per step."""
+        net, K, B = self.net, self.K, self.B
+        picks = []
+        for _ in range(windows):
+            c = int(self.rng.integers(len(self.crystals)))
+            cr, tr = self.crystals[c], self.traj[c]
+            k0 = int(self.rng.integers(0, tr.shape[0] - K))
+            b = torch.as_tensor(self.rng.choice(tr.shape[1], size=min(B, tr.shape[1]), replace=False),
+                                device=tr.device)
+            picks.append((cr, tr, k0, b))
+        feats = torch.cat([cr.features()[k0:k0 + K] for cr, tr, k0, b in picks]).contiguous()
+        maps = net.forward(feats)
+        dmaps = torch.zeros_like(maps)
+        total = 0.0
+        for w, (cr, tr, k0, b) in enumerate(picks):
+            total += self._window(cr, tr, k0, b, maps[w * K:(w + 1) * K], dmaps[w * K:(w + 1) * K])
+        net.backward(dmaps)
+        net.adam(lr=lr)
+        return total / (windows * K)
+
+    def _window(self, cr, tr, k0, b, maps, dmaps):
+        K, n = self.K, self.n
+        psi = tr[k0][b].contiguous()
+        nb = psi.shape[0]
+        tb = torch.empty((K, n, n), dtype=torch.complex64, device=psi.device)
+        w_in = torch.empty((K, nb, n, n), dtype=torch.complex64, device=psi.device)   # t_k psi_k
+        u = torch.empty_like(w_in)                                                      # before (1 + A)
+        adj = torch.zeros((K + 1, nb, n, n), dtype=torch.complex64, device=psi.device)  # loss adjoints
+        loss = 0.0
+        for k in range(K):
+            s = k0 + k
+            engine.map_trans(cr.trans_coarse[s], maps[k], 1, out=tb[k])
+            w_in[k].copy_(psi)
+            engine.mul_plane(w_in[k], cr.trans_coarse[s])
+            cr.plan.step_waves(psi, tb[k], cr.ptab_coarse)
+            u[k].copy_(psi)
+            engine.apply_map(psi, maps[k], 0)
+            target = tr[s + 1][b].contiguous()
+            denom = float(target.abs().pow(2).sum().item())
+            engine.residual(psi, target, 1.0 / (K * denom), adj[k + 1], self.loss_buf)
+            loss += float(self.loss_buf.item()) * K
+        g = adj[K].clone()
+        for k in range(K - 1, -1, -1):
+            engine.map_grad(u[k], g, 0, dmaps[k])
+            engine.apply_map(g, maps[k], 0, conj=True)
+            cr.plan.step_waves(g, cr.ones, cr.ptab_coarse_adj)
+            engine.map_grad(w_in[k], g, 1, dmaps[k], accumulate=True)
+            engine.mul_plane(g, tb[k], conj=True)
+            if k > 0:
+                g += adj[k]
+        return loss
+
+
+def training_crystals(n=256, seed=0, random_count=6, thickness=1000.0):
+    """Si [001], SrTiO3 [001] and seeded random cubic crystals on an n x n grid."""
+    rng = np.random.default_rng(seed)
+    cells = max(1, int(round(n * 0.085 / 5.431)))
+    out = [('Si[001]', structures.silicon((cells, cells, int(math.ceil(thickness / 5.431)))), 5.431 / 4, 5.431)]
+    cs = max(1, int(round(n * 0.085 / 3.905)))
+    out.append(('SrTiO3[001]', structures.srtio3((cs, cs, int(math.ceil(thickness / 3.905)))), 3.905 / 2, 3.905))
+    for i in range(random_count):
+        basis, species, a = structures.random_cubic(rng)
+        m = max(1, int(round(n * 0.1 / a)))
+        nz = int(math.ceil(thickness / a))
+        out.append((f'random{i}', structures.tile(basis, species, (m, m, nz), a), float(rng.uniform(1.0, 2.0)), a))
+    return out
 
 
 def rel_l2(a, b):

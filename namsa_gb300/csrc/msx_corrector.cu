@@ -1,20 +1,28 @@
-// Learned coarse-slice corrector: a spectral-convolution network that maps the
-// wave after one 4x-thick slice (and that slice's transmission) to the wave
-// four fine slices would give.  Forward, backward and the Adam update are
-// hand-written kernels; the host drives them from msx_corrector_* below.
+// Learned coarse-slice corrector: a spectral-convolution network that turns
+// the potentials of the fine slices inside one thick (coarse) slice into two
+// per-pixel complex correction maps A, B of the coarse multislice step
 //
-// Network (C channels, L layers, K x K retained Fourier modes):
-//   x0 = [Re psi_c, Im psi_c, Re t_c, Im t_c]                       (4 channels)
-//   a0 = W0 x0 + b0
-//   a_l = gelu( Spec_l(a_{l-1}) + W_l a_{l-1} + b_l ),  l = 1..L
-//       Spec(u)[o] = Re( IDFT_K( sum_i R[k][o][i] DFT_K(u)[i][k] ) ) / (H W)
-//       DFT_K keeps the K x K lowest modes (frequencies -K/2 .. K/2-1 per axis)
-//   h  = gelu(P1 a_L + c1);  o = P2 h + c2                          (2 channels)
-//   psi_pred = psi_c + (o_0 + i o_1)
-// Waves are scaled by sqrt(H W) by the caller so that they are O(1).
-// Loss: sum_b w_b sum |psi_pred - psi_f|^2 / denom (w_b = 1 without sample
-// weights).  gelu is the tanh form.
-// All arithmetic is FP32; reductions over pixels are two-stage and ordered.
+//   psi <- (1 + A) . IFFT[ P_c . FFT[ (1 + B) . t_c . psi ] ]
+//
+// so that one corrected coarse step follows `ratio` fine steps more closely
+// than the plain coarse step does.  The maps depend on the crystal only, so
+// the network runs once per coarse slice; the corrected multislice of every
+// probe then costs what a plain coarse-slice multislice costs (the maps fold
+// into the transmission slices).
+//
+// Network (C channels, L spectral layers, MX x MY retained modes), all
+// activations pixel-major (S, H, W, channels) float32:
+//   a_0 = x W0^T + b0                                   (lift of Cin input channels)
+//   a_l = gelu( Spec_l(a_{l-1}) + a_{l-1} W_l^T + b_l ), l = 1..L
+//         Spec(u) = IDFT( R[mode] . DFT(u) ) on the modes kx in [0, MX),
+//         ky in [-MY/2, MY/2) (real fields: kx >= 1 counted twice)
+//   h   = gelu(a_L P1^T + c1);  o = h P2^T + c2            (4 outputs: Re A, Im A, Re B, Im B)
+// Every contraction -- the lift, the pointwise layers, the head, their weight
+// gradients and the four partial-DFT stages of each spectral layer -- is a
+// bfloat16 GEMM with FP32 accumulation on the tensor cores (TcGemm,
+// msx_tcgemm.cu); the per-mode channel mixing (a C x C complex product per
+// mode, 0.3 % of the layer's multiply-adds), the activations and Adam are
+// FP32 kernels here.  gelu is the tanh form.
 #include "msx.h"
 #include "msx_internal.h"
 
@@ -25,148 +33,11 @@
 namespace msx {
 namespace nn {
 
-constexpr int kMaxC = 32;
-constexpr int kK = 8;  // retained modes per axis
-
-__device__ __forceinline__ float gelu_f(float z) {
-  const float k = 0.7978845608028654f;  // sqrt(2/pi)
-  const float u = k * (z + 0.044715f * z * z * z);
-  return 0.5f * z * (1.f + tanhf(u));
-}
 __device__ __forceinline__ float gelu_d(float z) {
   const float k = 0.7978845608028654f;
   const float u = k * (z + 0.044715f * z * z * z);
   const float th = tanhf(u);
   return 0.5f * (1.f + th) + 0.5f * z * (1.f - th * th) * k * (1.f + 3.f * 0.044715f * z * z);
-}
-
-// mode index m (0..K-1) -> frequency -K/2..K/2-1 mapped into [0, N)
-__host__ __device__ __forceinline__ int mode_freq(int m, int n) { return m < kK / 2 ? m : n - (kK - m); }
-
-// x0 from the interleaved complex inputs: x0[b][0..3][p]
-__global__ void inputs_kernel(const float2* __restrict__ psi_c, const float2* __restrict__ tc, int HW, int B,
-                              float* __restrict__ x0) {
-  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= (long long)B * HW) return;
-  const int b = (int)(i / HW), p = (int)(i % HW);
-  const float2 w = psi_c[i], t = tc[i];
-  float* o = x0 + (size_t)b * 4 * HW + p;
-  o[0] = w.x;
-  o[HW] = w.y;
-  o[2 * HW] = t.x;
-  o[3 * HW] = t.y;
-}
-
-// z[b][o][p] = sum_i Wm[o][i] in[b][i][p] + bias[o] (+ add[b][o][p]); optional a = gelu(z)
-__global__ void linear_fwd_kernel(const float* __restrict__ in, int Cin, const float* __restrict__ Wm,
-                                  const float* __restrict__ bias, int Cout, int HW, int B, const float* __restrict__ add,
-                                  float* __restrict__ z, float* __restrict__ a) {
-  __shared__ float sw[kMaxC * kMaxC + kMaxC];
-  for (int k = threadIdx.x; k < Cout * Cin; k += blockDim.x) sw[k] = Wm[k];
-  for (int k = threadIdx.x; k < Cout; k += blockDim.x) sw[kMaxC * kMaxC + k] = bias[k];
-  __syncthreads();
-  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= (long long)B * HW) return;
-  const int b = (int)(i / HW), p = (int)(i % HW);
-  float x[kMaxC];
-  const float* ip = in + (size_t)b * Cin * HW + p;
-#pragma unroll
-  for (int c = 0; c < kMaxC; ++c)
-    if (c < Cin) x[c] = ip[(size_t)c * HW];
-  for (int o = 0; o < Cout; ++o) {
-    float s = sw[kMaxC * kMaxC + o];
-#pragma unroll
-    for (int c = 0; c < kMaxC; ++c)
-      if (c < Cin) s = fmaf(sw[o * Cin + c], x[c], s);
-    const size_t oi = ((size_t)b * Cout + o) * HW + p;
-    if (add) s += add[oi];
-    z[oi] = s;
-    if (a) a[oi] = gelu_f(s);
-  }
-}
-
-// din[b][i][p] (+)= sum_o Wm[o][i] dz[b][o][p]
-__global__ void linear_bwd_data_kernel(const float* __restrict__ dz, int Cout, const float* __restrict__ Wm, int Cin,
-                                       int HW, int B, int accumulate, float* __restrict__ din) {
-  __shared__ float sw[kMaxC * kMaxC];
-  for (int k = threadIdx.x; k < Cout * Cin; k += blockDim.x) sw[k] = Wm[k];
-  __syncthreads();
-  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= (long long)B * HW) return;
-  const int b = (int)(i / HW), p = (int)(i % HW);
-  float g[kMaxC];
-#pragma unroll
-  for (int o = 0; o < kMaxC; ++o)
-    if (o < Cout) g[o] = dz[((size_t)b * Cout + o) * HW + p];
-  for (int c = 0; c < Cin; ++c) {
-    float s = 0.f;
-#pragma unroll
-    for (int o = 0; o < kMaxC; ++o)
-      if (o < Cout) s = fmaf(sw[o * Cin + c], g[o], s);
-    const size_t oi = ((size_t)b * Cin + c) * HW + p;
-    din[oi] = accumulate ? din[oi] + s : s;
-  }
-}
-
-// Partial weight/bias gradients of one chunk of (b, p): part[chunk][o*Cin+i], part[chunk][Cout*Cin+o].
-// 256 threads; thread t owns the (o, i) pairs t, t+256, ...
-__global__ void linear_bwd_weight_kernel(const float* __restrict__ dz, int Cout, const float* __restrict__ in, int Cin,
-                                         int HW, int B, int chunk, float* __restrict__ part) {
-  __shared__ float sg[32][kMaxC];
-  __shared__ float sx[32][kMaxC];
-  const long long total = (long long)B * HW;
-  const long long start = (long long)blockIdx.x * chunk;
-  const long long end = start + chunk < total ? start + chunk : total;
-  const int npair = Cout * Cin + Cout;
-  float acc[(kMaxC * kMaxC + kMaxC + 255) / 256];
-#pragma unroll
-  for (int k = 0; k < (kMaxC * kMaxC + kMaxC + 255) / 256; ++k) acc[k] = 0.f;
-  for (long long q0 = start; q0 < end; q0 += 32) {
-    // stage 32 pixels of dz and in
-    for (int e = threadIdx.x; e < 32 * kMaxC; e += blockDim.x) {
-      const int j = e / kMaxC, c = e % kMaxC;
-      const long long q = q0 + j;
-      float gv = 0.f, xv = 0.f;
-      if (q < end) {
-        const int b = (int)(q / HW), p = (int)(q % HW);
-        if (c < Cout) gv = dz[((size_t)b * Cout + c) * HW + p];
-        if (c < Cin) xv = in[((size_t)b * Cin + c) * HW + p];
-      }
-      sg[j][c] = gv;
-      sx[j][c] = xv;
-    }
-    __syncthreads();
-#pragma unroll
-    for (int k = 0; k < (kMaxC * kMaxC + kMaxC + 255) / 256; ++k) {
-      const int pr = threadIdx.x + 256 * k;
-      if (pr < npair) {
-        float s = acc[k];
-        if (pr < Cout * Cin) {
-          const int o = pr / Cin, c = pr % Cin;
-          for (int j = 0; j < 32; ++j) s = fmaf(sg[j][o], sx[j][c], s);
-        } else {
-          const int o = pr - Cout * Cin;
-          for (int j = 0; j < 32; ++j) s += sg[j][o];
-        }
-        acc[k] = s;
-      }
-    }
-    __syncthreads();
-  }
-#pragma unroll
-  for (int k = 0; k < (kMaxC * kMaxC + kMaxC + 255) / 256; ++k) {
-    const int pr = threadIdx.x + 256 * k;
-    if (pr < npair) part[(size_t)blockIdx.x * npair + pr] = acc[k];
-  }
-}
-
-// grad[j] (+)= sum over chunks of part[chunk][j], chunks in order
-__global__ void reduce_parts_kernel(const float* __restrict__ part, int nchunks, int n, float* __restrict__ grad) {
-  const int j = blockIdx.x * blockDim.x + threadIdx.x;
-  if (j >= n) return;
-  float s = 0.f;
-  for (int k = 0; k < nchunks; ++k) s += part[(size_t)k * n + j];
-  grad[j] = s;
 }
 
 __global__ void gelu_bwd_kernel(const float* __restrict__ da, const float* __restrict__ z, long long n,
@@ -175,193 +46,85 @@ __global__ void gelu_bwd_kernel(const float* __restrict__ da, const float* __res
   if (i < n) dz[i] = da[i] * gelu_d(z[i]);
 }
 
-// out[r][m] = scale * sum_x in[r][x] e^{-2 pi i f_m x / W}, rows r of real input.  One warp per row.
-__global__ void dft_x_kernel(const float* __restrict__ in, long long rows, int W, float scale, float2* __restrict__ out) {
-  const long long r = (long long)blockIdx.x * (blockDim.x / 32) + (threadIdx.x >> 5);
-  const int lane = threadIdx.x & 31;
-  if (r >= rows) return;
-  const float* row = in + (size_t)r * W;
-  float re[kK], im[kK];
-#pragma unroll
-  for (int m = 0; m < kK; ++m) re[m] = im[m] = 0.f;
-  for (int x = lane; x < W; x += 32) {
-    const float v = row[x];
-#pragma unroll
-    for (int m = 0; m < kK; ++m) {
-      float s, c;
-      sincospif(-2.f * (float)((long long)mode_freq(m, W) * x % W) / (float)W, &s, &c);
-      re[m] = fmaf(v, c, re[m]);
-      im[m] = fmaf(v, s, im[m]);
-    }
-  }
-#pragma unroll
-  for (int m = 0; m < kK; ++m) {
-    for (int o = 16; o > 0; o >>= 1) {
-      re[m] += __shfl_down_sync(0xffffffffu, re[m], o);
-      im[m] += __shfl_down_sync(0xffffffffu, im[m], o);
-    }
-  }
-  if (lane == 0)
-#pragma unroll
-    for (int m = 0; m < kK; ++m) out[(size_t)r * kK + m] = make_float2(re[m] * scale, im[m] * scale);
-}
-
-// out[q][a][m] = sum_y in[q][y][m] e^{sgn 2 pi i f_a y / H} for the planes q; one warp per (q, m).
-__global__ void dft_y_kernel(const float2* __restrict__ in, long long planes, int H, float sgn, float2* __restrict__ out) {
-  const long long w = (long long)blockIdx.x * (blockDim.x / 32) + (threadIdx.x >> 5);
-  const int lane = threadIdx.x & 31;
-  if (w >= planes * kK) return;
-  const long long q = w / kK;
-  const int m = (int)(w % kK);
-  float re[kK], im[kK];
-#pragma unroll
-  for (int a = 0; a < kK; ++a) re[a] = im[a] = 0.f;
-  for (int y = lane; y < H; y += 32) {
-    const float2 v = in[((size_t)q * H + y) * kK + m];
-#pragma unroll
-    for (int a = 0; a < kK; ++a) {
-      float s, c;
-      sincospif(sgn * 2.f * (float)((long long)mode_freq(a, H) * y % H) / (float)H, &s, &c);
-      re[a] += v.x * c - v.y * s;
-      im[a] += v.x * s + v.y * c;
-    }
-  }
-#pragma unroll
-  for (int a = 0; a < kK; ++a) {
-    for (int o = 16; o > 0; o >>= 1) {
-      re[a] += __shfl_down_sync(0xffffffffu, re[a], o);
-      im[a] += __shfl_down_sync(0xffffffffu, im[a], o);
-    }
-  }
-  if (lane == 0)
-#pragma unroll
-    for (int a = 0; a < kK; ++a) out[((size_t)q * kK + a) * kK + m] = make_float2(re[a], im[a]);
-}
-
-// out[q][y][m] = sum_a in[q][a][m] e^{+2 pi i f_a y / H}; one thread per (q, y, m)
-__global__ void idft_y_kernel(const float2* __restrict__ in, long long planes, int H, float2* __restrict__ out) {
-  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= planes * H * kK) return;
-  const int m = (int)(i % kK);
-  const int y = (int)((i / kK) % H);
-  const long long q = i / ((long long)kK * H);
-  float re = 0.f, im = 0.f;
-#pragma unroll
-  for (int a = 0; a < kK; ++a) {
-    const float2 v = in[((size_t)q * kK + a) * kK + m];
-    float s, c;
-    sincospif(2.f * (float)((long long)mode_freq(a, H) * y % H) / (float)H, &s, &c);
-    re += v.x * c - v.y * s;
-    im += v.x * s + v.y * c;
-  }
-  out[i] = make_float2(re, im);
-}
-
-// v[r][x] (+)= scale * Re( sum_m in[r][m] e^{+2 pi i f_m x / W} ); one thread per (r, x)
-__global__ void idft_x_real_kernel(const float2* __restrict__ in, long long rows, int W, float scale, int accumulate,
-                                   float* __restrict__ v) {
-  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= rows * W) return;
-  const int x = (int)(i % W);
-  const long long r = i / W;
+// Column sums of a (rows x n) row-major matrix, first stage: part[chunk][c] over
+// the chunk's rows.  n divides 256; thread t sums column t % n over rows t / n,
+// t / n + 256 / n, ...; the 256 / n partial sums of a column are then added in order.
+__global__ void colsum_part_kernel(const float* __restrict__ x, long long rows, int n, long long chunk,
+                                   float* __restrict__ part) {
+  __shared__ float red[256];
+  const int t = threadIdx.x, c = t % n, step = 256 / n;
+  const long long r0 = (long long)blockIdx.x * chunk;
+  const long long r1 = r0 + chunk < rows ? r0 + chunk : rows;
   float s = 0.f;
-#pragma unroll
-  for (int m = 0; m < kK; ++m) {
-    const float2 c = in[(size_t)r * kK + m];
-    float sn, cs;
-    sincospif(2.f * (float)((long long)mode_freq(m, W) * x % W) / (float)W, &sn, &cs);
-    s += c.x * cs - c.y * sn;
+  for (long long r = r0 + t / n; r < r1; r += step) s += x[r * n + c];
+  red[t] = s;
+  __syncthreads();
+  if (t < n) {
+    float a = 0.f;
+    for (int j = 0; j < step; ++j) a += red[j * n + t];
+    part[(size_t)blockIdx.x * n + t] = a;
   }
-  s *= scale;
-  v[i] = accumulate ? v[i] + s : s;
 }
 
-// Y[b][o][a][m] = sum_i R[a][m][o][i] X[b][i][a][m]; R as (re, im) planes
-__global__ void mix_fwd_kernel(const float* __restrict__ Rr, const float* __restrict__ Ri, const float2* __restrict__ X,
-                               int C, int B, float2* __restrict__ Y) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= B * C * kK * kK) return;
-  const int am = i % (kK * kK), o = (i / (kK * kK)) % C, b = i / (kK * kK * C);
+// out[j] = sum over chunks k (in order) of part[k][j]
+__global__ void reduce_parts_kernel(const float* __restrict__ part, int nchunks, int n, float* __restrict__ out) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= n) return;
+  float s = 0.f;
+  for (int k = 0; k < nchunks; ++k) s += part[(size_t)k * n + j];
+  out[j] = s;
+}
+
+// Mode mixing.  X, Y: (S, C, NM) complex with NM = MX * MY modes; R: (NM, C, C) complex.
+// Y[s][o][m] = sum_i R[m][o][i] X[s][i][m]
+__global__ void mix_fwd_kernel(const float2* __restrict__ R, const float2* __restrict__ X, int C, int S, int NM,
+                               float2* __restrict__ Y) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= (long long)S * C * NM) return;
+  const int m = (int)(i % NM), o = (int)((i / NM) % C);
+  const long long s = i / ((long long)NM * C);
+  const float2* r = R + ((size_t)m * C + o) * C;
+  const float2* x = X + (size_t)s * C * NM + m;
   float re = 0.f, im = 0.f;
   for (int c = 0; c < C; ++c) {
-    const size_t ri = ((size_t)am * C + o) * C + c;
-    const float2 x = X[((size_t)b * C + c) * kK * kK + am];
-    re += Rr[ri] * x.x - Ri[ri] * x.y;
-    im += Rr[ri] * x.y + Ri[ri] * x.x;
+    const float2 w = __ldg(r + c), v = x[(size_t)c * NM];
+    re = fmaf(w.x, v.x, fmaf(-w.y, v.y, re));
+    im = fmaf(w.x, v.y, fmaf(w.y, v.x, im));
   }
   Y[i] = make_float2(re, im);
 }
 
-// dR[a][m][o][i] = sum_b dY[b][o][a][m] conj(X[b][i][a][m])
-__global__ void mix_bwd_weight_kernel(const float2* __restrict__ dY, const float2* __restrict__ X, int C, int B,
-                                      float* __restrict__ dRr, float* __restrict__ dRi) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= kK * kK * C * C) return;
-  const int c = i % C, o = (i / C) % C, am = i / (C * C);
-  float re = 0.f, im = 0.f;
-  for (int b = 0; b < B; ++b) {
-    const float2 g = dY[((size_t)b * C + o) * kK * kK + am];
-    const float2 x = X[((size_t)b * C + c) * kK * kK + am];
-    re += g.x * x.x + g.y * x.y;
-    im += g.y * x.x - g.x * x.y;
-  }
-  dRr[i] = re;
-  dRi[i] = im;
-}
-
-// dX[b][i][a][m] = sum_o conj(R[a][m][o][i]) dY[b][o][a][m]
-__global__ void mix_bwd_data_kernel(const float* __restrict__ Rr, const float* __restrict__ Ri, const float2* __restrict__ dY,
-                                    int C, int B, float2* __restrict__ dX) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= B * C * kK * kK) return;
-  const int am = i % (kK * kK), c = (i / (kK * kK)) % C, b = i / (kK * kK * C);
+// dX[s][i][m] = sum_o conj(R[m][o][i]) dY[s][o][m]
+__global__ void mix_bwd_data_kernel(const float2* __restrict__ R, const float2* __restrict__ dY, int C, int S, int NM,
+                                    float2* __restrict__ dX) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= (long long)S * C * NM) return;
+  const int m = (int)(i % NM), c = (int)((i / NM) % C);
+  const long long s = i / ((long long)NM * C);
+  const float2* g = dY + (size_t)s * C * NM + m;
   float re = 0.f, im = 0.f;
   for (int o = 0; o < C; ++o) {
-    const size_t ri = ((size_t)am * C + o) * C + c;
-    const float2 g = dY[((size_t)b * C + o) * kK * kK + am];
-    re += Rr[ri] * g.x + Ri[ri] * g.y;
-    im += Rr[ri] * g.y - Ri[ri] * g.x;
+    const float2 w = __ldg(R + ((size_t)m * C + o) * C + c), v = g[(size_t)o * NM];
+    re = fmaf(w.x, v.x, fmaf(w.y, v.y, re));
+    im = fmaf(w.x, v.y, fmaf(-w.y, v.x, im));
   }
   dX[i] = make_float2(re, im);
 }
 
-// psi_pred = psi_c + (o0 + i o1); with a target: dO = 2 (psi_pred - psi_f) / denom and per-block sums of |r|^2
-__global__ void output_kernel(const float* __restrict__ o, const float2* __restrict__ psi_c, const float2* __restrict__ psi_f,
-                              int HW, int B, float inv_denom, const float* __restrict__ sample_w, float2* __restrict__ pred,
-                              float* __restrict__ dO, double* __restrict__ block_sums) {
-  __shared__ double red[256];
+// dR[m][o][i] = sum_s dY[s][o][m] conj(X[s][i][m])  (as real parameters: d Re R, d Im R)
+__global__ void mix_bwd_weight_kernel(const float2* __restrict__ dY, const float2* __restrict__ X, int C, int S, int NM,
+                                      float2* __restrict__ dR) {
   const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  double sq = 0;
-  if (i < (long long)B * HW) {
-    const int b = (int)(i / HW), p = (int)(i % HW);
-    const float o0 = o[((size_t)b * 2) * HW + p], o1 = o[((size_t)b * 2 + 1) * HW + p];
-    const float2 c = psi_c[i];
-    const float2 w = make_float2(c.x + o0, c.y + o1);
-    if (pred) pred[i] = w;
-    if (psi_f) {
-      const float2 f = psi_f[i];
-      const float rx = w.x - f.x, ry = w.y - f.y;
-      const float wt = sample_w ? sample_w[b] * inv_denom : inv_denom;
-      sq = ((double)rx * rx + (double)ry * ry) * (double)wt;
-      dO[((size_t)b * 2) * HW + p] = 2.f * rx * wt;
-      dO[((size_t)b * 2 + 1) * HW + p] = 2.f * ry * wt;
-    }
+  if (i >= (long long)NM * C * C) return;
+  const int c = (int)(i % C), o = (int)((i / C) % C);
+  const int m = (int)(i / ((long long)C * C));
+  float re = 0.f, im = 0.f;
+  for (int s = 0; s < S; ++s) {
+    const float2 g = dY[((size_t)s * C + o) * NM + m], x = X[((size_t)s * C + c) * NM + m];
+    re = fmaf(g.x, x.x, fmaf(g.y, x.y, re));
+    im = fmaf(g.y, x.x, fmaf(-g.x, x.y, im));
   }
-  if (!block_sums) return;
-  red[threadIdx.x] = sq;
-  __syncthreads();
-  for (int s = blockDim.x / 2; s > 0; s >>= 1) {
-    if ((int)threadIdx.x < s) red[threadIdx.x] += red[threadIdx.x + s];
-    __syncthreads();
-  }
-  if (threadIdx.x == 0) block_sums[blockIdx.x] = red[0];
-}
-
-__global__ void sum_blocks_kernel(const double* __restrict__ s, int n, double scale, float* __restrict__ out) {
-  if (threadIdx.x != 0 || blockIdx.x != 0) return;
-  double acc = 0;
-  for (int i = 0; i < n; ++i) acc += s[i];
-  out[0] = (float)(acc * scale);
+  dR[i] = make_float2(re, im);
 }
 
 __global__ void adam_kernel(float* __restrict__ p, const float* __restrict__ g, float* __restrict__ m, float* __restrict__ v,
@@ -376,30 +139,132 @@ __global__ void adam_kernel(float* __restrict__ p, const float* __restrict__ g, 
   p[i] -= lr * (mi / c1) / (sqrtf(vi / c2) + eps);
 }
 
+// Network inputs of S coarse slices: out[s][p][c] for c < ratio: sigma * V of fine slice
+// ratio * s + c; c = ratio: their sum; c = ratio + 1: the constant `tval`.
+__global__ void features_kernel(const float* __restrict__ pot, int S, int ratio, long long P, float sigma, float tval,
+                                float* __restrict__ out) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= (long long)S * P) return;
+  const long long s = i / P, p = i % P;
+  const int cin = ratio + 2;
+  float* o = out + i * cin;
+  float sum = 0.f;
+  for (int j = 0; j < ratio; ++j) {
+    const float ph = sigma * pot[((size_t)s * ratio + j) * P + p];
+    o[j] = ph;
+    sum += ph;
+  }
+  o[ratio] = sum;
+  o[ratio + 1] = tval;
+}
+
+// Correction maps: maps (S, P, 4) = (Re A, Im A, Re B, Im B); `which` 0 = A, 1 = B.
+__device__ __forceinline__ float2 one_plus(const float* maps, long long sp, int which) {
+  const float* m = maps + sp * 4 + 2 * which;
+  return make_float2(1.f + m[0], m[1]);
+}
+
+// w[b][p] *= (1 + M_s[p]) (or its conjugate) for nb waves that all use sample s
+__global__ void map_mul_kernel(float2* __restrict__ w, int nb, long long P, const float* __restrict__ maps, int which,
+                               int conj) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= (long long)nb * P) return;
+  float2 f = one_plus(maps, i % P, which);
+  if (conj) f.y = -f.y;
+  w[i] = cmul(w[i], f);
+}
+
+// w[b][p] *= plane[p] (or its conjugate)
+__global__ void plane_mul_kernel(float2* __restrict__ w, long long n, long long P, const float2* __restrict__ plane,
+                                 int conj) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  float2 f = plane[i % P];
+  if (conj) f.y = -f.y;
+  w[i] = cmul(w[i], f);
+}
+
+// out[p] = t[p] (1 + M[p]) for one plane
+__global__ void map_trans_kernel(const float2* __restrict__ t, long long P, const float* __restrict__ maps, int which,
+                                 float2* __restrict__ out) {
+  const long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= P) return;
+  out[p] = cmul(t[p], one_plus(maps, p, which));
+}
+
+// dmaps[p][2 which], [2 which + 1] (+)= 2 sum_b conj(u[b][p]) g[b][p]  (b in order)
+__global__ void map_grad_kernel(const float2* __restrict__ u, const float2* __restrict__ g, int nb, long long P,
+                                int which, int accumulate, float* __restrict__ dmaps) {
+  const long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= P) return;
+  float re = 0.f, im = 0.f;
+  for (int b = 0; b < nb; ++b) {
+    const float2 a = u[(size_t)b * P + p], c = g[(size_t)b * P + p];
+    re = fmaf(a.x, c.x, fmaf(a.y, c.y, re));
+    im = fmaf(a.x, c.y, fmaf(-a.y, c.x, im));
+  }
+  float* d = dmaps + p * 4 + 2 * which;
+  if (accumulate) {
+    d[0] += 2.f * re;
+    d[1] += 2.f * im;
+  } else {
+    d[0] = 2.f * re;
+    d[1] = 2.f * im;
+  }
+}
+
+// g[i] (+)= wt (psi[i] - f[i]); per-block sums of wt |psi - f|^2 (double)
+__global__ void resid_kernel(const float2* __restrict__ psi, const float2* __restrict__ f, long long n, float wt,
+                             int accumulate, float2* __restrict__ g, double* __restrict__ sums) {
+  __shared__ double red[256];
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  double sq = 0;
+  if (i < n) {
+    const float2 a = psi[i], b = f[i];
+    const float rx = a.x - b.x, ry = a.y - b.y;
+    sq = ((double)rx * rx + (double)ry * ry) * wt;
+    const float2 v = make_float2(wt * rx, wt * ry);
+    g[i] = accumulate ? make_float2(g[i].x + v.x, g[i].y + v.y) : v;
+  }
+  red[threadIdx.x] = sq;
+  __syncthreads();
+  for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+    if ((int)threadIdx.x < s) red[threadIdx.x] += red[threadIdx.x + s];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) sums[blockIdx.x] = red[0];
+}
+
+__global__ void sum_blocks_kernel(const double* __restrict__ s, int n, float* __restrict__ out) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  double acc = 0;
+  for (int i = 0; i < n; ++i) acc += s[i];
+  out[0] = (float)acc;
+}
+
 }  // namespace nn
 }  // namespace msx
 
 using namespace msx;
 using namespace msx::nn;
 
-// ------------------------------------------------------------------ host object
 struct msx_corrector {
-  int H = 0, W = 0, C = 0, L = 0, maxB = 0;
+  int H = 0, W = 0, Cin = 0, C = 0, L = 0, MX = 0, MY = 0, maxS = 0;
+  long long P = 0;
   size_t nparams = 0;
-  // parameter offsets (floats)
-  size_t oW0, ob0, oP1, oc1, oP2, oc2;
-  std::vector<size_t> oRr, oRi, oWl, obl;
+  size_t oW0 = 0, ob0 = 0, oP1 = 0, oc1 = 0, oP2 = 0, oc2 = 0;
+  std::vector<size_t> oR, oW, ob;
   float *params = nullptr, *grads = nullptr, *m = nullptr, *v = nullptr;
-  // activations
-  float *x0 = nullptr, *a = nullptr, *z = nullptr, *h = nullptr, *zh = nullptr, *o = nullptr;
-  float *da = nullptr, *dz = nullptr, *dh = nullptr, *dO = nullptr;
-  float2 *X1 = nullptr, *X2 = nullptr, *Y = nullptr, *Z1 = nullptr;  // spectral scratch
-  float2 *dX2 = nullptr;
+  float *Bdx = nullptr, *Bdy = nullptr, *Biy = nullptr, *Bix = nullptr;  // partial DFT matrices
+  float *xin = nullptr, *a = nullptr, *z = nullptr, *zh = nullptr, *h = nullptr, *o = nullptr;
+  float *U1 = nullptr, *Xh = nullptr, *Yh = nullptr, *U2 = nullptr;
+  float *da = nullptr, *da2 = nullptr, *dz = nullptr;
   float* part = nullptr;
   size_t part_words = 0;
   double* sums = nullptr;
-  float* loss = nullptr;
-  int step = 0;
+  size_t sums_words = 0;
+  TcGemm gemm;
+  int S_last = 0, step = 0;
 };
 
 namespace {
@@ -409,153 +274,265 @@ int cfail(int code, const char* msg) {
   return code;
 }
 
-#define NN_CUDA(call)                                               \
-  do {                                                              \
-    cudaError_t e_ = (call);                                        \
-    if (e_ != cudaSuccess) return cfail(MSX_ERR_CUDA, cudaGetErrorString(e_)); \
+#define NN_CUDA(call)                                                            \
+  do {                                                                           \
+    cudaError_t e_ = (call);                                                     \
+    if (e_ != cudaSuccess) return cfail(MSX_ERR_CUDA, cudaGetErrorString(e_));   \
+  } while (0)
+#define NN_GEMM(call)                                                                              \
+  do {                                                                                             \
+    int r_ = (call);                                                                               \
+    if (r_ != MSX_OK) return cfail(r_, "corrector: tensor-core GEMM failed (sizes or allocation)"); \
   } while (0)
 
 inline unsigned blocks_for(long long n, int t) { return (unsigned)((n + t - 1) / t); }
 
-size_t act(const msx_corrector* k, int B) { return (size_t)B * k->C * k->H * k->W; }
+size_t act_words(const msx_corrector* k, int S) { return (size_t)S * k->P * k->C; }
+size_t u_words(const msx_corrector* k, int S) { return (size_t)S * k->H * k->C * k->MX * 2; }
+size_t x_words(const msx_corrector* k, int S) { return (size_t)S * k->C * k->MX * k->MY * 2; }
 
-// forward; keeps what the backward needs.  x0 from psi_c / tc.
-int forward(msx_corrector* k, const float2* psi_c, const float2* tc, int B, cudaStream_t st) {
-  const int HW = k->H * k->W, C = k->C;
-  const long long nb = (long long)B * HW;
-  float* P = k->params;
-  inputs_kernel<<<blocks_for(nb, 256), 256, 0, st>>>(psi_c, tc, HW, B, k->x0);
-  // a_0 = W0 x0 + b0 (stored at layer slot 0)
-  linear_fwd_kernel<<<blocks_for(nb, 128), 128, 0, st>>>(k->x0, 4, P + k->oW0, P + k->ob0, C, HW, B, nullptr,
-                                                         k->a, nullptr);
+Epi epi(float* y, Addr out) {
+  Epi e{};
+  e.y = y;
+  e.out = out;
+  e.scale = 1.f;
+  return e;
+}
+
+// Pixel-major activation (S, H, W, C) as rows (s, y, c) x columns x.
+Addr rows_syc(const msx_corrector* k) { return Addr{(long long)k->W * k->C, 1, k->C, k->C, 0, 1}; }
+// Complex (S, H, C, MX) as rows (s, c, m) x columns (2 y + re/im).
+Addr rows_scm(const msx_corrector* k) {
+  const long long cm = (long long)k->C * k->MX;
+  return Addr{(long long)k->H * cm * 2, 2, cm, cm * 2, 1, 2};
+}
+
+// out[j] = column sums of x (rows x n), n in {4, 32, 64, ...} dividing 256
+int colsum(msx_corrector* k, const float* x, long long rows, int n, float* out, cudaStream_t st) {
+  const long long chunk = 4096;
+  const int nchunks = (int)((rows + chunk - 1) / chunk);
+  if ((size_t)nchunks * n > k->part_words) return cfail(MSX_ERR_INVALID, "corrector: reduction buffer too small");
+  colsum_part_kernel<<<nchunks, 256, 0, st>>>(x, rows, n, chunk, k->part);
+  reduce_parts_kernel<<<blocks_for(n, 128), 128, 0, st>>>(k->part, nchunks, n, out);
+  NN_CUDA(cudaGetLastError());
+  return MSX_OK;
+}
+
+// weight gradient dW (n_out x n_in) = dY^T X over the S * P pixels (split K on the tensor cores)
+int wgrad(msx_corrector* k, const float* dY, int n_out, const float* X, int n_in, int S, float* dW, cudaStream_t st) {
+  const long long K = (long long)S * k->P;
+  const int ksplit = (int)std::min<long long>(128, std::max<long long>(1, K / 8192));
+  NN_GEMM(k->gemm.run(dY, colmajor(n_out), X, colmajor(n_in), n_out, n_in, K, epi(dW, rowmajor(n_in)), st, ksplit));
+  return MSX_OK;
+}
+
+int forward(msx_corrector* k, int S, cudaStream_t st) {
+  const long long SP = (long long)S * k->P;
+  const int C = k->C, H = k->H, W = k->W, MX = k->MX, MY = k->MY;
+  const int NM = MX * MY;
+  float* Pm = k->params;
+  const size_t A = act_words(k, S);
+  // lift
+  {
+    Epi e = epi(k->a, rowmajor(C));
+    e.bias = Pm + k->ob0;
+    NN_GEMM(k->gemm.run(k->xin, rowmajor(k->Cin), Pm + k->oW0, rowmajor(k->Cin), SP, C, k->Cin, e, st));
+  }
   for (int l = 0; l < k->L; ++l) {
-    float* ain = k->a + (size_t)l * act(k, B);
-    float* aout = k->a + (size_t)(l + 1) * act(k, B);
-    float* zl = k->z + (size_t)l * act(k, B);
-    float2* X2l = k->X2 + (size_t)l * B * C * kK * kK;
-    const long long rows = (long long)B * C * k->H;
-    dft_x_kernel<<<blocks_for(rows * 32, 256), 256, 0, st>>>(ain, rows, k->W, 1.f, k->X1);
-    dft_y_kernel<<<blocks_for((long long)B * C * kK * 32, 256), 256, 0, st>>>(k->X1, (long long)B * C, k->H, -1.f, X2l);
-    mix_fwd_kernel<<<blocks_for((long long)B * C * kK * kK, 256), 256, 0, st>>>(P + k->oRr[l], P + k->oRi[l], X2l, C, B, k->Y);
-    idft_y_kernel<<<blocks_for((long long)B * C * k->H * kK, 256), 256, 0, st>>>(k->Y, (long long)B * C, k->H, k->Z1);
-    idft_x_real_kernel<<<blocks_for(rows * k->W, 256), 256, 0, st>>>(k->Z1, rows, k->W, 1.f / (float)HW, 0, zl);
-    linear_fwd_kernel<<<blocks_for(nb, 128), 128, 0, st>>>(ain, C, P + k->oWl[l], P + k->obl[l], C, HW, B, zl, zl, aout);
-  }
-  linear_fwd_kernel<<<blocks_for(nb, 128), 128, 0, st>>>(k->a + (size_t)k->L * act(k, B), C, P + k->oP1, P + k->oc1, C,
-                                                         HW, B, nullptr, k->zh, k->h);
-  linear_fwd_kernel<<<blocks_for(nb, 128), 128, 0, st>>>(k->h, C, P + k->oP2, P + k->oc2, 2, HW, B, nullptr, k->o,
-                                                         nullptr);
-  NN_CUDA(cudaGetLastError());
-  return MSX_OK;
-}
-
-int weight_grad(msx_corrector* k, const float* dzp, int Cout, const float* in, int Cin, int B, float* gW, float* gb,
-                cudaStream_t st) {
-  const long long total = (long long)B * k->H * k->W;
-  const int chunk = 8192;
-  const int nchunks = (int)((total + chunk - 1) / chunk);
-  const int npair = Cout * Cin + Cout;
-  if ((size_t)nchunks * npair > k->part_words) return cfail(MSX_ERR_INVALID, "corrector partial buffer too small");
-  linear_bwd_weight_kernel<<<nchunks, 256, 0, st>>>(dzp, Cout, in, Cin, k->H * k->W, B, chunk, k->part);
-  // gW and gb are contiguous in the parameter layout (W then bias)
-  (void)gb;
-  reduce_parts_kernel<<<blocks_for(npair, 256), 256, 0, st>>>(k->part, nchunks, npair, gW);
-  NN_CUDA(cudaGetLastError());
-  return MSX_OK;
-}
-
-int backward(msx_corrector* k, int B, cudaStream_t st) {
-  const int HW = k->H * k->W, C = k->C;
-  const long long nb = (long long)B * HW;
-  float* P = k->params;
-  float* G = k->grads;
-  const size_t A = act(k, B);
-  // output layer: o = P2 h + c2
-  int rc = weight_grad(k, k->dO, 2, k->h, C, B, G + k->oP2, G + k->oc2, st);
-  if (rc) return rc;
-  linear_bwd_data_kernel<<<blocks_for(nb, 128), 128, 0, st>>>(k->dO, 2, P + k->oP2, C, HW, B, 0, k->dh);
-  gelu_bwd_kernel<<<blocks_for((long long)A, 256), 256, 0, st>>>(k->dh, k->zh, (long long)A, k->dz);
-  rc = weight_grad(k, k->dz, C, k->a + (size_t)k->L * A, C, B, G + k->oP1, G + k->oc1, st);
-  if (rc) return rc;
-  float* da = k->da;  // gradient w.r.t. a_L
-  linear_bwd_data_kernel<<<blocks_for(nb, 128), 128, 0, st>>>(k->dz, C, P + k->oP1, C, HW, B, 0, da);
-  for (int l = k->L - 1; l >= 0; --l) {
     float* ain = k->a + (size_t)l * A;
+    float* aout = k->a + (size_t)(l + 1) * A;
     float* zl = k->z + (size_t)l * A;
-    float2* X2l = k->X2 + (size_t)l * B * C * kK * kK;
-    gelu_bwd_kernel<<<blocks_for((long long)A, 256), 256, 0, st>>>(da, zl, (long long)A, k->dz);
-    rc = weight_grad(k, k->dz, C, ain, C, B, G + k->oWl[l], G + k->obl[l], st);
-    if (rc) return rc;
-    // da_{l} = W_l^T dz + spectral adjoint (written into da, which held da_{l+1})
-    linear_bwd_data_kernel<<<blocks_for(nb, 128), 128, 0, st>>>(k->dz, C, P + k->oWl[l], C, HW, B, 0, da);
-    const long long rows = (long long)B * C * k->H;
-    dft_x_kernel<<<blocks_for(rows * 32, 256), 256, 0, st>>>(k->dz, rows, k->W, 1.f / (float)HW, k->X1);
-    dft_y_kernel<<<blocks_for((long long)B * C * kK * 32, 256), 256, 0, st>>>(k->X1, (long long)B * C, k->H, -1.f, k->Y);
-    mix_bwd_weight_kernel<<<blocks_for((long long)kK * kK * C * C, 256), 256, 0, st>>>(k->Y, X2l, C, B, G + k->oRr[l],
-                                                                                      G + k->oRi[l]);
-    mix_bwd_data_kernel<<<blocks_for((long long)B * C * kK * kK, 256), 256, 0, st>>>(P + k->oRr[l], P + k->oRi[l], k->Y,
-                                                                                    C, B, k->dX2);
-    idft_y_kernel<<<blocks_for((long long)B * C * k->H * kK, 256), 256, 0, st>>>(k->dX2, (long long)B * C, k->H, k->Z1);
-    idft_x_real_kernel<<<blocks_for(rows * k->W, 256), 256, 0, st>>>(k->Z1, rows, k->W, 1.f, 1, da);
+    float* Xl = k->Xh + (size_t)l * x_words(k, S);
+    // DFT along x: rows (s, y, c), K = W -> U1 (S, H, C, MX) complex
+    NN_GEMM(k->gemm.run(ain, rows_syc(k), k->Bdx, rowmajor(W), (long long)S * H * C, 2 * MX, W,
+                        epi(k->U1, rowmajor(2 * MX)), st));
+    // DFT along y: rows (s, c, m), K = 2H -> X (S, C, MX, MY) complex
+    NN_GEMM(k->gemm.run(k->U1, rows_scm(k), k->Bdy, rowmajor(2 * H), (long long)S * C * MX, 2 * MY, 2 * H,
+                        epi(Xl, rowmajor(2 * MY)), st));
+    mix_fwd_kernel<<<blocks_for((long long)S * C * NM, 256), 256, 0, st>>>(
+        reinterpret_cast<const float2*>(Pm + k->oR[l]), reinterpret_cast<const float2*>(Xl), C, S, NM,
+        reinterpret_cast<float2*>(k->Yh));
+    NN_CUDA(cudaGetLastError());
+    // inverse DFT along y: rows (s, o, m), K = 2 MY -> U2 (S, H, C, MX) complex
+    NN_GEMM(k->gemm.run(k->Yh, rowmajor(2 * MY), k->Biy, rowmajor(2 * MY), (long long)S * C * MX, 2 * H, 2 * MY,
+                        epi(k->U2, rows_scm(k)), st));
+    // inverse DFT along x (real part, 1/(H W) folded in): rows (s, y, o), K = 2 MX -> z_l pixel-major
+    NN_GEMM(k->gemm.run(k->U2, rowmajor(2 * MX), k->Bix, rowmajor(2 * MX), (long long)S * H * C, W, 2 * MX,
+                        epi(zl, rows_syc(k)), st));
+    // pointwise layer: z_l += a W_l^T + b_l; a_l = gelu(z_l)
+    Epi e = epi(zl, rowmajor(C));
+    e.bias = Pm + k->ob[l];
+    e.accumulate = 1;
+    e.act = aout;
+    NN_GEMM(k->gemm.run(ain, rowmajor(C), Pm + k->oW[l], rowmajor(C), SP, C, C, e, st));
   }
-  // lift: a0 = W0 x0 + b0
-  rc = weight_grad(k, da, C, k->x0, 4, B, G + k->oW0, G + k->ob0, st);
-  if (rc) return rc;
-  NN_CUDA(cudaGetLastError());
+  {
+    Epi e = epi(k->zh, rowmajor(C));
+    e.bias = Pm + k->oc1;
+    e.act = k->h;
+    NN_GEMM(k->gemm.run(k->a + (size_t)k->L * A, rowmajor(C), Pm + k->oP1, rowmajor(C), SP, C, C, e, st));
+    Epi e2 = epi(k->o, rowmajor(4));
+    e2.bias = Pm + k->oc2;
+    NN_GEMM(k->gemm.run(k->h, rowmajor(C), Pm + k->oP2, rowmajor(C), SP, 4, C, e2, st));
+  }
   return MSX_OK;
+}
+
+int backward(msx_corrector* k, const float* dmaps, cudaStream_t st) {
+  const int S = k->S_last;
+  const long long SP = (long long)S * k->P;
+  const int C = k->C, H = k->H, W = k->W, MX = k->MX, MY = k->MY;
+  const int NM = MX * MY;
+  float* Pm = k->params;
+  float* G = k->grads;
+  const size_t A = act_words(k, S);
+  int rc;
+  // head: o = h P2^T + c2
+  if ((rc = wgrad(k, dmaps, 4, k->h, C, S, G + k->oP2, st))) return rc;
+  if ((rc = colsum(k, dmaps, SP, 4, G + k->oc2, st))) return rc;
+  NN_GEMM(k->gemm.run(dmaps, rowmajor(4), Pm + k->oP2, colmajor(C), SP, C, 4, epi(k->dz, rowmajor(C)), st));
+  gelu_bwd_kernel<<<blocks_for((long long)A, 256), 256, 0, st>>>(k->dz, k->zh, (long long)A, k->dz);
+  if ((rc = wgrad(k, k->dz, C, k->a + (size_t)k->L * A, C, S, G + k->oP1, st))) return rc;
+  if ((rc = colsum(k, k->dz, SP, C, G + k->oc1, st))) return rc;
+  NN_GEMM(k->gemm.run(k->dz, rowmajor(C), Pm + k->oP1, colmajor(C), SP, C, C, epi(k->da, rowmajor(C)), st));
+  for (int l = k->L - 1; l >= 0; --l) {
+    const float* ain = k->a + (size_t)l * A;
+    const float* zl = k->z + (size_t)l * A;
+    const float* Xl = k->Xh + (size_t)l * x_words(k, S);
+    gelu_bwd_kernel<<<blocks_for((long long)A, 256), 256, 0, st>>>(k->da, zl, (long long)A, k->dz);
+    NN_CUDA(cudaGetLastError());
+    if ((rc = wgrad(k, k->dz, C, ain, C, S, G + k->oW[l], st))) return rc;
+    if ((rc = colsum(k, k->dz, SP, C, G + k->ob[l], st))) return rc;
+    // pointwise part: da2 = dz W_l
+    NN_GEMM(k->gemm.run(k->dz, rowmajor(C), Pm + k->oW[l], colmajor(C), SP, C, C, epi(k->da2, rowmajor(C)), st));
+    // spectral part, in reverse: IDFT_x^T, IDFT_y^T, mixing, DFT_y^T, DFT_x^T
+    NN_GEMM(k->gemm.run(k->dz, rows_syc(k), k->Bix, colmajor(2 * MX), (long long)S * H * C, 2 * MX, W,
+                        epi(k->U2, rowmajor(2 * MX)), st));
+    NN_GEMM(k->gemm.run(k->U2, rows_scm(k), k->Biy, colmajor(2 * MY), (long long)S * C * MX, 2 * MY, 2 * H,
+                        epi(k->Yh, rowmajor(2 * MY)), st));
+    mix_bwd_weight_kernel<<<blocks_for((long long)NM * C * C, 256), 256, 0, st>>>(
+        reinterpret_cast<const float2*>(k->Yh), reinterpret_cast<const float2*>(Xl), C, S, NM,
+        reinterpret_cast<float2*>(G + k->oR[l]));
+    mix_bwd_data_kernel<<<blocks_for((long long)S * C * NM, 256), 256, 0, st>>>(
+        reinterpret_cast<const float2*>(Pm + k->oR[l]), reinterpret_cast<const float2*>(k->Yh), C, S, NM,
+        reinterpret_cast<float2*>(k->U1));  // dX (S, C, MX, MY) complex, in U1's space
+    NN_CUDA(cudaGetLastError());
+    // dX -> dU1 (S, H, C, MX): write into U2 (free now)
+    NN_GEMM(k->gemm.run(k->U1, rowmajor(2 * MY), k->Bdy, colmajor(2 * H), (long long)S * C * MX, 2 * H, 2 * MY,
+                        epi(k->U2, rows_scm(k)), st));
+    Epi e = epi(k->da2, rows_syc(k));
+    e.accumulate = 1;
+    NN_GEMM(k->gemm.run(k->U2, rowmajor(2 * MX), k->Bdx, colmajor(W), (long long)S * H * C, W, 2 * MX, e, st));
+    std::swap(k->da, k->da2);
+  }
+  // lift: a_0 = x W0^T + b0 (no activation)
+  if ((rc = wgrad(k, k->da, C, k->xin, k->Cin, S, G + k->oW0, st))) return rc;
+  if ((rc = colsum(k, k->da, SP, C, G + k->ob0, st))) return rc;
+  return MSX_OK;
+}
+
+// Partial DFT matrices (FP32, row-major) of an H x W grid with MX x MY modes.
+void build_dft(int H, int W, int MX, int MY, std::vector<float>& dx, std::vector<float>& dy, std::vector<float>& iy,
+               std::vector<float>& ix) {
+  const double two_pi = 6.283185307179586476925286766559;
+  dx.assign((size_t)2 * MX * W, 0.f);
+  for (int m = 0; m < MX; ++m)
+    for (int x = 0; x < W; ++x) {
+      const double th = two_pi * (double)(((long long)m * x) % W) / W;
+      dx[(size_t)(2 * m) * W + x] = (float)std::cos(th);
+      dx[(size_t)(2 * m + 1) * W + x] = (float)-std::sin(th);
+    }
+  dy.assign((size_t)2 * MY * 2 * H, 0.f);
+  iy.assign((size_t)2 * H * 2 * MY, 0.f);
+  for (int q = 0; q < MY; ++q) {
+    const long long f = q < MY / 2 ? q : q - MY;
+    for (int y = 0; y < H; ++y) {
+      const long long r = ((f * y) % H + H) % H;
+      const double th = two_pi * (double)r / H;
+      const float c = (float)std::cos(th), s = (float)std::sin(th);
+      dy[(size_t)(2 * q) * 2 * H + 2 * y] = c;
+      dy[(size_t)(2 * q) * 2 * H + 2 * y + 1] = s;
+      dy[(size_t)(2 * q + 1) * 2 * H + 2 * y] = -s;
+      dy[(size_t)(2 * q + 1) * 2 * H + 2 * y + 1] = c;
+      iy[(size_t)(2 * y) * 2 * MY + 2 * q] = c;
+      iy[(size_t)(2 * y) * 2 * MY + 2 * q + 1] = -s;
+      iy[(size_t)(2 * y + 1) * 2 * MY + 2 * q] = s;
+      iy[(size_t)(2 * y + 1) * 2 * MY + 2 * q + 1] = c;
+    }
+  }
+  ix.assign((size_t)W * 2 * MX, 0.f);
+  const double inv = 1.0 / ((double)H * W);
+  for (int x = 0; x < W; ++x)
+    for (int m = 0; m < MX; ++m) {
+      const double th = two_pi * (double)(((long long)m * x) % W) / W;
+      const double wm = (m == 0 ? 1.0 : 2.0) * inv;
+      ix[(size_t)x * 2 * MX + 2 * m] = (float)(wm * std::cos(th));
+      ix[(size_t)x * 2 * MX + 2 * m + 1] = (float)(-wm * std::sin(th));
+    }
 }
 
 }  // namespace
 
 extern "C" {
 
-int msx_corrector_create(int ny, int nx, int channels, int layers, int max_batch, msx_corrector** out) {
+int msx_corrector_create(int ny, int nx, int in_channels, int channels, int layers, int modes_x, int modes_y,
+                         int max_samples, msx_corrector** out) {
   if (!out) return cfail(MSX_ERR_INVALID, "null corrector pointer");
   *out = nullptr;
-  if (ny < kK || nx < kK || channels < 1 || channels > kMaxC || layers < 1 || layers > 16 || max_batch < 1)
-    return cfail(MSX_ERR_INVALID, "corrector: grid >= 8, 1..32 channels, 1..16 layers, batch >= 1");
+  if (ny < 8 || nx < 8 || ny > 4096 || nx > 4096 || in_channels < 1 || in_channels > 64 || channels < 1 ||
+      channels > 64 || 256 % channels || layers < 1 || layers > 16 || modes_x < 1 || modes_x > nx / 2 ||
+      modes_y < 2 || modes_y % 2 || modes_y > ny || max_samples < 1)
+    return cfail(MSX_ERR_INVALID, "corrector: grid 8..4096, 1..64 input channels, channels dividing 256 (<= 64), "
+                                  "1..16 layers, modes_x <= nx/2, even modes_y <= ny, samples >= 1");
   msx_corrector* k = new msx_corrector();
-  k->H = ny; k->W = nx; k->C = channels; k->L = layers; k->maxB = max_batch;
+  k->H = ny; k->W = nx; k->P = (long long)ny * nx; k->Cin = in_channels; k->C = channels; k->L = layers;
+  k->MX = modes_x; k->MY = modes_y; k->maxS = max_samples;
   const int C = channels;
   size_t off = 0;
-  // each weight matrix is immediately followed by its bias (the gradient reduction writes both)
-  k->oW0 = off; off += (size_t)C * 4; k->ob0 = off; off += C;
+  k->oW0 = off; off += (size_t)C * in_channels; k->ob0 = off; off += C;
   for (int l = 0; l < layers; ++l) {
-    k->oRr.push_back(off); off += (size_t)kK * kK * C * C;
-    k->oRi.push_back(off); off += (size_t)kK * kK * C * C;
-    k->oWl.push_back(off); off += (size_t)C * C;
-    k->obl.push_back(off); off += C;
+    k->oR.push_back(off); off += (size_t)modes_x * modes_y * C * C * 2;
+    k->oW.push_back(off); off += (size_t)C * C;
+    k->ob.push_back(off); off += C;
   }
   k->oP1 = off; off += (size_t)C * C; k->oc1 = off; off += C;
-  k->oP2 = off; off += (size_t)2 * C; k->oc2 = off; off += 2;
+  k->oP2 = off; off += (size_t)4 * C; k->oc2 = off; off += 4;
   k->nparams = off;
-  const size_t HW = (size_t)ny * nx, B = max_batch;
-  const size_t A = B * C * HW;
-  const size_t chunks = (B * HW + 8191) / 8192;
-  k->part_words = chunks * (size_t)(kMaxC * kMaxC + kMaxC);
+  const size_t S = max_samples, A = act_words(k, max_samples);
+  k->part_words = ((S * k->P + 4095) / 4096) * 64;
   cudaError_t e = cudaSuccess;
-  auto alloc = [&](void** p, size_t bytes) { if (e == cudaSuccess) e = cudaMalloc(p, bytes); };
-  alloc((void**)&k->params, 4 * off * sizeof(float));
+  auto alloc = [&](float** p, size_t words) { if (e == cudaSuccess) e = cudaMalloc((void**)p, words * sizeof(float)); };
+  alloc(&k->params, 4 * off);
   if (e == cudaSuccess) { k->grads = k->params + off; k->m = k->grads + off; k->v = k->m + off; }
-  alloc((void**)&k->x0, B * 4 * HW * sizeof(float));
-  alloc((void**)&k->a, (layers + 1) * A * sizeof(float));
-  alloc((void**)&k->z, layers * A * sizeof(float));
-  alloc((void**)&k->h, A * sizeof(float));
-  alloc((void**)&k->zh, A * sizeof(float));
-  alloc((void**)&k->o, B * 2 * HW * sizeof(float));
-  alloc((void**)&k->da, A * sizeof(float));
-  alloc((void**)&k->dz, A * sizeof(float));
-  alloc((void**)&k->dh, A * sizeof(float));
-  alloc((void**)&k->dO, B * 2 * HW * sizeof(float));
-  alloc((void**)&k->X1, B * C * ny * kK * sizeof(float2));
-  alloc((void**)&k->Z1, B * C * ny * kK * sizeof(float2));
-  alloc((void**)&k->X2, layers * B * C * kK * kK * sizeof(float2));
-  alloc((void**)&k->Y, B * C * kK * kK * sizeof(float2));
-  alloc((void**)&k->dX2, B * C * kK * kK * sizeof(float2));
-  alloc((void**)&k->part, k->part_words * sizeof(float));
-  alloc((void**)&k->sums, ((B * HW + 255) / 256) * sizeof(double));
-  alloc((void**)&k->loss, sizeof(float));
+  alloc(&k->Bdx, (size_t)2 * modes_x * nx);
+  alloc(&k->Bdy, (size_t)4 * modes_y * ny);
+  alloc(&k->Biy, (size_t)4 * modes_y * ny);
+  alloc(&k->Bix, (size_t)2 * modes_x * nx);
+  alloc(&k->xin, S * k->P * in_channels);
+  alloc(&k->a, (layers + 1) * A);
+  alloc(&k->z, layers * A);
+  alloc(&k->zh, A);
+  alloc(&k->h, A);
+  alloc(&k->o, S * k->P * 4);
+  alloc(&k->U1, std::max(u_words(k, max_samples), x_words(k, max_samples)));
+  alloc(&k->U2, u_words(k, max_samples));
+  alloc(&k->Xh, layers * x_words(k, max_samples));
+  alloc(&k->Yh, x_words(k, max_samples));
+  alloc(&k->da, A);
+  alloc(&k->da2, A);
+  alloc(&k->dz, A);
+  alloc(&k->part, k->part_words);
+  k->sums_words = (S * k->P * 64 + 255) / 256;
+  if (e == cudaSuccess) e = cudaMalloc((void**)&k->sums, k->sums_words * sizeof(double));
   if (e == cudaSuccess) e = cudaMemset(k->params, 0, 4 * off * sizeof(float));
+  if (e == cudaSuccess) {
+    std::vector<float> dx, dy, iy, ix;
+    build_dft(ny, nx, modes_x, modes_y, dx, dy, iy, ix);
+    e = cudaMemcpy(k->Bdx, dx.data(), dx.size() * sizeof(float), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(k->Bdy, dy.data(), dy.size() * sizeof(float), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(k->Biy, iy.data(), iy.size() * sizeof(float), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(k->Bix, ix.data(), ix.size() * sizeof(float), cudaMemcpyHostToDevice);
+  }
   if (e != cudaSuccess) {
     msx_corrector_destroy(k);
     return cfail(MSX_ERR_ALLOC, "corrector allocation failed");
@@ -566,10 +543,12 @@ int msx_corrector_create(int ny, int nx, int channels, int layers, int max_batch
 
 int msx_corrector_destroy(msx_corrector* k) {
   if (!k) return MSX_OK;
-  for (void* p : {(void*)k->params, (void*)k->x0, (void*)k->a, (void*)k->z, (void*)k->h, (void*)k->zh, (void*)k->o,
-                  (void*)k->da, (void*)k->dz, (void*)k->dh, (void*)k->dO, (void*)k->X1, (void*)k->Z1, (void*)k->X2,
-                  (void*)k->Y, (void*)k->dX2, (void*)k->part, (void*)k->sums, (void*)k->loss})
+  for (void* p : {(void*)k->params, (void*)k->Bdx, (void*)k->Bdy, (void*)k->Biy, (void*)k->Bix, (void*)k->xin,
+                  (void*)k->a, (void*)k->z, (void*)k->zh, (void*)k->h, (void*)k->o, (void*)k->U1, (void*)k->U2,
+                  (void*)k->Xh, (void*)k->Yh, (void*)k->da, (void*)k->da2, (void*)k->dz, (void*)k->part,
+                  (void*)k->sums})
     if (p) cudaFree(p);
+  k->gemm.release();
   delete k;
   return MSX_OK;
 }
@@ -582,36 +561,39 @@ int msx_corrector_params(msx_corrector* k, float** params_dev, float** grads_dev
   return MSX_OK;
 }
 
-int msx_corrector_forward(msx_corrector* k, const float* psi_c_dev, const float* tc_dev, int batch, float* pred_out_dev,
-                          void* stream) {
-  if (!k || !psi_c_dev || !tc_dev || !pred_out_dev || batch < 1 || batch > k->maxB)
-    return cfail(MSX_ERR_INVALID, "corrector forward: bad arguments");
-  cudaStream_t st = (cudaStream_t)stream;
-  int rc = forward(k, reinterpret_cast<const float2*>(psi_c_dev), reinterpret_cast<const float2*>(tc_dev), batch, st);
-  if (rc) return rc;
-  const long long nb = (long long)batch * k->H * k->W;
-  output_kernel<<<blocks_for(nb, 256), 256, 0, st>>>(k->o, reinterpret_cast<const float2*>(psi_c_dev), nullptr, k->H * k->W,
-                                                     batch, 0.f, nullptr, reinterpret_cast<float2*>(pred_out_dev), nullptr,
-                                                     nullptr);
-  NN_CUDA(cudaGetLastError());
+int msx_corrector_layout(const msx_corrector* k, size_t* offsets, int n) {
+  // W0, b0, then per layer R, W, b, then P1, c1, P2, c2
+  if (!k || !offsets || n < 6 + 3 * k->L) return cfail(MSX_ERR_INVALID, "corrector layout: need 6 + 3 L offsets");
+  int i = 0;
+  offsets[i++] = k->oW0;
+  offsets[i++] = k->ob0;
+  for (int l = 0; l < k->L; ++l) {
+    offsets[i++] = k->oR[l];
+    offsets[i++] = k->oW[l];
+    offsets[i++] = k->ob[l];
+  }
+  offsets[i++] = k->oP1;
+  offsets[i++] = k->oc1;
+  offsets[i++] = k->oP2;
+  offsets[i++] = k->oc2;
   return MSX_OK;
 }
 
-int msx_corrector_loss_grad(msx_corrector* k, const float* psi_c_dev, const float* tc_dev, const float* psi_f_dev,
-                            int batch, double denom, const float* sample_weights_dev, float* loss_out_dev, void* stream) {
-  if (!k || !psi_c_dev || !tc_dev || !psi_f_dev || batch < 1 || batch > k->maxB || !(denom > 0))
-    return cfail(MSX_ERR_INVALID, "corrector loss: bad arguments");
+int msx_corrector_forward(msx_corrector* k, const float* features_dev, int samples, float* maps_out_dev, void* stream) {
+  if (!k || !features_dev || !maps_out_dev || samples < 1 || samples > k->maxS)
+    return cfail(MSX_ERR_INVALID, "corrector forward: bad arguments");
   cudaStream_t st = (cudaStream_t)stream;
-  int rc = forward(k, reinterpret_cast<const float2*>(psi_c_dev), reinterpret_cast<const float2*>(tc_dev), batch, st);
+  NN_CUDA(cudaMemcpyAsync(k->xin, features_dev, sizeof(float) * samples * k->P * k->Cin, cudaMemcpyDeviceToDevice, st));
+  int rc = forward(k, samples, st);
   if (rc) return rc;
-  const long long nb = (long long)batch * k->H * k->W;
-  const unsigned nblk = blocks_for(nb, 256);
-  output_kernel<<<nblk, 256, 0, st>>>(k->o, reinterpret_cast<const float2*>(psi_c_dev),
-                                       reinterpret_cast<const float2*>(psi_f_dev), k->H * k->W, batch,
-                                       (float)(1.0 / denom), sample_weights_dev, nullptr, k->dO, k->sums);
-  sum_blocks_kernel<<<1, 32, 0, st>>>(k->sums, (int)nblk, 1.0, loss_out_dev ? loss_out_dev : k->loss);
-  rc = backward(k, batch, st);
-  return rc;
+  k->S_last = samples;
+  NN_CUDA(cudaMemcpyAsync(maps_out_dev, k->o, sizeof(float) * samples * k->P * 4, cudaMemcpyDeviceToDevice, st));
+  return MSX_OK;
+}
+
+int msx_corrector_backward(msx_corrector* k, const float* dmaps_dev, void* stream) {
+  if (!k || !dmaps_dev || k->S_last < 1) return cfail(MSX_ERR_INVALID, "corrector backward: run forward first");
+  return backward(k, dmaps_dev, (cudaStream_t)stream);
 }
 
 int msx_corrector_adam(msx_corrector* k, float lr, float beta1, float beta2, float eps, void* stream) {
@@ -620,6 +602,98 @@ int msx_corrector_adam(msx_corrector* k, float lr, float beta1, float beta2, flo
   const float c1 = 1.f - powf(beta1, (float)k->step), c2 = 1.f - powf(beta2, (float)k->step);
   adam_kernel<<<blocks_for((long long)k->nparams, 256), 256, 0, (cudaStream_t)stream>>>(
       k->params, k->grads, k->m, k->v, (long long)k->nparams, lr, beta1, beta2, eps, c1, c2);
+  NN_CUDA(cudaGetLastError());
+  return MSX_OK;
+}
+
+int msx_corrector_check(msx_corrector* k) {
+  if (!k) return cfail(MSX_ERR_INVALID, "null corrector");
+  NN_CUDA(cudaDeviceSynchronize());
+  const int rc = k->gemm.check();
+  if (rc == MSX_ERR_TIMEOUT) return cfail(rc, "a tensor-core GEMM wait of the corrector gave up");
+  return rc;
+}
+
+int msx_corrector_features(const float* pot_dev, int samples, int ratio, int ny, int nx, float sigma, float tval,
+                           float* features_out_dev, void* stream) {
+  if (!pot_dev || !features_out_dev || samples < 1 || ratio < 1 || ratio > 62 || ny < 1 || nx < 1)
+    return cfail(MSX_ERR_INVALID, "corrector features: bad arguments");
+  const long long P = (long long)ny * nx;
+  features_kernel<<<blocks_for((long long)samples * P, 256), 256, 0, (cudaStream_t)stream>>>(pot_dev, samples, ratio, P,
+                                                                                             sigma, tval,
+                                                                                             features_out_dev);
+  NN_CUDA(cudaGetLastError());
+  return MSX_OK;
+}
+
+int msx_corrector_apply_map(float* waves_dev, int num, int ny, int nx, const float* maps_dev, int which, int conj,
+                            void* stream) {
+  if (!waves_dev || !maps_dev || num < 0 || ny < 1 || nx < 1 || (which != 0 && which != 1))
+    return cfail(MSX_ERR_INVALID, "corrector apply map: bad arguments");
+  const long long P = (long long)ny * nx;
+  if (num == 0) return MSX_OK;
+  map_mul_kernel<<<blocks_for((long long)num * P, 256), 256, 0, (cudaStream_t)stream>>>(
+      reinterpret_cast<float2*>(waves_dev), num, P, maps_dev, which, conj ? 1 : 0);
+  NN_CUDA(cudaGetLastError());
+  return MSX_OK;
+}
+
+int msx_corrector_mul_plane(float* waves_dev, int num, int ny, int nx, const float* plane_dev, int conj,
+                            void* stream) {
+  if (!waves_dev || !plane_dev || num < 0 || ny < 1 || nx < 1)
+    return cfail(MSX_ERR_INVALID, "corrector plane product: bad arguments");
+  const long long P = (long long)ny * nx;
+  if (num == 0) return MSX_OK;
+  plane_mul_kernel<<<blocks_for((long long)num * P, 256), 256, 0, (cudaStream_t)stream>>>(
+      reinterpret_cast<float2*>(waves_dev), (long long)num * P, P, reinterpret_cast<const float2*>(plane_dev),
+      conj ? 1 : 0);
+  NN_CUDA(cudaGetLastError());
+  return MSX_OK;
+}
+
+int msx_corrector_map_trans(const float* trans_dev, int ny, int nx, const float* maps_dev, int which, float* out_dev,
+                            void* stream) {
+  if (!trans_dev || !maps_dev || !out_dev || ny < 1 || nx < 1 || (which != 0 && which != 1))
+    return cfail(MSX_ERR_INVALID, "corrector map transmission: bad arguments");
+  const long long P = (long long)ny * nx;
+  map_trans_kernel<<<blocks_for(P, 256), 256, 0, (cudaStream_t)stream>>>(reinterpret_cast<const float2*>(trans_dev), P,
+                                                                         maps_dev, which,
+                                                                         reinterpret_cast<float2*>(out_dev));
+  NN_CUDA(cudaGetLastError());
+  return MSX_OK;
+}
+
+int msx_corrector_map_grad(const float* u_dev, const float* g_dev, int num, int ny, int nx, int which, int accumulate,
+                           float* dmaps_dev, void* stream) {
+  if (!u_dev || !g_dev || !dmaps_dev || num < 1 || ny < 1 || nx < 1 || (which != 0 && which != 1))
+    return cfail(MSX_ERR_INVALID, "corrector map gradient: bad arguments");
+  const long long P = (long long)ny * nx;
+  map_grad_kernel<<<blocks_for(P, 256), 256, 0, (cudaStream_t)stream>>>(reinterpret_cast<const float2*>(u_dev),
+                                                                        reinterpret_cast<const float2*>(g_dev), num, P,
+                                                                        which, accumulate ? 1 : 0, dmaps_dev);
+  NN_CUDA(cudaGetLastError());
+  return MSX_OK;
+}
+
+int msx_corrector_residual(const float* psi_dev, const float* target_dev, int num, int ny, int nx, float weight,
+                           int accumulate, float* adjoint_dev, float* loss_out_dev, void* stream) {
+  if (!psi_dev || !target_dev || !adjoint_dev || !loss_out_dev || num < 1 || ny < 1 || nx < 1)
+    return cfail(MSX_ERR_INVALID, "corrector residual: bad arguments");
+  const long long n = (long long)num * ny * nx;
+  const unsigned nb = blocks_for(n, 256);
+  thread_local double* sums = nullptr;
+  thread_local size_t cap = 0;
+  if (nb > cap) {
+    if (sums) cudaFree(sums);
+    sums = nullptr;
+    cap = 0;
+    if (cudaMalloc(&sums, nb * sizeof(double)) != cudaSuccess) return cfail(MSX_ERR_ALLOC, "loss partials");
+    cap = nb;
+  }
+  cudaStream_t st = (cudaStream_t)stream;
+  resid_kernel<<<nb, 256, 0, st>>>(reinterpret_cast<const float2*>(psi_dev), reinterpret_cast<const float2*>(target_dev),
+                                   n, weight, accumulate ? 1 : 0, reinterpret_cast<float2*>(adjoint_dev), sums);
+  sum_blocks_kernel<<<1, 32, 0, st>>>(sums, (int)nb, loss_out_dev);
   NN_CUDA(cudaGetLastError());
   return MSX_OK;
 }

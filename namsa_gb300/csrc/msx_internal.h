@@ -23,4 +23,47 @@ cudaError_t launch_pfac(int Ny, int Nx, float kmax, double lambda, double slice_
 cudaError_t launch_ptab(int Ny, int Nx, float kmax, double lambda, double slice_t, float k_band, float2* ptab,
                         cudaStream_t st);
 
+// Strided addressing of a matrix element (r, k):
+//   (r / rc) * s1 + (r % rc) * s2 + (k / kc) * t1 + (k % kc) * t2.
+struct Addr {
+  long long s1, s2, rc;
+  long long t1, t2, kc;
+};
+// Row-major with leading dimension ld.
+inline Addr rowmajor(long long ld) { return Addr{ld, 0, 1, 1, 0, 1}; }
+// Element (r, k) at r + k * ld (column-major / transposed operand).
+inline Addr colmajor(long long ld) { return Addr{1, 0, 1, ld, 0, 1}; }
+
+// Epilogue of the tensor-core GEMM: z = scale * acc (+ bias[c]) (+ add[o]) (+ y[o] when accumulate);
+// y[o] = z; act[o] = gelu(z) when act is set; o is the address of (r, c) under `out`.
+struct Epi {
+  float* y;
+  Addr out;
+  long long M;
+  int N;
+  const float* bias;
+  const float* add;
+  float* act;
+  int accumulate;
+  float scale;
+};
+
+// D (M x N) = A (M x K) . B (N x K)^T on tcgen05 in bfloat16 with FP32 accumulation
+// (msx_tcgemm.cu).  Operand images and the error word are owned by the object.
+struct TcGemm {
+  void* a_img = nullptr;
+  void* b_img = nullptr;
+  size_t a_cap = 0, b_cap = 0;
+  int* err = nullptr;
+  int reserve(size_t a_bytes, size_t b_bytes);
+  float* part = nullptr;  // split-K partial sums
+  size_t part_cap = 0;
+  // ksplit > 1 splits K over that many CTAs per tile; partial tiles are summed
+  // in a fixed order before the epilogue (for the long-K weight gradients).
+  int run(const float* a, Addr aa, const float* b, Addr ba, long long M, int N, long long K, const Epi& e,
+          cudaStream_t st, int ksplit = 1);
+  int check();
+  void release();
+};
+
 }  // namespace msx

@@ -186,6 +186,28 @@ def step_waves_tc(waves, trans, ptab):
     return waves
 
 
+def gemm_bf16(a, b, bias=None, out=None, accumulate=False):
+    """a (m, k) @ b (n, k)^T (+ bias) in bfloat16 with FP32 accumulation on the
+    tensor cores; FP32 row-major tensors (rows may be strided)."""
+    for t, name in ((a, 'a'), (b, 'b')):
+        if not (isinstance(t, torch.Tensor) and t.is_cuda and t.dtype == torch.float32 and t.dim() == 2
+                and t.stride(1) == 1):
+            raise TypeError(f'{name} must be a 2-D float32 CUDA tensor with unit column stride')
+    m, k = a.shape
+    n, k2 = b.shape
+    if k2 != k:
+        raise ValueError('inner dimensions differ')
+    if out is None:
+        out = torch.zeros((m, n), dtype=torch.float32, device=a.device)
+    _lib.check(lib().msx_gemm_bf16(_ptr(a), a.stride(0), _ptr(b), b.stride(0), m, n, k, _ptr(out), out.stride(0),
+                                   _ptr(bias), int(bool(accumulate)), _stream()))
+    return out
+
+
+def gemm_check():
+    _lib.check(lib().msx_gemm_check())
+
+
 def tc_set_compensation(enable):
     """Per-line norm compensation of the tensor-core DFTs (default on) for this host thread."""
     _lib.check(lib().msx_tc_set_compensation(int(bool(enable))))
@@ -444,14 +466,18 @@ class _DevView:
 
 
 class Corrector:
-    """Learned coarse-slice corrector (spectral-convolution network) of libmsx."""
+    """Learned coarse-slice corrector network of libmsx (msx_corrector_*): maps
+    the features of S coarse slices (S, ny, nx, in_channels) to the correction
+    maps (S, ny, nx, 4) = (Re A, Im A, Re B, Im B) of the corrected coarse step
+    psi <- (1 + A) ifft2(P_c fft2((1 + B) t_c psi))."""
 
-    def __init__(self, ny, nx, channels=32, layers=4, max_batch=8):
+    def __init__(self, ny, nx, in_channels=6, channels=32, layers=4, modes_x=32, modes_y=64, max_samples=16):
         h = _vp()
-        _lib.check(lib().msx_corrector_create(int(ny), int(nx), int(channels), int(layers), int(max_batch),
-                                              ctypes.byref(h)))
+        _lib.check(lib().msx_corrector_create(int(ny), int(nx), int(in_channels), int(channels), int(layers),
+                                              int(modes_x), int(modes_y), int(max_samples), ctypes.byref(h)))
         self._h = h
-        self.ny, self.nx, self.channels, self.layers, self.max_batch = ny, nx, channels, layers, max_batch
+        self.ny, self.nx, self.in_channels, self.channels, self.layers = ny, nx, in_channels, channels, layers
+        self.modes_x, self.modes_y, self.max_samples = modes_x, modes_y, max_samples
         p, g = _vp(), _vp()
         n = ctypes.c_size_t()
         _lib.check(lib().msx_corrector_params(self._h, ctypes.byref(p), ctypes.byref(g), ctypes.byref(n)))
@@ -459,6 +485,25 @@ class Corrector:
         self.count = n.value
         self.params = torch.as_tensor(_DevView(p.value, n.value), device=dev)
         self.grads = torch.as_tensor(_DevView(g.value, n.value), device=dev)
+        offs = (ctypes.c_size_t * (6 + 3 * layers))()
+        _lib.check(lib().msx_corrector_layout(self._h, offs, 6 + 3 * layers))
+        self.offsets = [int(o) for o in offs]
+
+    def views(self, flat=None):
+        """Named views (W0, b0, R1, W1, b1, ..., P1, c1, P2, c2) into `flat` (default: the parameters)."""
+        flat = self.params if flat is None else flat
+        C, Ci, L = self.channels, self.in_channels, self.layers
+        shapes = [('W0', (C, Ci)), ('b0', (C,))]
+        for l in range(L):
+            shapes += [(f'R{l + 1}', (self.modes_x, self.modes_y, C, C, 2)), (f'W{l + 1}', (C, C)), (f'b{l + 1}', (C,))]
+        shapes += [('P1', (C, C)), ('c1', (C,)), ('P2', (4, C)), ('c2', (4,))]
+        out = {}
+        for (name, shape), off in zip(shapes, self.offsets):
+            n = 1
+            for d in shape:
+                n *= d
+            out[name] = flat[off:off + n].view(shape)
+        return out
 
     def close(self):
         if getattr(self, '_h', None) is not None:
@@ -471,26 +516,85 @@ class Corrector:
         except Exception:
             pass
 
-    def forward(self, psi_c, tc, out=None):
-        _need(psi_c, torch.complex64, 'psi_c', 3)
-        _need(tc, torch.complex64, 'tc', 3)
+    def forward(self, features, out=None):
+        _need(features, torch.float32, 'features', 4)
+        S = features.shape[0]
+        if tuple(features.shape[1:]) != (self.ny, self.nx, self.in_channels):
+            raise ValueError(f'features must be (S, {self.ny}, {self.nx}, {self.in_channels})')
         if out is None:
-            out = torch.empty_like(psi_c)
-        _lib.check(lib().msx_corrector_forward(self._h, _ptr(psi_c), _ptr(tc), psi_c.shape[0], _ptr(out), _stream()))
+            out = torch.empty((S, self.ny, self.nx, 4), dtype=torch.float32, device=features.device)
+        _lib.check(lib().msx_corrector_forward(self._h, _ptr(features), S, _ptr(out), _stream()))
         return out
 
-    def loss_grad(self, psi_c, tc, psi_f, denom, weights=None, loss_out=None):
-        """Loss sum_b w_b |pred_b - psi_f_b|^2 / denom and the parameter gradients."""
-        _need(psi_c, torch.complex64, 'psi_c', 3)
-        _need(tc, torch.complex64, 'tc', 3)
-        _need(psi_f, torch.complex64, 'psi_f', 3)
-        if weights is not None:
-            _need(weights, torch.float32, 'weights', 1)
-        if loss_out is None:
-            loss_out = torch.empty(1, dtype=torch.float32, device=psi_c.device)
-        _lib.check(lib().msx_corrector_loss_grad(self._h, _ptr(psi_c), _ptr(tc), _ptr(psi_f), psi_c.shape[0],
-                                                 float(denom), _ptr(weights), _ptr(loss_out), _stream()))
-        return loss_out
+    def backward(self, dmaps):
+        """Parameter gradients (into self.grads) for d loss / d maps of the last forward."""
+        _need(dmaps, torch.float32, 'dmaps', 4)
+        _lib.check(lib().msx_corrector_backward(self._h, _ptr(dmaps), _stream()))
 
     def adam(self, lr=1e-3, beta1=0.9, beta2=0.999, eps=1e-8):
         _lib.check(lib().msx_corrector_adam(self._h, float(lr), float(beta1), float(beta2), float(eps), _stream()))
+
+    def check(self):
+        _lib.check(lib().msx_corrector_check(self._h))
+
+
+def corrector_features(pot, ratio, sigma, tval, out=None):
+    """Network inputs (S, ny, nx, ratio + 2) of S = pot.shape[0] // ratio coarse slices
+    from fine potential slices pot (S * ratio, ny, nx) float32."""
+    _need(pot, torch.float32, 'pot', 3)
+    S = pot.shape[0] // ratio
+    ny, nx = pot.shape[1], pot.shape[2]
+    if out is None:
+        out = torch.empty((S, ny, nx, ratio + 2), dtype=torch.float32, device=pot.device)
+    _lib.check(lib().msx_corrector_features(_ptr(pot), S, int(ratio), ny, nx, float(sigma), float(tval), _ptr(out),
+                                            _stream()))
+    return out
+
+
+def apply_map(waves, maps, which, conj=False):
+    """waves (num, ny, nx) complex64 *= (1 + M) (or its conjugate); maps (ny, nx, 4), M = A (0) or B (1)."""
+    _need(waves, torch.complex64, 'waves', 3)
+    _need(maps, torch.float32, 'maps', 3)
+    _lib.check(lib().msx_corrector_apply_map(_ptr(waves), waves.shape[0], waves.shape[1], waves.shape[2], _ptr(maps),
+                                             int(which), int(bool(conj)), _stream()))
+    return waves
+
+
+def mul_plane(waves, plane, conj=False):
+    """waves (num, ny, nx) complex64 *= plane (ny, nx) complex64 (or its conjugate)."""
+    _need(waves, torch.complex64, 'waves', 3)
+    _need(plane, torch.complex64, 'plane', 2)
+    _lib.check(lib().msx_corrector_mul_plane(_ptr(waves), waves.shape[0], waves.shape[1], waves.shape[2], _ptr(plane),
+                                             int(bool(conj)), _stream()))
+    return waves
+
+
+def map_trans(trans, maps, which, out=None):
+    """trans (ny, nx) complex64 times (1 + M)."""
+    _need(trans, torch.complex64, 'trans', 2)
+    _need(maps, torch.float32, 'maps', 3)
+    if out is None:
+        out = torch.empty_like(trans)
+    _lib.check(lib().msx_corrector_map_trans(_ptr(trans), trans.shape[0], trans.shape[1], _ptr(maps), int(which),
+                                             _ptr(out), _stream()))
+    return out
+
+
+def map_grad(u, g, which, dmaps, accumulate=False):
+    """dmaps (ny, nx, 4)[.., M] (+)= 2 sum_b conj(u_b) g_b."""
+    _need(u, torch.complex64, 'u', 3)
+    _need(g, torch.complex64, 'g', 3)
+    _need(dmaps, torch.float32, 'dmaps', 3)
+    _lib.check(lib().msx_corrector_map_grad(_ptr(u), _ptr(g), u.shape[0], u.shape[1], u.shape[2], int(which),
+                                            int(bool(accumulate)), _ptr(dmaps), _stream()))
+    return dmaps
+
+
+def residual(psi, target, weight, adjoint, loss_out, accumulate=False):
+    """adjoint (+)= weight (psi - target); loss_out[0] = weight sum |psi - target|^2."""
+    _need(psi, torch.complex64, 'psi', 3)
+    _need(target, torch.complex64, 'target', 3)
+    _need(adjoint, torch.complex64, 'adjoint', 3)
+    _lib.check(lib().msx_corrector_residual(_ptr(psi), _ptr(target), psi.shape[0], psi.shape[1], psi.shape[2],
+                                            float(weight), int(bool(accumulate)), _ptr(adjoint), _ptr(loss_out),
+                                            _stream()))

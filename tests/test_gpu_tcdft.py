@@ -87,3 +87,25 @@ def test_tc_dft_norm_compensation_keeps_parseval():
     assert np.abs(r0 - 1).mean() > np.abs(r1 - 1).mean()
     ref = np.fft.fft(x.astype(np.complex128), axis=1)
     assert np.linalg.norm(z1 - ref) / np.linalg.norm(ref) < 5e-5
+
+
+@pytest.mark.parametrize('m,n,k', [(128, 32, 64), (300, 64, 100), (1000, 4, 32), (256, 200, 512), (129, 256, 64), (32, 40, 20000),
+                                   (64, 640, 192)])
+def test_gemm_bf16_matches_fp32_matmul_of_rounded_operands(m, n, k):
+    """The general tcgen05 GEMM against a plain PyTorch FP32 matmul of the same
+    bfloat16-rounded operands (only the accumulation order differs)."""
+    g = torch.Generator().manual_seed(m + n + k)
+    a = torch.randn(m, k, generator=g).to(DEV)
+    b = torch.randn(n, k, generator=g).to(DEV)
+    bias = torch.randn(n, generator=g).to(DEV)
+    ref = a.to(torch.bfloat16).float() @ b.to(torch.bfloat16).float().T + bias
+    got = engine.gemm_bf16(a, b, bias)
+    engine.gemm_check()
+    assert torch.allclose(got, ref, rtol=1e-4, atol=1e-4 * k ** 0.5), (got - ref).abs().max().item()
+    # accumulate into a strided output view
+    big = torch.ones(m, n + 7, device=DEV)
+    out = big[:, 3:3 + n]
+    engine.gemm_bf16(a, b, None, out=out, accumulate=True)
+    torch.cuda.synchronize()
+    assert torch.allclose(out, ref - bias + 1, rtol=1e-4, atol=1e-4 * k ** 0.5)
+    assert (big[:, :3] == 1).all() and (big[:, 3 + n:] == 1).all()
