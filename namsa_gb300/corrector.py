@@ -86,7 +86,7 @@ class Crystal:
         self.kmax, self.kband = kmax, kband
         self.ptab_fine = engine.propagator_table(n, n, kmax, self.sim.Lambda, slice_t, kband)
         self.ptab_coarse = engine.propagator_table(n, n, kmax, self.sim.Lambda, ratio * slice_t, kband)
-        self.ptab_coarse_adj = torch.conj(self.ptab_coarse).contiguous()
+        self.ptab_coarse_adj = torch.conj_physical(self.ptab_coarse)
         self.ones = torch.ones((n, n), dtype=torch.complex64, device=self.trans_fine.device)
         self.plan = engine.Plan(n, n)
         self._features = None
@@ -183,7 +183,8 @@ class RolloutTrainer:
         self.n = n
 
     def step(self, lr, windows=2):
-        """One Adam step on `windows` random rollout windows; returns the mean relative error per step."""
+        """One Adam step on `windows` random rollout windows; returns the loss, the mean
+        over windows and steps of the squared relative wave error."""
         net, K, B = self.net, self.K, self.B
         picks = []
         for _ in range(windows):
@@ -201,9 +202,12 @@ class RolloutTrainer:
             total += self._window(cr, tr, k0, b, maps[w * K:(w + 1) * K], dmaps[w * K:(w + 1) * K])
         net.backward(dmaps)
         net.adam(lr=lr)
-        return total / (windows * K)
+        return total / windows
 
     def _window(self, cr, tr, k0, b, maps, dmaps):
+        """Rollout of K corrected steps from the fine wave at coarse depth k0 (waves b);
+        writes d loss / d maps into dmaps and returns the loss, the mean over steps of
+        |psi_k - f_k|^2 / |f_k|^2."""
         K, n = self.K, self.n
         psi = tr[k0][b].contiguous()
         nb = psi.shape[0]
@@ -223,7 +227,7 @@ class RolloutTrainer:
             target = tr[s + 1][b].contiguous()
             denom = float(target.abs().pow(2).sum().item())
             engine.residual(psi, target, 1.0 / (K * denom), adj[k + 1], self.loss_buf)
-            loss += float(self.loss_buf.item()) * K
+            loss += float(self.loss_buf.item())
         g = adj[K].clone()
         for k in range(K - 1, -1, -1):
             engine.map_grad(u[k], g, 0, dmaps[k])
