@@ -446,6 +446,56 @@ def run_ours(args):
         dist.destroy_process_group()
 
 
+def uneven_breakdown(jobs, batch_ms, reps=3):
+    """Per grid size: the batch's jobs run one at a time through an autotuned plan of
+    that size (the standalone time of each job), and the same probe-slices at the rate
+    of a homogeneous 512-position run of that size (the matched homogeneous time)."""
+    import torch
+    from namsa_gb300 import engine
+    st = torch.cuda.current_stream()
+    out = {}
+    for n in sorted({j['trans'].shape[1] for j in jobs}):
+        js = [j for j in jobs if j['trans'].shape[1] == n]
+        big = max(js, key=lambda j: j['positions'].shape[0])
+        plan = engine.Plan(n, n)
+        plan.autotune(big['trans'], big['psik'], big['norm'], big['positions'], big['kmax'], big['lam'],
+                      big['slice_t'], big['k_band'])
+
+        def timed_ms(fn):
+            fn()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(st)
+            for _ in range(reps):
+                fn()
+            e1.record(st)
+            torch.cuda.synchronize()
+            return e0.elapsed_time(e1) / reps
+        alone = 0.0
+        pslices = 0
+        for j in js:
+            alone += timed_ms(lambda j=j: plan.multislice(j['trans'], j['psik'], j['norm'], j['positions'], j['kmax'],
+                                                          j['lam'], j['slice_t'], j['k_band'], out=j['out']))
+            pslices += j['positions'].shape[0] * j['trans'].shape[0]
+        # homogeneous rate: 512 positions through the first (up to) 32 slices of the largest job
+        S = min(32, big['trans'].shape[0])
+        pos = big['positions'][torch.arange(512, device=big['positions'].device) % big['positions'].shape[0]]
+        pos = (pos + 0.01 * torch.arange(512, device=pos.device, dtype=torch.float32)[:, None]).contiguous()
+        plan2 = engine.Plan(n, n)
+        plan2.autotune(big['trans'][:S].contiguous(), big['psik'], big['norm'], pos, big['kmax'], big['lam'],
+                       big['slice_t'], big['k_band'])
+        hom = timed_ms(lambda: plan2.multislice(big['trans'][:S].contiguous(), big['psik'], big['norm'], pos,
+                                                big['kmax'], big['lam'], big['slice_t'], big['k_band']))
+        ns_ps = hom * 1e6 / (512 * S)
+        out[str(n)] = {'jobs': len(js), 'probe_slices': pslices, 'standalone_ms': alone,
+                       'homogeneous_ns_per_probe_slice': ns_ps, 'matched_homogeneous_ms': pslices * ns_ps / 1e6}
+        plan.close()
+        plan2.close()
+    tot_alone = sum(v['standalone_ms'] for v in out.values())
+    tot_hom = sum(v['matched_homogeneous_ms'] for v in out.values())
+    return {'per_grid': out, 'batch_ms': batch_ms, 'sum_standalone_ms': tot_alone, 'sum_matched_homogeneous_ms': tot_hom,
+            'batch_rate_vs_standalone': tot_alone / batch_ms, 'batch_rate_vs_matched_homogeneous': tot_hom / batch_ms}
+
+
 def run_uneven(args):
     """64 seeded random crystals (grids 256..768^2, 50-500 A, 80-300 kV, 16-256
     positions each) in one graph-captured batch; probes/s over the whole batch."""
@@ -482,13 +532,14 @@ def run_uneven(args):
     grids = {}
     for s in specs:
         grids[s['n']] = grids.get(s['n'], 0) + 1
+    breakdown = uneven_breakdown(jobs, ms) if args.autotune else None
     line = {'metric': METRIC, 'value': P / (ms / 1e3), 'unit': UNIT, 'n_gpus': 1, 'steps': args.steps,
             'warmup': args.warmup, 'ms_per_step': ms, 'higher_is_better': True, 'scaling': 'weak',
             'vs_baseline': None, 'dtype': 'c64', 'data': 'synthetic (64 seeded random cubic crystals)',
             'config': {'workload': 'uneven batch of 64 random crystals, one CUDA graph', 'probes': P,
                        'probe_slices': ps, 'probe_slice_pixels_per_s': psp / (ms / 1e3),
                        'grids': grids, 'branches': args.branches, 'build_s': build_s,
-                       'autotune_s': tuned}}
+                       'autotune_s': tuned, 'breakdown': breakdown}}
     print(json.dumps(line), flush=True)
     batch.close()
 
@@ -547,7 +598,8 @@ def run_corrector(args):
                 'corrected_probes_per_s': len(pos) / t_corr,
                 'speedup_corrected_vs_fine': t_fine / t_corr,
                 'speedup_incl_network_per_1024_positions': (t_fine * 1024 / len(pos)) /
-                                                           (t_corr * 1024 / len(pos) + net_s)}
+                                                           (t_corr * 1024 / len(pos) +
+                                                            net_s * steps / cr.coarse_steps)}
         res[name] = out
     si = res['Si[001]']['1000A']
     line = {'metric': METRIC, 'value': si['corrected_probes_per_s'], 'unit': UNIT, 'n_gpus': 1,
