@@ -69,6 +69,9 @@ def parse():
     p.add_argument('--workload', default='scan', choices=['scan', 'uneven', 'corrector', 'precision'],
                    help='scan: the 512^2 Si [001] 1024-position scan; uneven: 64 seeded random crystals in one batch')
     p.add_argument('--branches', type=int, default=4, help='concurrent graph branches of the uneven batch')
+    p.add_argument('--corr-iters', type=int, default=0, help='corrector training iterations (0 = 300 x steps)')
+    p.add_argument('--corr-window', type=int, default=8, help='corrected coarse steps per training rollout window')
+    p.add_argument('--corr-positions', type=int, default=64, help='held-out positions of the corrector evaluation')
     return p.parse_args()
 
 
@@ -567,10 +570,10 @@ def run_corrector(args):
     torch.cuda.synchronize()
     gen_s = time.perf_counter() - t0
     pairs = int(sum((tr.shape[0] - 1) * tr.shape[1] for tr in trajs))
-    net = engine.Corrector(n, n, 6, C, L, 32, 64, max_samples=16)
+    net = engine.Corrector(n, n, 6, C, L, 32, 64, max_samples=max(16, 2 * args.corr_window))
     net.params.copy_(torch.from_numpy(CR.init_params(net, seed=0)))
-    trainer = CR.RolloutTrainer(net, [c for _, c, _ in crystals], trajs, window=8, waves=8, seed=0)
-    iters = max(1, args.steps) * 300
+    trainer = CR.RolloutTrainer(net, [c for _, c, _ in crystals], trajs, window=args.corr_window, waves=8, seed=0)
+    iters = args.corr_iters if args.corr_iters > 0 else max(1, args.steps) * 300
     t1 = time.perf_counter()
     losses = [trainer.step(lr=2e-3 * 0.5 * (1 + math.cos(math.pi * i / iters))) for i in range(iters)]
     torch.cuda.synchronize()
@@ -578,7 +581,7 @@ def run_corrector(args):
     net.check()
     res = {}
     for name, cr, a in crystals[:2]:
-        pos = np.random.default_rng(7).uniform(0, a, size=(64, 2))
+        pos = np.random.default_rng(7).uniform(0, a, size=(args.corr_positions, 2))
         t2 = time.perf_counter()
         maps = CR.crystal_maps(net, cr)
         torch.cuda.synchronize()
@@ -609,6 +612,7 @@ def run_corrector(args):
             'config': {'workload': 'learned coarse-slice corrector, 256^2, 200 keV, 4x slices', 'pairs': pairs,
                        'generate_s': gen_s, 'train_s': train_s, 'train_iters': iters,
                        'loss_first': float(np.mean(losses[:10])), 'loss_last': float(np.mean(losses[-50:])),
+                       'window': args.corr_window,
                        'channels': C, 'layers': L, 'modes': '32 x 64 (kx x ky)', 'results': res}}
     print(json.dumps(line), flush=True)
     net.close()
