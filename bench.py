@@ -69,8 +69,8 @@ def parse():
     p.add_argument('--workload', default='scan', choices=['scan', 'uneven', 'corrector', 'precision'],
                    help='scan: the 512^2 Si [001] 1024-position scan; uneven: 64 seeded random crystals in one batch')
     p.add_argument('--branches', type=int, default=4, help='concurrent graph branches of the uneven batch')
-    p.add_argument('--corr-iters', type=int, default=0, help='corrector training iterations (0 = 300 x steps)')
-    p.add_argument('--corr-window', type=int, default=8, help='corrected coarse steps per training rollout window')
+    p.add_argument('--corr-iters', type=int, default=0, help='corrector training iterations (0 = 600 x steps)')
+    p.add_argument('--corr-window', type=int, default=16, help='corrected coarse steps per training rollout window')
     p.add_argument('--corr-positions', type=int, default=64, help='held-out positions of the corrector evaluation')
     return p.parse_args()
 
@@ -566,14 +566,14 @@ def run_corrector(args):
     for name, sites, t, a in specs:
         cr = CR.Crystal(sites, n, t)
         crystals.append((name, cr, a))
-        trajs.append(cr.trajectory(rng.uniform(0, a, size=(20, 2))))
+        trajs.append(cr.trajectory(rng.uniform(0, a, size=(22, 2))))
     torch.cuda.synchronize()
     gen_s = time.perf_counter() - t0
     pairs = int(sum((tr.shape[0] - 1) * tr.shape[1] for tr in trajs))
     net = engine.Corrector(n, n, 6, C, L, 32, 64, max_samples=max(16, 2 * args.corr_window))
     net.params.copy_(torch.from_numpy(CR.init_params(net, seed=0)))
     trainer = CR.RolloutTrainer(net, [c for _, c, _ in crystals], trajs, window=args.corr_window, waves=8, seed=0)
-    iters = args.corr_iters if args.corr_iters > 0 else max(1, args.steps) * 300
+    iters = args.corr_iters if args.corr_iters > 0 else max(1, args.steps) * 600
     t1 = time.perf_counter()
     losses = [trainer.step(lr=2e-3 * 0.5 * (1 + math.cos(math.pi * i / iters))) for i in range(iters)]
     torch.cuda.synchronize()

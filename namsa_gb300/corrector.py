@@ -127,6 +127,19 @@ class Crystal:
         return out
 
 
+def wave_norms(traj):
+    """sum |f|^2 of every wave of a trajectory (steps + 1, P, n, n), as a host array (steps + 1, P)."""
+    zero = torch.zeros_like(traj[0, :1])
+    adj = torch.empty_like(zero)
+    buf = torch.zeros(1, dtype=torch.float32, device=traj.device)
+    out = np.zeros(traj.shape[:2])
+    for k in range(traj.shape[0]):
+        for p in range(traj.shape[1]):
+            engine.residual(zero, traj[k, p:p + 1], 1.0, adj, buf)
+            out[k, p] = float(buf.item())
+    return out
+
+
 def crystal_maps(net, crystal):
     """Correction maps of every coarse slice of a crystal (the network runs once per slice)."""
     f = crystal.features()
@@ -175,6 +188,7 @@ class RolloutTrainer:
 
     def __init__(self, net, crystals, trajectories, window=8, waves=8, seed=0):
         self.net, self.crystals, self.traj = net, crystals, trajectories
+        self.norms = [wave_norms(t) for t in trajectories]
         self.K, self.B = window, waves
         self.rng = np.random.default_rng(seed)
         n = crystals[0].n
@@ -191,20 +205,20 @@ class RolloutTrainer:
             c = int(self.rng.integers(len(self.crystals)))
             cr, tr = self.crystals[c], self.traj[c]
             k0 = int(self.rng.integers(0, tr.shape[0] - K))
-            b = torch.as_tensor(self.rng.choice(tr.shape[1], size=min(B, tr.shape[1]), replace=False),
-                                device=tr.device)
-            picks.append((cr, tr, k0, b))
-        feats = torch.cat([cr.features()[k0:k0 + K] for cr, tr, k0, b in picks]).contiguous()
+            bi = self.rng.choice(tr.shape[1], size=min(B, tr.shape[1]), replace=False)
+            b = torch.as_tensor(bi, device=tr.device)
+            picks.append((cr, tr, k0, b, self.norms[c][:, bi].sum(1)))
+        feats = torch.cat([cr.features()[k0:k0 + K] for cr, tr, k0, b, nrm in picks]).contiguous()
         maps = net.forward(feats)
         dmaps = torch.zeros_like(maps)
         total = 0.0
-        for w, (cr, tr, k0, b) in enumerate(picks):
-            total += self._window(cr, tr, k0, b, maps[w * K:(w + 1) * K], dmaps[w * K:(w + 1) * K])
+        for w, (cr, tr, k0, b, nrm) in enumerate(picks):
+            total += self._window(cr, tr, k0, b, maps[w * K:(w + 1) * K], dmaps[w * K:(w + 1) * K], nrm)
         net.backward(dmaps)
         net.adam(lr=lr)
         return total / windows
 
-    def _window(self, cr, tr, k0, b, maps, dmaps):
+    def _window(self, cr, tr, k0, b, maps, dmaps, norms=None):
         """Rollout of K corrected steps from the fine wave at coarse depth k0 (waves b);
         writes d loss / d maps into dmaps and returns the loss, the mean over steps of
         |psi_k - f_k|^2 / |f_k|^2."""
@@ -225,7 +239,11 @@ class RolloutTrainer:
             u[k].copy_(psi)
             engine.apply_map(psi, maps[k], 0)
             target = tr[s + 1][b].contiguous()
-            denom = float(target.abs().pow(2).sum().item())
+            if norms is None:
+                engine.residual(torch.zeros_like(target), target, 1.0, adj[k + 1], self.loss_buf)
+                denom = float(self.loss_buf.item())
+            else:
+                denom = float(norms[s + 1])
             engine.residual(psi, target, 1.0 / (K * denom), adj[k + 1], self.loss_buf)
             loss += float(self.loss_buf.item())
         g = adj[K].clone()

@@ -235,11 +235,19 @@ __global__ void resid_kernel(const float2* __restrict__ psi, const float2* __res
   if (threadIdx.x == 0) sums[blockIdx.x] = red[0];
 }
 
+// out[0] = sum of s[0..n): one block of 256 threads, strided partial sums then a
+// fixed-order tree, so the result does not depend on timing.
 __global__ void sum_blocks_kernel(const double* __restrict__ s, int n, float* __restrict__ out) {
-  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  __shared__ double red[256];
   double acc = 0;
-  for (int i = 0; i < n; ++i) acc += s[i];
-  out[0] = (float)acc;
+  for (int i = threadIdx.x; i < n; i += 256) acc += s[i];
+  red[threadIdx.x] = acc;
+  __syncthreads();
+  for (int w = 128; w > 0; w >>= 1) {
+    if ((int)threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) out[0] = (float)red[0];
 }
 
 }  // namespace nn
@@ -693,7 +701,7 @@ int msx_corrector_residual(const float* psi_dev, const float* target_dev, int nu
   cudaStream_t st = (cudaStream_t)stream;
   resid_kernel<<<nb, 256, 0, st>>>(reinterpret_cast<const float2*>(psi_dev), reinterpret_cast<const float2*>(target_dev),
                                    n, weight, accumulate ? 1 : 0, reinterpret_cast<float2*>(adjoint_dev), sums);
-  sum_blocks_kernel<<<1, 32, 0, st>>>(sums, (int)nb, loss_out_dev);
+  sum_blocks_kernel<<<1, 256, 0, st>>>(sums, (int)nb, loss_out_dev);
   NN_CUDA(cudaGetLastError());
   return MSX_OK;
 }

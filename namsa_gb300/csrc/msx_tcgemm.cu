@@ -67,24 +67,42 @@ __host__ __device__ __forceinline__ long long addr_of(const Addr& a, long long r
 }
 
 // img[(tile * kblocks + kb)][row][k] (swizzled) = bf16(src(r, k)); zero outside rows x K.
-// One thread per (padded row, 8 consecutive k): 16 bytes out.
+// One thread per (padded row, 8 consecutive k): 16 bytes out.  The row part of the
+// address and the split of k0 are computed once per thread; the 8 elements step
+// through k incrementally, with two 16-byte loads when they are contiguous.
 __global__ void pack_kernel(const float* __restrict__ src, Addr a, long long rows, long long K, int tile_rows,
                             long long rows_pad, int kblocks, uint4* __restrict__ img) {
   const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   const long long chunks = (long long)kblocks * (BK / 8);
   if (i >= rows_pad * chunks) return;
   const long long r = i / chunks;
-  const int ch = (int)(i % chunks);
+  const int ch = (int)(i - r * chunks);
   const long long k0 = (long long)ch * 8;
   __align__(16) __nv_bfloat16 v[8];
+  if (r < rows && k0 < K) {
+    const float* base = src + (r / a.rc) * a.s1 + (r % a.rc) * a.s2;
+    if (a.kc == 1 && a.t1 == 1 && k0 + 8 <= K && ((reinterpret_cast<uintptr_t>(base + k0) & 15u) == 0)) {
+      const float4 lo = __ldg(reinterpret_cast<const float4*>(base + k0));
+      const float4 hi = __ldg(reinterpret_cast<const float4*>(base + k0) + 1);
+      v[0] = __float2bfloat16_rn(lo.x); v[1] = __float2bfloat16_rn(lo.y);
+      v[2] = __float2bfloat16_rn(lo.z); v[3] = __float2bfloat16_rn(lo.w);
+      v[4] = __float2bfloat16_rn(hi.x); v[5] = __float2bfloat16_rn(hi.y);
+      v[6] = __float2bfloat16_rn(hi.z); v[7] = __float2bfloat16_rn(hi.w);
+    } else {
+      long long q = k0 / a.kc, rem = k0 - q * a.kc;
 #pragma unroll
-  for (int j = 0; j < 8; ++j) {
-    const long long k = k0 + j;
-    const float x = (r < rows && k < K) ? __ldg(src + addr_of(a, r, k)) : 0.f;
-    v[j] = __float2bfloat16_rn(x);
+      for (int j = 0; j < 8; ++j) {
+        const float x = (k0 + j < K) ? __ldg(base + q * a.t1 + rem * a.t2) : 0.f;
+        v[j] = __float2bfloat16_rn(x);
+        if (++rem == a.kc) { rem = 0; ++q; }
+      }
+    }
+  } else {
+#pragma unroll
+    for (int j = 0; j < 8; ++j) v[j] = __float2bfloat16_rn(0.f);
   }
   const long long tile = r / tile_rows;
-  const int row = (int)(r % tile_rows), kb = (int)(k0 / BK);
+  const int row = (int)(r - tile * tile_rows), kb = (int)(k0 / BK);
   const size_t byte = ((size_t)tile * kblocks + kb) * ((size_t)tile_rows * BK * 2) + sw128(row, (int)(k0 % BK));
   img[byte / 16] = *reinterpret_cast<const uint4*>(v);
 }
@@ -173,6 +191,7 @@ __global__ void __launch_bounds__(128) gemm_kernel(const uint8_t* __restrict__ A
     const bool row_ok = r < e.M;
     const long long rbase = row_ok ? (r / e.out.rc) * e.out.s1 + (r % e.out.rc) * e.out.s2 : 0;
     const bool split_cols = e.out.kc != 1;
+    const bool stage_cols = !split_cols && e.out.t1 == 1;
     for (int c0 = 0; c0 < BN; c0 += 32) {
       uint32_t v[32];
       const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0;
@@ -186,7 +205,29 @@ __global__ void __launch_bounds__(128) gemm_kernel(const uint8_t* __restrict__ A
           : "r"(taddr)
           : "memory");
       asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-      if (part) {
+      if (!part && stage_cols) {
+        // columns contiguous in the output: pass the warp's 32 x 32 block through shared
+        // memory (the pipeline stages are idle now) and store each row with the lanes
+        // along its columns
+        float* blk = reinterpret_cast<float*>(smem) + warp * (32 * 33);
+#pragma unroll
+        for (int i = 0; i < 32; ++i) blk[lane * 33 + i] = __uint_as_float(v[i]);
+        __syncwarp();
+        const int c = nt * BN + c0 + lane;
+        const float bias_c = (e.bias && c < e.N) ? __ldg(e.bias + c) : 0.f;
+        for (int rr = 0; rr < 32; ++rr) {
+          const long long rw = (long long)mt * BM + warp * 32 + rr;
+          if (rw < e.M && c < e.N) {
+            const long long o = (rw / e.out.rc) * e.out.s1 + (rw % e.out.rc) * e.out.s2 + c;
+            float z = blk[rr * 33 + lane] * e.scale + bias_c;
+            if (e.add) z += e.add[o];
+            if (e.accumulate) z += e.y[o];
+            e.y[o] = z;
+            if (e.act) e.act[o] = gelu_t(z);
+          }
+        }
+        __syncwarp();
+      } else if (part) {
         float* pp = part + ((size_t)split * tiles + tile) * (size_t)(BM * BN) + (size_t)(warp * 32 + lane) * BN + c0;
 #pragma unroll
         for (int i = 0; i < 32; ++i) pp[i] = __uint_as_float(v[i]);
