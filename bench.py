@@ -72,6 +72,8 @@ def parse():
     p.add_argument('--corr-iters', type=int, default=0, help='corrector training iterations (0 = 600 x steps)')
     p.add_argument('--corr-window', type=int, default=16, help='corrected coarse steps per training rollout window')
     p.add_argument('--corr-positions', type=int, default=64, help='held-out positions of the corrector evaluation')
+    p.add_argument('--corr-form', type=int, default=0, choices=[0, 1],
+                   help='correction factors: 0 = 1 + M, 1 = unit modulus exp(i Im M)')
     return p.parse_args()
 
 
@@ -572,7 +574,8 @@ def run_corrector(args):
     pairs = int(sum((tr.shape[0] - 1) * tr.shape[1] for tr in trajs))
     net = engine.Corrector(n, n, 6, C, L, 32, 64, max_samples=max(16, 2 * args.corr_window))
     net.params.copy_(torch.from_numpy(CR.init_params(net, seed=0)))
-    trainer = CR.RolloutTrainer(net, [c for _, c, _ in crystals], trajs, window=args.corr_window, waves=8, seed=0)
+    trainer = CR.RolloutTrainer(net, [c for _, c, _ in crystals], trajs, window=args.corr_window, waves=8, seed=0,
+                                form=args.corr_form)
     iters = args.corr_iters if args.corr_iters > 0 else max(1, args.steps) * 600
     t1 = time.perf_counter()
     losses = [trainer.step(lr=2e-3 * 0.5 * (1 + math.cos(math.pi * i / iters))) for i in range(iters)]
@@ -589,7 +592,7 @@ def run_corrector(args):
         out = {'network_s_per_crystal': net_s, 'coarse_slices': int(cr.coarse_steps)}
         for thick in (200.0, 500.0, 1000.0):
             steps = min(cr.coarse_steps, int(round(thick / (cr.ratio * cr.slice_t))))
-            trans = cr.effective_slices(maps[:steps].contiguous())
+            trans = cr.effective_slices(maps[:steps].contiguous(), args.corr_form)
             ref, t_fine = CR.timed(lambda: CR.fine_multislice(cr, pos, steps))
             coarse, t_coarse = CR.timed(lambda: CR.coarse_multislice(cr, pos, steps))
             corr, t_corr = CR.timed(lambda: CR.corrected_multislice(net, cr, pos, steps, trans=trans))
@@ -597,6 +600,8 @@ def run_corrector(args):
                 'thickness_A': steps * cr.ratio * cr.slice_t, 'positions': len(pos),
                 'err_coarse_vs_fine': float(CR.rel_l2(coarse, ref).mean()),
                 'err_corrected_vs_fine': float(CR.rel_l2(corr, ref).mean()),
+                'intensity_coarse_over_fine': float((coarse.double().sum() / ref.double().sum()).item()),
+                'intensity_corrected_over_fine': float((corr.double().sum() / ref.double().sum()).item()),
                 'fine_probes_per_s': len(pos) / t_fine, 'coarse_probes_per_s': len(pos) / t_coarse,
                 'corrected_probes_per_s': len(pos) / t_corr,
                 'speedup_corrected_vs_fine': t_fine / t_corr,
@@ -612,7 +617,7 @@ def run_corrector(args):
             'config': {'workload': 'learned coarse-slice corrector, 256^2, 200 keV, 4x slices', 'pairs': pairs,
                        'generate_s': gen_s, 'train_s': train_s, 'train_iters': iters,
                        'loss_first': float(np.mean(losses[:10])), 'loss_last': float(np.mean(losses[-50:])),
-                       'window': args.corr_window,
+                       'window': args.corr_window, 'map_form': ['1 + M', 'exp(i Im M)'][args.corr_form],
                        'channels': C, 'layers': L, 'modes': '32 x 64 (kx x ky)', 'results': res}}
     print(json.dumps(line), flush=True)
     net.close()

@@ -413,12 +413,15 @@ MSX_API int msx_selftest_wait(int arrive, int limit_log2, void* stream);
  *                          slices pot (S * ratio, ny, nx): sigma V of each fine
  *                          slice, their sum and the constant tval (in_channels =
  *                          ratio + 2)
- * Rollout helpers on complex64 waves (num, ny, nx) with one map set (ny, nx, 4):
- *  msx_corrector_apply_map:  waves *= (1 + M) (conj: its conjugate), M = A (which 0) or B (1)
+ * Rollout helpers on complex64 waves (num, ny, nx) with one map set (ny, nx, 4).  A map M = A
+ * (which 0) or B (which 1) acts as the factor 1 + M (form 0) or as the unit-modulus factor
+ * exp(i Im M) (form 1, Re M unused: the corrected step then preserves the norm like the exact one):
+ *  msx_corrector_apply_map:  waves *= factor (conj: its conjugate)
  *  msx_corrector_mul_plane:  waves *= plane (conj: its conjugate) for one complex (ny, nx) plane
- *  msx_corrector_map_trans:  out = trans (1 + M) for one (ny, nx) plane
- *  msx_corrector_map_grad:   dmaps[.., M] (+)= 2 sum_b conj(u_b) g_b (d loss / d Re M, d Im M
- *                            for a map that multiplied u, g the adjoint of the product)
+ *  msx_corrector_map_trans:  out = trans * factor for one (ny, nx) plane
+ *  msx_corrector_map_grad:   d loss / d (Re M, Im M) (+)= from G = sum_b conj(u_b) g_b, for a factor
+ *                            that multiplied u with g the adjoint of the product: (2 Re G, 2 Im G)
+ *                            for form 0, (0, 2 Re(conj(G) i factor)) for form 1 (maps_dev needed)
  *  msx_corrector_residual:   adjoint (+)= weight (psi - target); *loss_out = weight sum |psi - target|^2
  */
 MSX_API int msx_corrector_create(int ny, int nx, int in_channels, int channels, int layers, int modes_x, int modes_y,
@@ -434,13 +437,13 @@ MSX_API int msx_corrector_check(msx_corrector* corrector);
 MSX_API int msx_corrector_features(const float* pot_dev, int samples, int ratio, int ny, int nx, float sigma,
                                    float tval, float* features_out_dev, void* stream);
 MSX_API int msx_corrector_apply_map(float* waves_dev, int num, int ny, int nx, const float* maps_dev, int which,
-                                    int conj, void* stream);
+                                    int conj, int form, void* stream);
 MSX_API int msx_corrector_mul_plane(float* waves_dev, int num, int ny, int nx, const float* plane_dev, int conj,
                                     void* stream);
 MSX_API int msx_corrector_map_trans(const float* trans_dev, int ny, int nx, const float* maps_dev, int which,
-                                    float* out_dev, void* stream);
+                                    int form, float* out_dev, void* stream);
 MSX_API int msx_corrector_map_grad(const float* u_dev, const float* g_dev, int num, int ny, int nx, int which,
-                                   int accumulate, float* dmaps_dev, void* stream);
+                                   int accumulate, int form, const float* maps_dev, float* dmaps_dev, void* stream);
 MSX_API int msx_corrector_residual(const float* psi_dev, const float* target_dev, int num, int ny, int nx, float weight,
                                    int accumulate, float* adjoint_dev, float* loss_out_dev, void* stream);
 

@@ -86,10 +86,12 @@ SIGNATURES = [
     ('msx_corrector_check', _c.c_int, [_vp]),
     ('msx_corrector_features', _c.c_int, [_vp, _c.c_int, _c.c_int, _c.c_int, _c.c_int, _c.c_float, _c.c_float, _vp,
                                           _vp]),
-    ('msx_corrector_apply_map', _c.c_int, [_vp, _c.c_int, _c.c_int, _c.c_int, _vp, _c.c_int, _c.c_int, _vp]),
+    ('msx_corrector_apply_map', _c.c_int, [_vp, _c.c_int, _c.c_int, _c.c_int, _vp, _c.c_int, _c.c_int, _c.c_int,
+                                           _vp]),
     ('msx_corrector_mul_plane', _c.c_int, [_vp, _c.c_int, _c.c_int, _c.c_int, _vp, _c.c_int, _vp]),
-    ('msx_corrector_map_trans', _c.c_int, [_vp, _c.c_int, _c.c_int, _vp, _c.c_int, _vp, _vp]),
-    ('msx_corrector_map_grad', _c.c_int, [_vp, _vp, _c.c_int, _c.c_int, _c.c_int, _c.c_int, _c.c_int, _vp, _vp]),
+    ('msx_corrector_map_trans', _c.c_int, [_vp, _c.c_int, _c.c_int, _vp, _c.c_int, _c.c_int, _vp, _vp]),
+    ('msx_corrector_map_grad', _c.c_int, [_vp, _vp, _c.c_int, _c.c_int, _c.c_int, _c.c_int, _c.c_int, _c.c_int, _vp,
+                                          _vp, _vp]),
     ('msx_corrector_residual', _c.c_int, [_vp, _vp, _c.c_int, _c.c_int, _c.c_int, _c.c_float, _c.c_int, _vp, _vp,
                                           _vp]),
     ('msx_plan_autotune', _c.c_int, [_vp, _vp, _c.c_int, _vp, _vp, _vp, _c.c_int, _c.c_float, _c.c_double,

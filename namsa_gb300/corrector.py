@@ -115,15 +115,16 @@ class Crystal:
             out[k + 1] = w
         return out
 
-    def effective_slices(self, maps):
-        """Transmission slices of the corrected multislice (S + 1, n, n) from the maps (S, n, n, 4)."""
+    def effective_slices(self, maps, form=0):
+        """Transmission slices of the corrected multislice (S + 1, n, n) from the maps (S, n, n, 4)
+        (form 0: factors 1 + M; form 1: unit-modulus factors exp(i Im M))."""
         S = maps.shape[0]
         out = torch.empty((S + 1, self.n, self.n), dtype=torch.complex64, device=maps.device)
         for k in range(S):
-            engine.map_trans(self.trans_coarse[k], maps[k], 1, out=out[k])
+            engine.map_trans(self.trans_coarse[k], maps[k], 1, out=out[k], form=form)
             if k > 0:
-                engine.map_trans(out[k].clone(), maps[k - 1], 0, out=out[k])
-        engine.map_trans(self.ones, maps[S - 1], 0, out=out[S])
+                engine.map_trans(out[k].clone(), maps[k - 1], 0, out=out[k], form=form)
+        engine.map_trans(self.ones, maps[S - 1], 0, out=out[S], form=form)
         return out
 
 
@@ -150,13 +151,13 @@ def crystal_maps(net, crystal):
     return out
 
 
-def corrected_multislice(net, crystal, positions, steps=None, maps=None, trans=None):
+def corrected_multislice(net, crystal, positions, steps=None, maps=None, trans=None, form=0):
     """CBED of the corrected coarse-slice multislice through `steps` coarse slices,
     run by Plan.multislice on the effective transmission slices."""
     steps = crystal.coarse_steps if steps is None else steps
     if trans is None:
         maps = crystal_maps(net, crystal) if maps is None else maps
-        trans = crystal.effective_slices(maps[:steps].contiguous())
+        trans = crystal.effective_slices(maps[:steps].contiguous(), form)
     sim = crystal.sim
     pos = torch.as_tensor(np.asarray(positions, np.float32), device=crystal.trans_fine.device)
     return crystal.plan.multislice(trans, sim.psi_k_dev, sim.norm_dev, pos, crystal.kmax, sim.Lambda,
@@ -186,10 +187,10 @@ def fine_multislice(crystal, positions, steps=None):
 class RolloutTrainer:
     """Windowed rollout training of a corrector over a set of crystals."""
 
-    def __init__(self, net, crystals, trajectories, window=8, waves=8, seed=0):
+    def __init__(self, net, crystals, trajectories, window=8, waves=8, seed=0, form=0):
         self.net, self.crystals, self.traj = net, crystals, trajectories
         self.norms = [wave_norms(t) for t in trajectories]
-        self.K, self.B = window, waves
+        self.K, self.B, self.form = window, waves, form
         self.rng = np.random.default_rng(seed)
         n = crystals[0].n
         dev = crystals[0].trans_fine.device
@@ -222,7 +223,7 @@ class RolloutTrainer:
         """Rollout of K corrected steps from the fine wave at coarse depth k0 (waves b);
         writes d loss / d maps into dmaps and returns the loss, the mean over steps of
         |psi_k - f_k|^2 / |f_k|^2."""
-        K, n = self.K, self.n
+        K, n, form = self.K, self.n, self.form
         psi = tr[k0][b].contiguous()
         nb = psi.shape[0]
         tb = torch.empty((K, n, n), dtype=torch.complex64, device=psi.device)
@@ -232,12 +233,12 @@ class RolloutTrainer:
         loss = 0.0
         for k in range(K):
             s = k0 + k
-            engine.map_trans(cr.trans_coarse[s], maps[k], 1, out=tb[k])
+            engine.map_trans(cr.trans_coarse[s], maps[k], 1, out=tb[k], form=form)
             w_in[k].copy_(psi)
             engine.mul_plane(w_in[k], cr.trans_coarse[s])
             cr.plan.step_waves(psi, tb[k], cr.ptab_coarse)
             u[k].copy_(psi)
-            engine.apply_map(psi, maps[k], 0)
+            engine.apply_map(psi, maps[k], 0, form=form)
             target = tr[s + 1][b].contiguous()
             if norms is None:
                 engine.residual(torch.zeros_like(target), target, 1.0, adj[k + 1], self.loss_buf)
@@ -248,10 +249,10 @@ class RolloutTrainer:
             loss += float(self.loss_buf.item())
         g = adj[K].clone()
         for k in range(K - 1, -1, -1):
-            engine.map_grad(u[k], g, 0, dmaps[k])
-            engine.apply_map(g, maps[k], 0, conj=True)
+            engine.map_grad(u[k], g, 0, dmaps[k], form=form, maps=maps[k])
+            engine.apply_map(g, maps[k], 0, conj=True, form=form)
             cr.plan.step_waves(g, cr.ones, cr.ptab_coarse_adj)
-            engine.map_grad(w_in[k], g, 1, dmaps[k], accumulate=True)
+            engine.map_grad(w_in[k], g, 1, dmaps[k], accumulate=True, form=form, maps=maps[k])
             engine.mul_plane(g, tb[k], conj=True)
             if k > 0:
                 g += adj[k]

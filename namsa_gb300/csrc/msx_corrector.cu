@@ -159,17 +159,24 @@ __global__ void features_kernel(const float* __restrict__ pot, int S, int ratio,
 }
 
 // Correction maps: maps (S, P, 4) = (Re A, Im A, Re B, Im B); `which` 0 = A, 1 = B.
-__device__ __forceinline__ float2 one_plus(const float* maps, long long sp, int which) {
+// form 0: the factor is 1 + M; form 1: the unit-modulus factor exp(i Im M) (Re M unused),
+// which keeps the corrected step as norm-preserving as the exact one.
+__device__ __forceinline__ float2 one_plus(const float* maps, long long sp, int which, int form) {
   const float* m = maps + sp * 4 + 2 * which;
+  if (form) {
+    float sn, cs;
+    sincosf(m[1], &sn, &cs);
+    return make_float2(cs, sn);
+  }
   return make_float2(1.f + m[0], m[1]);
 }
 
 // w[b][p] *= (1 + M_s[p]) (or its conjugate) for nb waves that all use sample s
 __global__ void map_mul_kernel(float2* __restrict__ w, int nb, long long P, const float* __restrict__ maps, int which,
-                               int conj) {
+                               int conj, int form) {
   const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= (long long)nb * P) return;
-  float2 f = one_plus(maps, i % P, which);
+  float2 f = one_plus(maps, i % P, which, form);
   if (conj) f.y = -f.y;
   w[i] = cmul(w[i], f);
 }
@@ -186,15 +193,19 @@ __global__ void plane_mul_kernel(float2* __restrict__ w, long long n, long long 
 
 // out[p] = t[p] (1 + M[p]) for one plane
 __global__ void map_trans_kernel(const float2* __restrict__ t, long long P, const float* __restrict__ maps, int which,
-                                 float2* __restrict__ out) {
+                                 int form, float2* __restrict__ out) {
   const long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (p >= P) return;
-  out[p] = cmul(t[p], one_plus(maps, p, which));
+  out[p] = cmul(t[p], one_plus(maps, p, which, form));
 }
 
-// dmaps[p][2 which], [2 which + 1] (+)= 2 sum_b conj(u[b][p]) g[b][p]  (b in order)
+// G = sum_b conj(u[b][p]) g[b][p] (b in order) is d loss / d conj(factor) for a factor
+// that multiplied u.  form 0: dmaps[p][2 which], [2 which + 1] (+)= 2 Re G, 2 Im G;
+// form 1 (factor exp(i theta), theta = Im M): d/d theta = 2 Re(conj(G) i factor)
+// = 2 (Im G cos theta - Re G sin theta), and 0 for Re M.
 __global__ void map_grad_kernel(const float2* __restrict__ u, const float2* __restrict__ g, int nb, long long P,
-                                int which, int accumulate, float* __restrict__ dmaps) {
+                                int which, int accumulate, int form, const float* __restrict__ maps,
+                                float* __restrict__ dmaps) {
   const long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (p >= P) return;
   float re = 0.f, im = 0.f;
@@ -202,6 +213,12 @@ __global__ void map_grad_kernel(const float2* __restrict__ u, const float2* __re
     const float2 a = u[(size_t)b * P + p], c = g[(size_t)b * P + p];
     re = fmaf(a.x, c.x, fmaf(a.y, c.y, re));
     im = fmaf(a.x, c.y, fmaf(-a.y, c.x, im));
+  }
+  if (form) {
+    const float2 f = one_plus(maps, p, which, 1);
+    const float dth = im * f.x - re * f.y;
+    re = 0.f;
+    im = dth;
   }
   float* d = dmaps + p * 4 + 2 * which;
   if (accumulate) {
@@ -635,13 +652,13 @@ int msx_corrector_features(const float* pot_dev, int samples, int ratio, int ny,
 }
 
 int msx_corrector_apply_map(float* waves_dev, int num, int ny, int nx, const float* maps_dev, int which, int conj,
-                            void* stream) {
+                            int form, void* stream) {
   if (!waves_dev || !maps_dev || num < 0 || ny < 1 || nx < 1 || (which != 0 && which != 1))
     return cfail(MSX_ERR_INVALID, "corrector apply map: bad arguments");
   const long long P = (long long)ny * nx;
   if (num == 0) return MSX_OK;
   map_mul_kernel<<<blocks_for((long long)num * P, 256), 256, 0, (cudaStream_t)stream>>>(
-      reinterpret_cast<float2*>(waves_dev), num, P, maps_dev, which, conj ? 1 : 0);
+      reinterpret_cast<float2*>(waves_dev), num, P, maps_dev, which, conj ? 1 : 0, form ? 1 : 0);
   NN_CUDA(cudaGetLastError());
   return MSX_OK;
 }
@@ -659,26 +676,28 @@ int msx_corrector_mul_plane(float* waves_dev, int num, int ny, int nx, const flo
   return MSX_OK;
 }
 
-int msx_corrector_map_trans(const float* trans_dev, int ny, int nx, const float* maps_dev, int which, float* out_dev,
-                            void* stream) {
+int msx_corrector_map_trans(const float* trans_dev, int ny, int nx, const float* maps_dev, int which, int form,
+                            float* out_dev, void* stream) {
   if (!trans_dev || !maps_dev || !out_dev || ny < 1 || nx < 1 || (which != 0 && which != 1))
     return cfail(MSX_ERR_INVALID, "corrector map transmission: bad arguments");
   const long long P = (long long)ny * nx;
   map_trans_kernel<<<blocks_for(P, 256), 256, 0, (cudaStream_t)stream>>>(reinterpret_cast<const float2*>(trans_dev), P,
-                                                                         maps_dev, which,
+                                                                         maps_dev, which, form ? 1 : 0,
                                                                          reinterpret_cast<float2*>(out_dev));
   NN_CUDA(cudaGetLastError());
   return MSX_OK;
 }
 
 int msx_corrector_map_grad(const float* u_dev, const float* g_dev, int num, int ny, int nx, int which, int accumulate,
-                           float* dmaps_dev, void* stream) {
-  if (!u_dev || !g_dev || !dmaps_dev || num < 1 || ny < 1 || nx < 1 || (which != 0 && which != 1))
+                           int form, const float* maps_dev, float* dmaps_dev, void* stream) {
+  if (!u_dev || !g_dev || !dmaps_dev || num < 1 || ny < 1 || nx < 1 || (which != 0 && which != 1) ||
+      (form && !maps_dev))
     return cfail(MSX_ERR_INVALID, "corrector map gradient: bad arguments");
   const long long P = (long long)ny * nx;
   map_grad_kernel<<<blocks_for(P, 256), 256, 0, (cudaStream_t)stream>>>(reinterpret_cast<const float2*>(u_dev),
                                                                         reinterpret_cast<const float2*>(g_dev), num, P,
-                                                                        which, accumulate ? 1 : 0, dmaps_dev);
+                                                                        which, accumulate ? 1 : 0, form ? 1 : 0,
+                                                                        maps_dev, dmaps_dev);
   NN_CUDA(cudaGetLastError());
   return MSX_OK;
 }

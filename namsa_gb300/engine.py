@@ -551,12 +551,13 @@ def corrector_features(pot, ratio, sigma, tval, out=None):
     return out
 
 
-def apply_map(waves, maps, which, conj=False):
-    """waves (num, ny, nx) complex64 *= (1 + M) (or its conjugate); maps (ny, nx, 4), M = A (0) or B (1)."""
+def apply_map(waves, maps, which, conj=False, form=0):
+    """waves (num, ny, nx) complex64 *= factor (or its conjugate); maps (ny, nx, 4), M = A (0) or B (1);
+    factor 1 + M (form 0) or exp(i Im M) (form 1)."""
     _need(waves, torch.complex64, 'waves', 3)
     _need(maps, torch.float32, 'maps', 3)
     _lib.check(lib().msx_corrector_apply_map(_ptr(waves), waves.shape[0], waves.shape[1], waves.shape[2], _ptr(maps),
-                                             int(which), int(bool(conj)), _stream()))
+                                             int(which), int(bool(conj)), int(form), _stream()))
     return waves
 
 
@@ -569,24 +570,25 @@ def mul_plane(waves, plane, conj=False):
     return waves
 
 
-def map_trans(trans, maps, which, out=None):
-    """trans (ny, nx) complex64 times (1 + M)."""
+def map_trans(trans, maps, which, out=None, form=0):
+    """trans (ny, nx) complex64 times the factor of map M (1 + M, or exp(i Im M) for form 1)."""
     _need(trans, torch.complex64, 'trans', 2)
     _need(maps, torch.float32, 'maps', 3)
     if out is None:
         out = torch.empty_like(trans)
     _lib.check(lib().msx_corrector_map_trans(_ptr(trans), trans.shape[0], trans.shape[1], _ptr(maps), int(which),
-                                             _ptr(out), _stream()))
+                                             int(form), _ptr(out), _stream()))
     return out
 
 
-def map_grad(u, g, which, dmaps, accumulate=False):
-    """dmaps (ny, nx, 4)[.., M] (+)= 2 sum_b conj(u_b) g_b."""
+def map_grad(u, g, which, dmaps, accumulate=False, form=0, maps=None):
+    """Gradient of the loss with respect to map M (into dmaps (ny, nx, 4)) for a factor that
+    multiplied u, g the adjoint of the product; form 1 needs the maps."""
     _need(u, torch.complex64, 'u', 3)
     _need(g, torch.complex64, 'g', 3)
     _need(dmaps, torch.float32, 'dmaps', 3)
     _lib.check(lib().msx_corrector_map_grad(_ptr(u), _ptr(g), u.shape[0], u.shape[1], u.shape[2], int(which),
-                                            int(bool(accumulate)), _ptr(dmaps), _stream()))
+                                            int(bool(accumulate)), int(form), _ptr(maps), _ptr(dmaps), _stream()))
     return dmaps
 
 

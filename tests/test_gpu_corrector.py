@@ -6,7 +6,8 @@
   the same bfloat16 operand rounding, and against the plain FP64 oracle.
 * Rollout adjoint: the map gradients of a windowed corrected rollout,
   back-propagated through the engine's slice step with the conjugate
-  propagator, against a central difference of the loss along a random direction.
+  propagator, against a central difference of the loss along a random
+  direction, for factors 1 + M and for unit-modulus factors exp(i Im M).
 * Training: a corrector trained by rollouts on Si [001] at 256^2 (200 keV,
   fine slices a/4, coarse slices a) lowers the CBED error of 4x-thick slicing
   against plain fine slicing over 200 Angstrom on held-out probe positions, run
@@ -65,13 +66,14 @@ def test_network_forward_backward_match_oracle(H, W, Cin, C, L, MX, MY, S):
     net.close()
 
 
-def test_rollout_adjoint_matches_central_difference():
+@pytest.mark.parametrize('form', [0, 1])
+def test_rollout_adjoint_matches_central_difference(form):
     torch.cuda.set_device(0)
     cr = CR.Crystal(structures.silicon((1, 1, 6)), 64, 5.431 / 4)
     rng = np.random.default_rng(0)
     tr = cr.trajectory(rng.uniform(0, 5.431, size=(3, 2)), steps=4)
     net = engine.Corrector(64, 64, 6, 8, 1, 8, 16, max_samples=4)
-    trainer = CR.RolloutTrainer(net, [cr], [tr], window=3, waves=3)
+    trainer = CR.RolloutTrainer(net, [cr], [tr], window=3, waves=3, form=form)
     maps = (0.05 * torch.randn(3, 64, 64, 4, generator=torch.Generator().manual_seed(1))).to(DEV)
     dmaps = torch.zeros_like(maps)
     b = torch.arange(3, device=DEV)
