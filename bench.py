@@ -72,7 +72,7 @@ def parse():
     p.add_argument('--corr-iters', type=int, default=0, help='corrector training iterations (0 = 600 x steps)')
     p.add_argument('--corr-window', type=int, default=16, help='corrected coarse steps per training rollout window')
     p.add_argument('--corr-positions', type=int, default=64, help='held-out positions of the corrector evaluation')
-    p.add_argument('--corr-form', type=int, default=0, choices=[0, 1],
+    p.add_argument('--corr-form', type=int, default=1, choices=[0, 1],
                    help='correction factors: 0 = 1 + M, 1 = unit modulus exp(i Im M)')
     return p.parse_args()
 

@@ -5,14 +5,17 @@ fine one: the transmission of the fine slices it contains and the Fresnel
 propagator of their summed thickness.  It costs a quarter of the fine steps
 but its splitting error grows with the thickness.  The corrected coarse step is
 
-    psi <- (1 + A_k) ifft2(P_c fft2((1 + B_k) t_k psi))
+    psi <- a_k ifft2(P_c fft2(b_k t_k psi)),   a_k = exp(i Im A_k),  b_k = exp(i Im B_k)
 
-with per-pixel complex maps A_k, B_k that the corrector network
+with per-pixel maps A_k, B_k that the corrector network
 (``engine.Corrector``, csrc/msx_corrector.cu) computes from the potentials of
 the fine slices inside coarse slice k.  The maps depend on the crystal only, so
 they fold into the transmission slices of a plain multislice run:
 
-    t'_0 = (1 + B_0) t_0,  t'_k = (1 + A_{k-1})(1 + B_k) t_k,  t'_S = 1 + A_{S-1}
+    t'_0 = b_0 t_0,  t'_k = a_{k-1} b_k t_k,  t'_S = a_{S-1}
+
+(unit-modulus factors keep each corrected step norm-preserving like the exact
+fine steps; the general factors 1 + M are kept as ``form=0``)
 
 (the extra last slice only multiplies; its propagator phase does not change
 the CBED).  The corrected multislice of every probe position therefore runs
@@ -39,6 +42,10 @@ from .msa import MSAGPU
 PROBE = {'smooth_apert': True, 'apert_smooth': 50, 'spherical_phase': True,
          'aberration_dict': {'C1': 0., 'C3': 0., 'C5': 0.}, 'scherzer': False}
 RATIO = 4
+# Correction factors: 0 = 1 + M, 1 = exp(i Im M).  The unit-modulus form keeps every corrected
+# step norm-preserving, as the exact fine steps are; with 1 + M the total intensity drifted by
+# 2 % over 1000 A of Si and long rollouts lost their gain.
+FORM = 1
 
 
 def init_params(net, seed=0, out_scale=1e-2, spec_scale=0.5):
@@ -115,7 +122,7 @@ class Crystal:
             out[k + 1] = w
         return out
 
-    def effective_slices(self, maps, form=0):
+    def effective_slices(self, maps, form=FORM):
         """Transmission slices of the corrected multislice (S + 1, n, n) from the maps (S, n, n, 4)
         (form 0: factors 1 + M; form 1: unit-modulus factors exp(i Im M))."""
         S = maps.shape[0]
@@ -151,7 +158,7 @@ def crystal_maps(net, crystal):
     return out
 
 
-def corrected_multislice(net, crystal, positions, steps=None, maps=None, trans=None, form=0):
+def corrected_multislice(net, crystal, positions, steps=None, maps=None, trans=None, form=FORM):
     """CBED of the corrected coarse-slice multislice through `steps` coarse slices,
     run by Plan.multislice on the effective transmission slices."""
     steps = crystal.coarse_steps if steps is None else steps
@@ -187,7 +194,7 @@ def fine_multislice(crystal, positions, steps=None):
 class RolloutTrainer:
     """Windowed rollout training of a corrector over a set of crystals."""
 
-    def __init__(self, net, crystals, trajectories, window=8, waves=8, seed=0, form=0):
+    def __init__(self, net, crystals, trajectories, window=8, waves=8, seed=0, form=FORM):
         self.net, self.crystals, self.traj = net, crystals, trajectories
         self.norms = [wave_norms(t) for t in trajectories]
         self.K, self.B, self.form = window, waves, form
