@@ -301,6 +301,17 @@ MSX_API int msx_multislice_noalloc(const float* trans_dev, int num_slices, const
  */
 MSX_API int msx_process_cbed(const float* cbed_dev, int num_patterns, int height, int width, void* out_fp16_dev,
                              void* stream);
+
+/*
+ * Detector signals of a stored CBED stack: out[p][d] = sum_k cbed[p][k] w_d[k]
+ * (float64, a fixed summation order), weights (num_detectors, height, width)
+ * float32; with weights NULL and num_detectors 1, the plain sum of each
+ * pattern.  Replaces MSA.integrate_cbed (namsa/msa.py:426-439) for stacks
+ * already computed and the per-pattern sums of MSA.check_simulation
+ * (namsa/msa.py:363-371).
+ */
+MSX_API int msx_integrate_cbed(const float* cbed_dev, int num_patterns, int height, int width, const float* weights_dev,
+                               int num_detectors, double* out_dev, void* stream);
 MSX_API int msx_process_potential(const float* trans_dev, int num_slices, int ny, int nx, float* work_dev,
                                   void* out_fp16_dev, void* stream);
 

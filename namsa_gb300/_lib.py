@@ -58,6 +58,7 @@ SIGNATURES = [
     ('msx_multislice_noalloc', _c.c_int, [_vp, _c.c_int, _vp, _vp, _vp, _c.c_int, _c.c_int, _c.c_int, _c.c_float,
                                           _c.c_double, _c.c_double, _c.c_float, _vp, _c.c_int, _c.c_int, _vp]),
     ('msx_process_cbed', _c.c_int, [_vp, _c.c_int, _c.c_int, _c.c_int, _vp, _vp]),
+    ('msx_integrate_cbed', _c.c_int, [_vp, _c.c_int, _c.c_int, _c.c_int, _vp, _c.c_int, _vp, _vp]),
     ('msx_process_potential', _c.c_int, [_vp, _c.c_int, _c.c_int, _c.c_int, _vp, _vp, _vp]),
     ('msx_integrate_potential', _c.c_int, [_vp, _vp, _c.c_int, _c.c_int, _c.c_int, _c.c_int, _c.c_int, _c.c_int,
                                            _c.c_float, _vp, _vp]),

@@ -117,11 +117,47 @@ __global__ void integrate_potential_kernel(const float* __restrict__ pot, const 
   trans[((size_t)s * ny + y) * nx + x] = make_float2(cosf(arg), sinf(arg));
 }
 
+// One CTA per (pattern p, detector d): out[p][d] = sum_k cbed[p][k] w_d[k] in double,
+// strided partial sums then the block sum (a fixed order); w == null sums the pattern.
+__global__ void integrate_cbed_kernel(const float* __restrict__ cbed, long long n, const float* __restrict__ w,
+                                      int ndet, double* __restrict__ out) {
+  __shared__ double sh[32];
+  const long long p = blockIdx.x / ndet;
+  const int d = (int)(blockIdx.x % ndet);
+  const float* c = cbed + p * n;
+  const float* wd = w ? w + (long long)d * n : nullptr;
+  double acc = 0;
+  for (long long k = threadIdx.x; k < n; k += blockDim.x) acc += wd ? (double)c[k] * (double)wd[k] : (double)c[k];
+  const double s = block_sum(acc, sh);
+  if (threadIdx.x == 0) out[blockIdx.x] = s;
+}
+
 }  // namespace msx
 
 using namespace msx;
 
 extern "C" {
+
+int msx_integrate_cbed(const float* cbed_dev, int num_patterns, int height, int width, const float* weights_dev,
+                       int num_detectors, double* out_dev, void* stream) {
+  if (num_patterns < 0 || height <= 0 || width <= 0 || num_detectors < 1 || num_detectors > 65535) {
+    set_last_error("integrate_cbed: bad sizes");
+    return MSX_ERR_INVALID;
+  }
+  if (num_patterns == 0) return MSX_OK;
+  if (!cbed_dev || !out_dev || (!weights_dev && num_detectors != 1)) {
+    set_last_error("integrate_cbed: null pointer (weights may be null only for one plain sum)");
+    return MSX_ERR_INVALID;
+  }
+  integrate_cbed_kernel<<<(unsigned)((long long)num_patterns * num_detectors), 256, 0, (cudaStream_t)stream>>>(
+      cbed_dev, (long long)height * width, weights_dev, num_detectors, out_dev);
+  const cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) {
+    set_last_error(cudaGetErrorString(e));
+    return MSX_ERR_CUDA;
+  }
+  return MSX_OK;
+}
 
 int msx_process_cbed(const float* cbed_dev, int num_patterns, int height, int width, void* out_fp16_dev, void* stream) {
   if (num_patterns < 0 || height <= 0 || width <= 0) {

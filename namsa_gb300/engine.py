@@ -137,6 +137,22 @@ def process_cbed(cbed):
     return out
 
 
+def integrate_cbed(cbed, weights=None):
+    """Detector signals (P, ndet) float64 of a CBED stack (P, ny, nx) float32 with
+    weights (ndet, ny, nx) float32; without weights the sum of each pattern (P, 1)."""
+    _need(cbed, torch.float32, 'cbed', 3)
+    P, ny, nx = cbed.shape
+    nd = 1
+    if weights is not None:
+        _need(weights, torch.float32, 'weights', 3)
+        if tuple(weights.shape[1:]) != (ny, nx):
+            raise ValueError('weights must be (ndet, ny, nx) like the patterns')
+        nd = weights.shape[0]
+    out = torch.empty((P, nd), dtype=torch.float64, device=cbed.device)
+    _lib.check(lib().msx_integrate_cbed(_ptr(cbed), P, ny, nx, _ptr(weights), nd, _ptr(out), _stream()))
+    return out
+
+
 def process_potential(trans):
     """Projected-potential label (1, w, w) float16 of a transmission stack (S, ny, nx)."""
     _need(trans, torch.complex64, 'trans', 3)

@@ -401,7 +401,7 @@ class MSAGPU:
     def check_simulation(self):
         """Integrated intensity per pattern (msa.py:363-371).  Patterns that are not
         finite (NaN or Inf inputs) raise a RuntimeWarning naming how many."""
-        prob = self.cbed.double().sum((1, 2)).cpu().numpy()
+        prob = engine.integrate_cbed(self.cbed)[:, 0].cpu().numpy()
         bad = ~np.isfinite(prob)
         if bad.any():
             warn(f'{int(bad.sum())} of {prob.size} CBED patterns are not finite (NaN or Inf in the inputs)',
@@ -418,8 +418,8 @@ class MSAGPU:
                 raise ValueError('Detector angles exceed maximum scattering angle simulated and/or are inconsistent')
             detector_array = annular_detector(self.sampling, self.kpix_size, self.Lambda,
                                               detector_params['inner_angle'], detector_params['outer_angle'])
-        det = torch.as_tensor(np.asarray(detector_array, np.float32), device=self.cbed.device)
-        img = (self.cbed * det).sum((1, 2))
+        det = torch.as_tensor(np.asarray(detector_array, np.float32)[None], device=self.cbed.device).contiguous()
+        img = engine.integrate_cbed(self.cbed, det)[:, 0]
         return img.reshape(tuple(int(g) for g in self.grid_steps)).cpu().numpy(), detector_array
 
     def close(self):

@@ -454,3 +454,26 @@ def test_probe_stack_without_transmission(ny, nx):
     sim.multislice(crop=128)
     assert sim.probes.dtype == np.float32 and sim.probes.shape == (12, 128, 128)
     sim.close()
+
+
+def test_integrate_cbed_of_a_stored_stack_matches_oracle():
+    """MSAGPU.integrate_cbed and check_simulation reduce the stored CBED stack in libmsx
+    (msx_integrate_cbed); the signals equal the oracle's integrate_cbed (namsa/msa.py:426-439)
+    of the same stack, and the per-pattern sums its float64 sums."""
+    sc = O.si_supercell(4, 4, 3)
+    pd = {'smooth_apert': True, 'apert_smooth': 50, 'spherical_phase': True,
+          'aberration_dict': {'C1': 0., 'C3': 1e4, 'C5': 0.}, 'scherzer': False}
+    sim = M.MSAGPU(200, 30e-3, sc, sampling=np.array([128, 128]), debye_waller=False)
+    sim.setup_device(0)
+    sim.calc_atomic_potentials()
+    sim.build_potential_slices(5.431 / 4)
+    sim.build_probe(pd)
+    sim.generate_probe_positions(grid_steps=np.array([3, 2]))
+    sim.multislice()
+    stack = sim.probes.astype(np.float64)
+    img, det = sim.integrate_cbed(detector_params={'inner_angle': 20e-3, 'outer_angle': 60e-3})
+    ref = O.integrate_cbed(stack, sim.grid_steps, det)
+    np.testing.assert_allclose(img, ref, rtol=1e-10)
+    np.testing.assert_array_equal(det, O.annular_detector(sim.sampling, sim.kpix_size, sim.Lambda, 20e-3, 60e-3))
+    np.testing.assert_allclose(sim.check_simulation(), stack.sum((1, 2)), rtol=1e-10)
+    sim.close()
