@@ -107,53 +107,12 @@ __global__ void pack_kernel(const float* __restrict__ src, Addr a, long long row
   img[byte / 16] = *reinterpret_cast<const uint4*>(v);
 }
 
-// A rows (r, k) of K block kb for tile row `row` (thread = row), rounded to bfloat16 and
-// written into the K-major 128-byte-swizzled image of the stage; zero outside rows x K.
-__device__ __forceinline__ void write_a_row(uint8_t* st, const float* __restrict__ asrc, const Addr& aa, long long r,
-                                            bool row_ok, const float* rowp, long long K, int kb, int row) {
-  const long long kbase = (long long)kb * BK;
-  const bool contiguous = aa.kc == 1 && aa.t1 == 1;
-  long long q = 0, rem = 0;
-  if (row_ok && !contiguous) {
-    q = kbase / aa.kc;
-    rem = kbase - q * aa.kc;
-  }
-#pragma unroll 2
-  for (int c = 0; c < BK / 8; ++c) {
-    const long long k0 = kbase + c * 8;
-    __align__(16) __nv_bfloat16 v[8];
-    if (row_ok && contiguous && k0 + 8 <= K && ((reinterpret_cast<uintptr_t>(rowp + k0) & 15u) == 0)) {
-      const float4 lo = __ldg(reinterpret_cast<const float4*>(rowp + k0));
-      const float4 hi = __ldg(reinterpret_cast<const float4*>(rowp + k0) + 1);
-      v[0] = __float2bfloat16_rn(lo.x); v[1] = __float2bfloat16_rn(lo.y);
-      v[2] = __float2bfloat16_rn(lo.z); v[3] = __float2bfloat16_rn(lo.w);
-      v[4] = __float2bfloat16_rn(hi.x); v[5] = __float2bfloat16_rn(hi.y);
-      v[6] = __float2bfloat16_rn(hi.z); v[7] = __float2bfloat16_rn(hi.w);
-    } else {
-#pragma unroll
-      for (int j = 0; j < 8; ++j) {
-        const long long k = k0 + j;
-        float x = 0.f;
-        if (row_ok && k < K) x = __ldg(contiguous ? rowp + k : rowp + q * aa.t1 + rem * aa.t2);
-        v[j] = __float2bfloat16_rn(x);
-        if (!contiguous && ++rem == aa.kc) { rem = 0; ++q; }
-      }
-    }
-    *reinterpret_cast<uint4*>(st + sw128(row, c * 8)) = *reinterpret_cast<const uint4*>(v);
-  }
-}
-
-// One CTA per 128 x BN tile of D (and K range when split).  A is read from its FP32
-// source by the CTA's 128 threads (thread = tile row), rounded and written into the
-// stage, and released to the tensor core by a proxy fence and an arrival on the
-// stage's `full` barrier (128 arrivals plus the B copy's transaction bytes); B arrives
-// by one bulk copy per K block from its packed image.  With part != null the CTA
-// (tile, split) sums K blocks [split * kper, ...) and writes its raw 128 x BN partial
-// to part[(split * tiles + tile) * 128 * BN].
+// With part != null the CTA (tile, split) sums K blocks [split * kper, ...) and
+// writes its raw 128 x BN partial to part[(split * tiles + tile) * 128 * BN].
 template <int BN>
-__global__ void __launch_bounds__(128) gemm_kernel(const float* __restrict__ asrc, Addr aa, long long M, long long K,
-                                                   const uint8_t* __restrict__ B, int kblocks, int ntiles_n, int kper,
-                                                   float* __restrict__ part, Epi e, int* __restrict__ err) {
+__global__ void __launch_bounds__(128) gemm_kernel(const uint8_t* __restrict__ A, const uint8_t* __restrict__ B,
+                                                   int kblocks, int ntiles_n, int kper, float* __restrict__ part,
+                                                   Epi e, int* __restrict__ err) {
   using C = Cfg<BN>;
   extern __shared__ __align__(1024) uint8_t smem_raw[];
   uint8_t* smem = smem_raw + ((1024u - (smem_u32(smem_raw) & 1023u)) & 1023u);
@@ -172,7 +131,7 @@ __global__ void __launch_bounds__(128) gemm_kernel(const float* __restrict__ asr
   }
   if (threadIdx.x == 32) {
     for (int s = 0; s < STAGES; ++s) {
-      mbar_init(&full[s], 129);  // 128 A writers + the B copy's arrival with its transaction bytes
+      mbar_init(&full[s], 1);
       mbar_init(&empty[s], 1);
     }
     mbar_init(&done, 1);
@@ -183,35 +142,29 @@ __global__ void __launch_bounds__(128) gemm_kernel(const float* __restrict__ asr
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   const uint32_t tmem = tmem_base;
 
-  const int row = threadIdx.x;
-  const long long r = (long long)mt * BM + row;
-  const bool row_ok = r < M;
-  const float* rowp = row_ok ? asrc + (r / aa.rc) * aa.s1 + (r % aa.rc) * aa.s2 : asrc;
-  const uint8_t* b_tile = B + (size_t)nt * kblocks * C::B_BYTES;
-  bool alive = true;
-  for (int i = 0; i < kb1 - kb0; ++i) {
-    const int kb = kb0 + i, s = i % STAGES;
-    uint8_t* st = smem + s * C::STAGE_BYTES;
-    if (i >= STAGES && !mbar_wait_bounded(&empty[s], ((i / STAGES) - 1) & 1)) {  // stage read by the MMAs
-      atomicOr(err, 2);
-      alive = false;
-      break;
-    }
-    if (threadIdx.x == 0) {
-      mbar_expect_tx(&full[s], C::B_BYTES);
+  if (threadIdx.x == 0) {  // producer
+    const uint8_t* a_tile = A + (size_t)mt * kblocks * A_BYTES;
+    const uint8_t* b_tile = B + (size_t)nt * kblocks * C::B_BYTES;
+    for (int i = 0; i < kb1 - kb0; ++i) {
+      const int kb = kb0 + i, s = i % STAGES;
+      if (i >= STAGES && !mbar_wait_bounded(&empty[s], ((i / STAGES) - 1) & 1)) {
+        atomicOr(err, 2);
+        break;
+      }
+      uint8_t* st = smem + s * C::STAGE_BYTES;
+      mbar_expect_tx(&full[s], C::STAGE_BYTES);
+      bulk_g2s(st, a_tile + (size_t)kb * A_BYTES, A_BYTES, &full[s]);
       bulk_g2s(st + A_BYTES, b_tile + (size_t)kb * C::B_BYTES, C::B_BYTES, &full[s]);
     }
-    write_a_row(st, asrc, aa, r, row_ok, rowp, K, kb, row);
-    fence_proxy_async();  // the generic-proxy writes precede the tensor core's reads
-    mbar_arrive(&full[s]);
-    if (threadIdx.x == 32) {  // MMA issuer
+  } else if (threadIdx.x == 32) {  // MMA issuer
+    for (int i = 0; i < kb1 - kb0; ++i) {
+      const int s = i % STAGES;
       if (!mbar_wait_bounded(&full[s], (i / STAGES) & 1)) {
         atomicOr(err, 4);
-        alive = false;
         break;
       }
       asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-      const uint32_t sa = smem_u32(st);
+      const uint32_t st = smem_u32(smem + s * C::STAGE_BYTES);
 #pragma unroll
       for (int j = 0; j < BK / 16; ++j) {
         const uint32_t off = (uint32_t)j * 32u;
@@ -219,18 +172,16 @@ __global__ void __launch_bounds__(128) gemm_kernel(const float* __restrict__ asr
         asm volatile(
             "{\n\t .reg .pred p;\n\t setp.ne.b32 p, %4, 0;\n\t"
             "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(tmem),
-            "l"(sdesc(sa + off)), "l"(sdesc(sa + A_BYTES + off)), "r"(C::IDESC), "r"(acc)
+            "l"(sdesc(st + off)), "l"(sdesc(st + A_BYTES + off)), "r"(C::IDESC), "r"(acc)
             : "memory");
       }
       asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
                        smem_u32(&empty[s]))
                    : "memory");
     }
-  }
-  (void)alive;
-  if (threadIdx.x == 32)
     asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(&done))
                  : "memory");
+  }
   __syncwarp();
   const bool ok = mbar_wait_bounded(&done, 0);
   if (!ok && lane == 0) atomicOr(err, 8);
@@ -325,8 +276,8 @@ __global__ void splitk_reduce_kernel(const float* __restrict__ part, int splits,
 }
 
 template <int BN>
-cudaError_t launch_gemm_bn(const float* a, const Addr& aa, long long M, long long K, const uint8_t* b, long long mtiles,
-                           int ntiles, int kblocks, int kper, float* part, const Epi& e, int* err, cudaStream_t st) {
+cudaError_t launch_gemm_bn(const uint8_t* a, const uint8_t* b, long long mtiles, int ntiles, int kblocks, int kper,
+                           float* part, const Epi& e, int* err, cudaStream_t st) {
   static bool configured = false;
   if (!configured) {
     cudaError_t c = cudaFuncSetAttribute(gemm_kernel<BN>, cudaFuncAttributeMaxDynamicSharedMemorySize, Cfg<BN>::SMEM);
@@ -334,8 +285,8 @@ cudaError_t launch_gemm_bn(const float* a, const Addr& aa, long long M, long lon
     configured = true;
   }
   const int splits = (kblocks + kper - 1) / kper;
-  gemm_kernel<BN><<<(unsigned)(mtiles * ntiles * splits), 128, Cfg<BN>::SMEM, st>>>(a, aa, M, K, b, kblocks, ntiles,
-                                                                                     kper, part, e, err);
+  gemm_kernel<BN><<<(unsigned)(mtiles * ntiles * splits), 128, Cfg<BN>::SMEM, st>>>(a, b, kblocks, ntiles, kper, part,
+                                                                                     e, err);
   if (part) {
     const long long n = e.M * (long long)e.N;
     splitk_reduce_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(part, splits, (int)(mtiles * ntiles), ntiles, BN,
@@ -394,8 +345,9 @@ int TcGemm::run(const float* a, Addr aa, const float* b, Addr ba, long long M, i
   int kper = kblocks;
   if (ksplit > 1) kper = (kblocks + ksplit - 1) / ksplit;
   const int splits = (kblocks + kper - 1) / kper;
+  const size_t a_bytes = (size_t)mtiles * kblocks * tg::A_BYTES;
   const size_t b_bytes = (size_t)ntiles * kblocks * bn * tg::BK * 2;
-  int rc = reserve(0, b_bytes);
+  int rc = reserve(a_bytes, b_bytes);
   if (rc != MSX_OK) return rc;
   float* pbuf = nullptr;
   if (splits > 1) {
@@ -409,20 +361,23 @@ int TcGemm::run(const float* a, Addr aa, const float* b, Addr ba, long long M, i
     }
     pbuf = part;
   }
-  const long long b_rows = (long long)ntiles * bn;
-  const long long b_thr = b_rows * kblocks * (tg::BK / 8);
+  const long long a_rows = mtiles * tg::BM, b_rows = (long long)ntiles * bn;
+  const long long a_thr = a_rows * kblocks * (tg::BK / 8), b_thr = b_rows * kblocks * (tg::BK / 8);
+  tg::pack_kernel<<<(unsigned)((a_thr + 255) / 256), 256, 0, st>>>(a, aa, M, K, tg::BM, a_rows, kblocks,
+                                                                   reinterpret_cast<uint4*>(a_img));
   tg::pack_kernel<<<(unsigned)((b_thr + 255) / 256), 256, 0, st>>>(b, ba, N, K, bn, b_rows, kblocks,
                                                                    reinterpret_cast<uint4*>(b_img));
   Epi e = epi;
   e.M = M;
   e.N = N;
+  const uint8_t* ai = reinterpret_cast<const uint8_t*>(a_img);
   const uint8_t* bi = reinterpret_cast<const uint8_t*>(b_img);
   cudaError_t c;
   switch (bn) {
-    case 32: c = tg::launch_gemm_bn<32>(a, aa, M, K, bi, mtiles, ntiles, kblocks, kper, pbuf, e, err, st); break;
-    case 64: c = tg::launch_gemm_bn<64>(a, aa, M, K, bi, mtiles, ntiles, kblocks, kper, pbuf, e, err, st); break;
-    case 128: c = tg::launch_gemm_bn<128>(a, aa, M, K, bi, mtiles, ntiles, kblocks, kper, pbuf, e, err, st); break;
-    default: c = tg::launch_gemm_bn<256>(a, aa, M, K, bi, mtiles, ntiles, kblocks, kper, pbuf, e, err, st); break;
+    case 32: c = tg::launch_gemm_bn<32>(ai, bi, mtiles, ntiles, kblocks, kper, pbuf, e, err, st); break;
+    case 64: c = tg::launch_gemm_bn<64>(ai, bi, mtiles, ntiles, kblocks, kper, pbuf, e, err, st); break;
+    case 128: c = tg::launch_gemm_bn<128>(ai, bi, mtiles, ntiles, kblocks, kper, pbuf, e, err, st); break;
+    default: c = tg::launch_gemm_bn<256>(ai, bi, mtiles, ntiles, kblocks, kper, pbuf, e, err, st); break;
   }
   return c == cudaSuccess ? MSX_OK : MSX_ERR_CUDA;
 }
