@@ -18,11 +18,11 @@
 //         ky in [-MY/2, MY/2) (real fields: kx >= 1 counted twice)
 //   h   = gelu(a_L P1^T + c1);  o = h P2^T + c2            (4 outputs: Re A, Im A, Re B, Im B)
 // Every contraction -- the lift, the pointwise layers, the head, their weight
-// gradients and the four partial-DFT stages of each spectral layer -- is a
-// bfloat16 GEMM with FP32 accumulation on the tensor cores (TcGemm,
-// msx_tcgemm.cu); the per-mode channel mixing (a C x C complex product per
-// mode, 0.3 % of the layer's multiply-adds), the activations and Adam are
-// FP32 kernels here.  gelu is the tanh form.
+// gradients, the four partial-DFT stages of each spectral layer and the per-mode
+// channel mixing (four batched real GEMMs per complex C x C product, one batch
+// per mode) -- is a bfloat16 GEMM with FP32 accumulation on the tensor cores
+// (TcGemm, msx_tcgemm.cu); the activations, reductions and Adam are FP32
+// kernels here.  gelu is the tanh form.
 #include "msx.h"
 #include "msx_internal.h"
 
@@ -73,58 +73,6 @@ __global__ void reduce_parts_kernel(const float* __restrict__ part, int nchunks,
   float s = 0.f;
   for (int k = 0; k < nchunks; ++k) s += part[(size_t)k * n + j];
   out[j] = s;
-}
-
-// Mode mixing.  X, Y: (S, C, NM) complex with NM = MX * MY modes; R: (NM, C, C) complex.
-// Y[s][o][m] = sum_i R[m][o][i] X[s][i][m]
-__global__ void mix_fwd_kernel(const float2* __restrict__ R, const float2* __restrict__ X, int C, int S, int NM,
-                               float2* __restrict__ Y) {
-  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= (long long)S * C * NM) return;
-  const int m = (int)(i % NM), o = (int)((i / NM) % C);
-  const long long s = i / ((long long)NM * C);
-  const float2* r = R + ((size_t)m * C + o) * C;
-  const float2* x = X + (size_t)s * C * NM + m;
-  float re = 0.f, im = 0.f;
-  for (int c = 0; c < C; ++c) {
-    const float2 w = __ldg(r + c), v = x[(size_t)c * NM];
-    re = fmaf(w.x, v.x, fmaf(-w.y, v.y, re));
-    im = fmaf(w.x, v.y, fmaf(w.y, v.x, im));
-  }
-  Y[i] = make_float2(re, im);
-}
-
-// dX[s][i][m] = sum_o conj(R[m][o][i]) dY[s][o][m]
-__global__ void mix_bwd_data_kernel(const float2* __restrict__ R, const float2* __restrict__ dY, int C, int S, int NM,
-                                    float2* __restrict__ dX) {
-  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= (long long)S * C * NM) return;
-  const int m = (int)(i % NM), c = (int)((i / NM) % C);
-  const long long s = i / ((long long)NM * C);
-  const float2* g = dY + (size_t)s * C * NM + m;
-  float re = 0.f, im = 0.f;
-  for (int o = 0; o < C; ++o) {
-    const float2 w = __ldg(R + ((size_t)m * C + o) * C + c), v = g[(size_t)o * NM];
-    re = fmaf(w.x, v.x, fmaf(w.y, v.y, re));
-    im = fmaf(w.x, v.y, fmaf(-w.y, v.x, im));
-  }
-  dX[i] = make_float2(re, im);
-}
-
-// dR[m][o][i] = sum_s dY[s][o][m] conj(X[s][i][m])  (as real parameters: d Re R, d Im R)
-__global__ void mix_bwd_weight_kernel(const float2* __restrict__ dY, const float2* __restrict__ X, int C, int S, int NM,
-                                      float2* __restrict__ dR) {
-  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= (long long)NM * C * C) return;
-  const int c = (int)(i % C), o = (int)((i / C) % C);
-  const int m = (int)(i / ((long long)C * C));
-  float re = 0.f, im = 0.f;
-  for (int s = 0; s < S; ++s) {
-    const float2 g = dY[((size_t)s * C + o) * NM + m], x = X[((size_t)s * C + c) * NM + m];
-    re = fmaf(g.x, x.x, fmaf(g.y, x.y, re));
-    im = fmaf(g.y, x.x, fmaf(-g.x, x.y, im));
-  }
-  dR[i] = make_float2(re, im);
 }
 
 __global__ void adam_kernel(float* __restrict__ p, const float* __restrict__ g, float* __restrict__ m, float* __restrict__ v,
@@ -351,10 +299,70 @@ int wgrad(msx_corrector* k, const float* dY, int n_out, const float* X, int n_in
   return MSX_OK;
 }
 
+// Per-mode channel mixing as batched tensor-core GEMMs, one batch per mode m: a complex
+// C x C product is four real GEMMs over the real and imaginary planes.
+//   X, Y: (S, C, NM) complex (float index ((s C + c) NM + m) 2 + e); R: (NM, C, C) complex.
+Addr modes_rows_s(const msx_corrector* k) {  // rows s, k = channel, of an (S, C, NM) complex array
+  const long long nm2 = 2LL * k->MX * k->MY;
+  return Addr{(long long)k->C * nm2, 0, 1, nm2, 0, 1};
+}
+Addr modes_rows_c(const msx_corrector* k) {  // rows channel, k = s
+  const long long nm2 = 2LL * k->MX * k->MY;
+  return Addr{nm2, 0, 1, (long long)k->C * nm2, 0, 1};
+}
+
+// Y = R X per mode: Yr = Xr Rr^T - Xi Ri^T, Yi = Xr Ri^T + Xi Rr^T
+int mix_forward(msx_corrector* k, const float* R, const float* X, int S, float* Y, cudaStream_t st) {
+  const int C = k->C, NM = k->MX * k->MY;
+  const Addr xa = modes_rows_s(k), ra = Addr{2LL * C, 0, 1, 2, 0, 1};
+  const long long rbs = 2LL * C * C;
+  for (int e = 0; e < 2; ++e) {
+    for (int part = 0; part < 2; ++part) {
+      // e = 0 (real out): Xr Rr^T then -Xi Ri^T; e = 1 (imag out): Xr Ri^T then Xi Rr^T
+      const float* xs = X + part;
+      const float* rs = R + ((e + part) & 1);
+      Epi ep = epi(Y + e, xa);
+      ep.accumulate = part;
+      ep.scale = (e == 0 && part == 1) ? -1.f : 1.f;
+      NN_GEMM(k->gemm.run_batched(xs, xa, 2, rs, ra, rbs, S, C, C, ep, 2, NM, st));
+    }
+  }
+  return MSX_OK;
+}
+
+// dX = conj(R)^T dY per mode: dXr = dYr Rr + dYi Ri, dXi = dYi Rr - dYr Ri
+// dR = dY X^H over the samples: dRr = dYr^T Xr + dYi^T Xi, dRi = dYi^T Xr - dYr^T Xi
+int mix_backward(msx_corrector* k, const float* R, const float* X, const float* dY, int S, float* dX, float* dR,
+                 cudaStream_t st) {
+  const int C = k->C, NM = k->MX * k->MY;
+  const Addr xa = modes_rows_s(k), ca = modes_rows_c(k);
+  const Addr rt = Addr{2, 0, 1, 2LL * C, 0, 1};  // B(i, o) = R[o][i]
+  const Addr ro = Addr{2LL * C, 0, 1, 2, 0, 1};  // out (o, i) of R's layout
+  const long long rbs = 2LL * C * C;
+  for (int e = 0; e < 2; ++e) {
+    for (int part = 0; part < 2; ++part) {
+      // dXr: dYr Rr + dYi Ri;  dXi: dYi Rr - dYr Ri
+      const float* gy = dY + (e == 0 ? part : 1 - part);
+      const float* rs = R + part;
+      Epi ep = epi(dX + e, xa);
+      ep.accumulate = part;
+      ep.scale = (e == 1 && part == 1) ? -1.f : 1.f;
+      NN_GEMM(k->gemm.run_batched(gy, xa, 2, rs, rt, rbs, S, C, C, ep, 2, NM, st));
+      // dRr: dYr Xr + dYi Xi;  dRi: dYi Xr - dYr Xi   (rows o, columns i, K = samples)
+      const float* gr = dY + (e == 0 ? part : 1 - part);
+      const float* xs = X + part;
+      Epi er = epi(dR + e, ro);
+      er.accumulate = part;
+      er.scale = (e == 1 && part == 1) ? -1.f : 1.f;
+      NN_GEMM(k->gemm.run_batched(gr, ca, 2, xs, ca, 2, C, C, S, er, rbs, NM, st));
+    }
+  }
+  return MSX_OK;
+}
+
 int forward(msx_corrector* k, int S, cudaStream_t st) {
   const long long SP = (long long)S * k->P;
   const int C = k->C, H = k->H, W = k->W, MX = k->MX, MY = k->MY;
-  const int NM = MX * MY;
   float* Pm = k->params;
   const size_t A = act_words(k, S);
   // lift
@@ -374,10 +382,10 @@ int forward(msx_corrector* k, int S, cudaStream_t st) {
     // DFT along y: rows (s, c, m), K = 2H -> X (S, C, MX, MY) complex
     NN_GEMM(k->gemm.run(k->U1, rows_scm(k), k->Bdy, rowmajor(2 * H), (long long)S * C * MX, 2 * MY, 2 * H,
                         epi(Xl, rowmajor(2 * MY)), st));
-    mix_fwd_kernel<<<blocks_for((long long)S * C * NM, 256), 256, 0, st>>>(
-        reinterpret_cast<const float2*>(Pm + k->oR[l]), reinterpret_cast<const float2*>(Xl), C, S, NM,
-        reinterpret_cast<float2*>(k->Yh));
-    NN_CUDA(cudaGetLastError());
+    {
+      const int rc = mix_forward(k, Pm + k->oR[l], Xl, S, k->Yh, st);
+      if (rc) return rc;
+    }
     // inverse DFT along y: rows (s, o, m), K = 2 MY -> U2 (S, H, C, MX) complex
     NN_GEMM(k->gemm.run(k->Yh, rowmajor(2 * MY), k->Biy, rowmajor(2 * MY), (long long)S * C * MX, 2 * H, 2 * MY,
                         epi(k->U2, rows_scm(k)), st));
@@ -407,7 +415,6 @@ int backward(msx_corrector* k, const float* dmaps, cudaStream_t st) {
   const int S = k->S_last;
   const long long SP = (long long)S * k->P;
   const int C = k->C, H = k->H, W = k->W, MX = k->MX, MY = k->MY;
-  const int NM = MX * MY;
   float* Pm = k->params;
   float* G = k->grads;
   const size_t A = act_words(k, S);
@@ -435,13 +442,8 @@ int backward(msx_corrector* k, const float* dmaps, cudaStream_t st) {
                         epi(k->U2, rowmajor(2 * MX)), st));
     NN_GEMM(k->gemm.run(k->U2, rows_scm(k), k->Biy, colmajor(2 * MY), (long long)S * C * MX, 2 * MY, 2 * H,
                         epi(k->Yh, rowmajor(2 * MY)), st));
-    mix_bwd_weight_kernel<<<blocks_for((long long)NM * C * C, 256), 256, 0, st>>>(
-        reinterpret_cast<const float2*>(k->Yh), reinterpret_cast<const float2*>(Xl), C, S, NM,
-        reinterpret_cast<float2*>(G + k->oR[l]));
-    mix_bwd_data_kernel<<<blocks_for((long long)S * C * NM, 256), 256, 0, st>>>(
-        reinterpret_cast<const float2*>(Pm + k->oR[l]), reinterpret_cast<const float2*>(k->Yh), C, S, NM,
-        reinterpret_cast<float2*>(k->U1));  // dX (S, C, MX, MY) complex, in U1's space
-    NN_CUDA(cudaGetLastError());
+    // dX (S, C, MX, MY) complex into U1's space; dR into the gradients
+    if ((rc = mix_backward(k, Pm + k->oR[l], Xl, k->Yh, S, k->U1, G + k->oR[l], st))) return rc;
     // dX -> dU1 (S, H, C, MX): write into U2 (free now)
     NN_GEMM(k->gemm.run(k->U1, rowmajor(2 * MY), k->Bdy, colmajor(2 * H), (long long)S * C * MX, 2 * H, 2 * MY,
                         epi(k->U2, rows_scm(k)), st));

@@ -46,6 +46,7 @@ struct Epi {
   float* act;
   int accumulate;
   float scale;
+  long long ybs;  // batched GEMMs: offset of batch b's output (y, add, act) is b * ybs
 };
 
 // D (M x N) = A (M x K) . B (N x K)^T on tcgen05 in bfloat16 with FP32 accumulation
@@ -62,6 +63,10 @@ struct TcGemm {
   // in a fixed order before the epilogue (for the long-K weight gradients).
   int run(const float* a, Addr aa, const float* b, Addr ba, long long M, int N, long long K, const Epi& e,
           cudaStream_t st, int ksplit = 1);
+  // `batch` independent GEMMs of the same shape; batch b reads A at a + b * a_bs, B at
+  // b_ptr + b * b_bs and writes at e.y + b * y_bs (floats); no K split.
+  int run_batched(const float* a, Addr aa, long long a_bs, const float* b, Addr ba, long long b_bs, long long M,
+                  int N, long long K, const Epi& e, long long y_bs, int batch, cudaStream_t st);
   int check();
   void release();
 };

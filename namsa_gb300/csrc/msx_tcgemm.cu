@@ -71,10 +71,16 @@ __host__ __device__ __forceinline__ long long addr_of(const Addr& a, long long r
 // address and the split of k0 are computed once per thread; the 8 elements step
 // through k incrementally, with two 16-byte loads when they are contiguous.
 __global__ void pack_kernel(const float* __restrict__ src, Addr a, long long rows, long long K, int tile_rows,
-                            long long rows_pad, int kblocks, uint4* __restrict__ img) {
-  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+                            long long rows_pad, int kblocks, uint4* __restrict__ img, int batch = 1,
+                            long long src_bs = 0) {
+  long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   const long long chunks = (long long)kblocks * (BK / 8);
-  if (i >= rows_pad * chunks) return;
+  const long long per = rows_pad * chunks;
+  if (i >= per * batch) return;
+  const long long bt = i / per;  // batch of this element; its image and source are offset by it
+  i -= bt * per;
+  src += bt * src_bs;
+  img += bt * (per * 8 * 2 / 16);
   const long long r = i / chunks;
   const int ch = (int)(i - r * chunks);
   const long long k0 = (long long)ch * 8;
@@ -111,16 +117,24 @@ __global__ void pack_kernel(const float* __restrict__ src, Addr a, long long row
 // writes its raw 128 x BN partial to part[(split * tiles + tile) * 128 * BN].
 template <int BN>
 __global__ void __launch_bounds__(128) gemm_kernel(const uint8_t* __restrict__ A, const uint8_t* __restrict__ B,
-                                                   int kblocks, int ntiles_n, int kper, float* __restrict__ part,
-                                                   Epi e, int* __restrict__ err) {
+                                                   int kblocks, int ntiles_n, int ntiles_total, int kper,
+                                                   float* __restrict__ part, Epi e, int* __restrict__ err) {
   using C = Cfg<BN>;
   extern __shared__ __align__(1024) uint8_t smem_raw[];
   uint8_t* smem = smem_raw + ((1024u - (smem_u32(smem_raw) & 1023u)) & 1023u);
   __shared__ uint64_t full[STAGES], empty[STAGES], done;
   __shared__ uint32_t tmem_base;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int tiles = (int)gridDim.x / ((kblocks + kper - 1) / kper);
-  const int split = (int)blockIdx.x / tiles, tile = (int)blockIdx.x % tiles;
+  const int splits = (kblocks + kper - 1) / kper;
+  const int tiles = ntiles_total;
+  const int bt = (int)blockIdx.x / (tiles * splits);  // batch
+  const int inb = (int)blockIdx.x - bt * tiles * splits;
+  const int split = inb / tiles, tile = inb % tiles;
+  A += (size_t)bt * (size_t)(tiles / ntiles_n) * kblocks * A_BYTES;
+  B += (size_t)bt * (size_t)ntiles_n * kblocks * C::B_BYTES;
+  e.y += bt * e.ybs;
+  if (e.add) e.add += bt * e.ybs;
+  if (e.act) e.act += bt * e.ybs;
   const int mt = tile / ntiles_n, nt = tile % ntiles_n;
   const int kb0 = split * kper, kb1 = kb0 + kper < kblocks ? kb0 + kper : kblocks;
   if (warp == 0) {
@@ -277,7 +291,7 @@ __global__ void splitk_reduce_kernel(const float* __restrict__ part, int splits,
 
 template <int BN>
 cudaError_t launch_gemm_bn(const uint8_t* a, const uint8_t* b, long long mtiles, int ntiles, int kblocks, int kper,
-                           float* part, const Epi& e, int* err, cudaStream_t st) {
+                           float* part, const Epi& e, int* err, cudaStream_t st, int batch = 1) {
   static bool configured = false;
   if (!configured) {
     cudaError_t c = cudaFuncSetAttribute(gemm_kernel<BN>, cudaFuncAttributeMaxDynamicSharedMemorySize, Cfg<BN>::SMEM);
@@ -285,8 +299,8 @@ cudaError_t launch_gemm_bn(const uint8_t* a, const uint8_t* b, long long mtiles,
     configured = true;
   }
   const int splits = (kblocks + kper - 1) / kper;
-  gemm_kernel<BN><<<(unsigned)(mtiles * ntiles * splits), 128, Cfg<BN>::SMEM, st>>>(a, b, kblocks, ntiles, kper, part,
-                                                                                     e, err);
+  gemm_kernel<BN><<<(unsigned)(mtiles * ntiles * splits * batch), 128, Cfg<BN>::SMEM, st>>>(
+      a, b, kblocks, ntiles, (int)(mtiles * ntiles), kper, part, e, err);
   if (part) {
     const long long n = e.M * (long long)e.N;
     splitk_reduce_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(part, splits, (int)(mtiles * ntiles), ntiles, BN,
@@ -378,6 +392,41 @@ int TcGemm::run(const float* a, Addr aa, const float* b, Addr ba, long long M, i
     case 64: c = tg::launch_gemm_bn<64>(ai, bi, mtiles, ntiles, kblocks, kper, pbuf, e, err, st); break;
     case 128: c = tg::launch_gemm_bn<128>(ai, bi, mtiles, ntiles, kblocks, kper, pbuf, e, err, st); break;
     default: c = tg::launch_gemm_bn<256>(ai, bi, mtiles, ntiles, kblocks, kper, pbuf, e, err, st); break;
+  }
+  return c == cudaSuccess ? MSX_OK : MSX_ERR_CUDA;
+}
+
+int TcGemm::run_batched(const float* a, Addr aa, long long a_bs, const float* b, Addr ba, long long b_bs, long long M,
+                        int N, long long K, const Epi& epi, long long y_bs, int batch, cudaStream_t st) {
+  if (batch < 1 || M <= 0 || N <= 0 || K <= 0 || N > 4096) return MSX_ERR_INVALID;
+  const int bn = bn_for(N);
+  const long long mtiles = (M + tg::BM - 1) / tg::BM;
+  const int ntiles = (N + bn - 1) / bn;
+  const long long kbl = (K + tg::BK - 1) / tg::BK;
+  if (kbl > (1LL << 30) || mtiles * ntiles * batch > (1LL << 30)) return MSX_ERR_INVALID;
+  const int kblocks = (int)kbl;
+  const size_t a_bytes = (size_t)batch * mtiles * kblocks * tg::A_BYTES;
+  const size_t b_bytes = (size_t)batch * ntiles * kblocks * bn * tg::BK * 2;
+  int rc = reserve(a_bytes, b_bytes);
+  if (rc != MSX_OK) return rc;
+  const long long a_rows = mtiles * tg::BM, b_rows = (long long)ntiles * bn;
+  const long long a_thr = a_rows * kblocks * (tg::BK / 8) * batch, b_thr = b_rows * kblocks * (tg::BK / 8) * batch;
+  tg::pack_kernel<<<(unsigned)((a_thr + 255) / 256), 256, 0, st>>>(a, aa, M, K, tg::BM, a_rows, kblocks,
+                                                                   reinterpret_cast<uint4*>(a_img), batch, a_bs);
+  tg::pack_kernel<<<(unsigned)((b_thr + 255) / 256), 256, 0, st>>>(b, ba, N, K, bn, b_rows, kblocks,
+                                                                   reinterpret_cast<uint4*>(b_img), batch, b_bs);
+  Epi e = epi;
+  e.M = M;
+  e.N = N;
+  e.ybs = y_bs;
+  const uint8_t* ai = reinterpret_cast<const uint8_t*>(a_img);
+  const uint8_t* bi = reinterpret_cast<const uint8_t*>(b_img);
+  cudaError_t c;
+  switch (bn) {
+    case 32: c = tg::launch_gemm_bn<32>(ai, bi, mtiles, ntiles, kblocks, kblocks, nullptr, e, err, st, batch); break;
+    case 64: c = tg::launch_gemm_bn<64>(ai, bi, mtiles, ntiles, kblocks, kblocks, nullptr, e, err, st, batch); break;
+    case 128: c = tg::launch_gemm_bn<128>(ai, bi, mtiles, ntiles, kblocks, kblocks, nullptr, e, err, st, batch); break;
+    default: c = tg::launch_gemm_bn<256>(ai, bi, mtiles, ntiles, kblocks, kblocks, nullptr, e, err, st, batch); break;
   }
   return c == cudaSuccess ? MSX_OK : MSX_ERR_CUDA;
 }

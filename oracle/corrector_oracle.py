@@ -121,6 +121,22 @@ def _gelu_d(z):
 
 
 # ------------------------------------------------------------------ forward / backward
+def _mix(net, Rr, Ri, Ur, Ui, kind):
+    """Per-mode complex channel mixing as the four real GEMMs the CUDA code runs
+    (operands rounded to bfloat16 when the net emulates the tensor cores).
+    fwd: Y = R X; data: dX = conj(R)^T dY (U = dY); weight: dR = dY X^H summed over
+    samples (U = dY, returned with X given as Rr, Ri of shape (S, i, m, q))."""
+    b = bf16 if net.emulate else (lambda x: x)
+    if kind == 'fwd':
+        e = lambda r, u: np.einsum('mqoi,simq->somq', b(r), b(u))
+        return (e(Rr, Ur) - e(Ri, Ui)) + 1j * (e(Ri, Ur) + e(Rr, Ui))
+    if kind == 'data':
+        e = lambda r, u: np.einsum('mqoi,somq->simq', b(r), b(u))
+        return (e(Rr, Ur) + e(Ri, Ui)) + 1j * (e(Rr, Ui) - e(Ri, Ur))
+    e = lambda u, x: np.einsum('somq,simq->mqoi', b(u), b(x))
+    return (e(Ur, Rr) + e(Ui, Ri)) + 1j * (e(Ui, Rr) - e(Ur, Ri))
+
+
 def _spec(net, p, l, a):
     """Spectral part of layer l for a (S, H, W, C); returns (sp, X) with X the retained modes."""
     S, H, W, C, MX, MY = a.shape[0], net.H, net.W, net.C, net.MX, net.MY
@@ -128,8 +144,8 @@ def _spec(net, p, l, a):
     A2 = U1.transpose(0, 2, 3, 1, 4).reshape(S * C * MX, 2 * H)
     Xr = net.g(A2, net.Bdy).reshape(S, C, MX, MY, 2)
     X = Xr[..., 0] + 1j * Xr[..., 1]
-    R = p[f'R{l + 1}'][..., 0] + 1j * p[f'R{l + 1}'][..., 1]                  # (MX, MY, o, i)
-    Y = np.einsum('mqoi,simq->somq', R, X)
+    Rr, Ri = p[f'R{l + 1}'][..., 0], p[f'R{l + 1}'][..., 1]                    # (MX, MY, o, i)
+    Y = _mix(net, Rr, Ri, X.real, X.imag, 'fwd')
     Yr = np.stack([Y.real, Y.imag], -1).reshape(S * C * MX, 2 * MY)
     U2 = net.g(Yr, net.Biy).reshape(S, C, MX, H, 2).transpose(0, 3, 1, 2, 4)   # (S, H, C, MX, 2)
     sp = net.g(U2.reshape(S * H * C, 2 * MX), net.Bix).reshape(S, H, C, W).transpose(0, 1, 3, 2)
@@ -179,10 +195,10 @@ def backward(net, cache, dmaps):
         dU2 = net.g(dz.transpose(0, 1, 3, 2).reshape(S * H * C, W), net.Bix.T).reshape(S, H, C, MX, 2)
         dYr = net.g(dU2.transpose(0, 2, 3, 1, 4).reshape(S * C * MX, 2 * H), net.Biy.T).reshape(S, C, MX, MY, 2)
         dY = dYr[..., 0] + 1j * dYr[..., 1]
-        R = p[f'R{l + 1}'][..., 0] + 1j * p[f'R{l + 1}'][..., 1]
-        dR = np.einsum('somq,simq->mqoi', dY, np.conj(Xs[l]))
+        Rr, Ri = p[f'R{l + 1}'][..., 0], p[f'R{l + 1}'][..., 1]
+        dR = _mix(net, Xs[l].real, Xs[l].imag, dY.real, dY.imag, 'weight')
         g[f'R{l + 1}'] = np.stack([dR.real, dR.imag], -1)
-        dX = np.einsum('mqoi,somq->simq', np.conj(R), dY)
+        dX = _mix(net, Rr, Ri, dY.real, dY.imag, 'data')
         dXr = np.stack([dX.real, dX.imag], -1).reshape(S * C * MX, 2 * MY)
         dU1 = net.g(dXr, net.Bdy.T).reshape(S, C, MX, H, 2).transpose(0, 3, 1, 2, 4)
         da_sp = net.g(dU1.reshape(S * H * C, 2 * MX), net.Bdx.T).reshape(S, H, C, W).transpose(0, 1, 3, 2)
