@@ -29,6 +29,7 @@
 
 #include <cuda_bf16.h>
 
+#include <atomic>
 #include <cstring>
 
 namespace msx {
@@ -292,11 +293,16 @@ __global__ void splitk_reduce_kernel(const float* __restrict__ part, int splits,
 template <int BN>
 cudaError_t launch_gemm_bn(const uint8_t* a, const uint8_t* b, long long mtiles, int ntiles, int kblocks, int kper,
                            float* part, const Epi& e, int* err, cudaStream_t st, int batch = 1) {
-  static bool configured = false;
-  if (!configured) {
+  // the shared-memory attribute is set once per device (it belongs to the device's context)
+  static std::atomic<unsigned long long> configured{0};
+  int dev = 0;
+  cudaError_t c0 = cudaGetDevice(&dev);
+  if (c0 != cudaSuccess) return c0;
+  const unsigned long long bit = 1ull << (dev & 63);
+  if (!(configured.load(std::memory_order_acquire) & bit)) {
     cudaError_t c = cudaFuncSetAttribute(gemm_kernel<BN>, cudaFuncAttributeMaxDynamicSharedMemorySize, Cfg<BN>::SMEM);
     if (c != cudaSuccess) return c;
-    configured = true;
+    configured.fetch_or(bit, std::memory_order_release);
   }
   const int splits = (kblocks + kper - 1) / kper;
   gemm_kernel<BN><<<(unsigned)(mtiles * ntiles * splits * batch), 128, Cfg<BN>::SMEM, st>>>(
