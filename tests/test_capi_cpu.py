@@ -103,3 +103,24 @@ def test_noalloc_rejects_misaligned_pointers(libmsx):
                  (good, good, good, odd, good), (good, good, good, good, odd + 2)]:
         assert call(*args) == _lib.MSX_ERR_INVALID
         assert 'aligned' in _lib.last_error()
+
+
+def test_newer_entry_points_reject_bad_arguments_without_device(libmsx):
+    """Argument checks of the stored-stack detector reduction, the tensor-core GEMM, the
+    probe stack and the corrector run on the host before any device work."""
+    from namsa_gb300 import _lib
+    vp = ctypes.c_void_p
+    assert libmsx.msx_integrate_cbed(vp(0x1000), 2, 0, 8, None, 1, vp(0x2000), None) == _lib.MSX_ERR_INVALID
+    assert libmsx.msx_integrate_cbed(vp(0x1000), 2, 8, 8, None, 3, vp(0x2000), None) == _lib.MSX_ERR_INVALID
+    assert 'weights' in _lib.last_error()
+    assert libmsx.msx_gemm_bf16(vp(0x1000), 4, vp(0x2000), 4, 8, 8, 8, vp(0x3000), 8, None, 0, None) == \
+        _lib.MSX_ERR_INVALID  # leading dimensions shorter than the rows
+    assert libmsx.msx_gemm_bf16(vp(0x1000), 8, vp(0x2000), 8, 8, 5000, 8, vp(0x3000), 5000, None, 0, None) == \
+        _lib.MSX_ERR_INVALID  # n above 4096
+    assert libmsx.msx_plan_probe_stack(None, None, None, None, 1, 1.0, None, None) == _lib.MSX_ERR_INVALID
+    h = ctypes.c_void_p()
+    assert libmsx.msx_corrector_create(256, 256, 6, 48, 4, 32, 64, 4, ctypes.byref(h)) == _lib.MSX_ERR_INVALID
+    assert libmsx.msx_corrector_create(256, 256, 6, 32, 4, 200, 64, 4, ctypes.byref(h)) == _lib.MSX_ERR_INVALID
+    assert libmsx.msx_corrector_apply_map(None, 1, 8, 8, None, 0, 0, 0, None) == _lib.MSX_ERR_INVALID
+    assert libmsx.msx_corrector_map_grad(vp(0x1000), vp(0x2000), 1, 8, 8, 0, 0, 1, None, vp(0x3000), None) == \
+        _lib.MSX_ERR_INVALID  # the phase form needs the maps
