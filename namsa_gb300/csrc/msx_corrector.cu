@@ -299,34 +299,20 @@ int wgrad(msx_corrector* k, const float* dY, int n_out, const float* X, int n_in
   return MSX_OK;
 }
 
-// Per-mode channel mixing as batched tensor-core GEMMs, one batch per mode m: a complex
-// C x C product is four real GEMMs over the real and imaginary planes.
+// Per-mode channel mixing as batched tensor-core GEMMs, one batch per mode m, each
+// complex product as one real GEMM over [real, imaginary] planes (TcGemm::run_cplx).
 //   X, Y: (S, C, NM) complex (float index ((s C + c) NM + m) 2 + e); R: (NM, C, C) complex.
-Addr modes_rows_s(const msx_corrector* k) {  // rows s, k = channel, of an (S, C, NM) complex array
+// Rows s, columns (part, channel) of an (S, C, NM) complex array, for one mode.
+Addr modes_rows_s_parts(const msx_corrector* k) {
   const long long nm2 = 2LL * k->MX * k->MY;
-  return Addr{(long long)k->C * nm2, 0, 1, nm2, 0, 1};
-}
-Addr modes_rows_c(const msx_corrector* k) {  // rows channel, k = s
-  const long long nm2 = 2LL * k->MX * k->MY;
-  return Addr{nm2, 0, 1, (long long)k->C * nm2, 0, 1};
+  return Addr{(long long)k->C * nm2, 0, 1, 1, nm2, k->C};
 }
 
-// Y = R X per mode: Yr = Xr Rr^T - Xi Ri^T, Yi = Xr Ri^T + Xi Rr^T
+// Y = R X per mode: [Yr, Yi] = [Xr, Xi] against rows [Rr, -Ri] and [Ri, Rr]
 int mix_forward(msx_corrector* k, const float* R, const float* X, int S, float* Y, cudaStream_t st) {
   const int C = k->C, NM = k->MX * k->MY;
-  const Addr xa = modes_rows_s(k), ra = Addr{2LL * C, 0, 1, 2, 0, 1};
-  const long long rbs = 2LL * C * C;
-  for (int e = 0; e < 2; ++e) {
-    for (int part = 0; part < 2; ++part) {
-      // e = 0 (real out): Xr Rr^T then -Xi Ri^T; e = 1 (imag out): Xr Ri^T then Xi Rr^T
-      const float* xs = X + part;
-      const float* rs = R + ((e + part) & 1);
-      Epi ep = epi(Y + e, xa);
-      ep.accumulate = part;
-      ep.scale = (e == 0 && part == 1) ? -1.f : 1.f;
-      NN_GEMM(k->gemm.run_batched(xs, xa, 2, rs, ra, rbs, S, C, C, ep, 2, NM, st));
-    }
-  }
+  const Addr xa = modes_rows_s_parts(k);
+  NN_GEMM(k->gemm.run_cplx(X, xa, 2, R, 2LL * C, 2, 2LL * C * C, C, C, 1, S, epi(Y, xa), 2, NM, st));
   return MSX_OK;
 }
 
@@ -335,28 +321,15 @@ int mix_forward(msx_corrector* k, const float* R, const float* X, int S, float* 
 int mix_backward(msx_corrector* k, const float* R, const float* X, const float* dY, int S, float* dX, float* dR,
                  cudaStream_t st) {
   const int C = k->C, NM = k->MX * k->MY;
-  const Addr xa = modes_rows_s(k), ca = modes_rows_c(k);
-  const Addr rt = Addr{2, 0, 1, 2LL * C, 0, 1};  // B(i, o) = R[o][i]
-  const Addr ro = Addr{2LL * C, 0, 1, 2, 0, 1};  // out (o, i) of R's layout
-  const long long rbs = 2LL * C * C;
-  for (int e = 0; e < 2; ++e) {
-    for (int part = 0; part < 2; ++part) {
-      // dXr: dYr Rr + dYi Ri;  dXi: dYi Rr - dYr Ri
-      const float* gy = dY + (e == 0 ? part : 1 - part);
-      const float* rs = R + part;
-      Epi ep = epi(dX + e, xa);
-      ep.accumulate = part;
-      ep.scale = (e == 1 && part == 1) ? -1.f : 1.f;
-      NN_GEMM(k->gemm.run_batched(gy, xa, 2, rs, rt, rbs, S, C, C, ep, 2, NM, st));
-      // dRr: dYr Xr + dYi Xi;  dRi: dYi Xr - dYr Xi   (rows o, columns i, K = samples)
-      const float* gr = dY + (e == 0 ? part : 1 - part);
-      const float* xs = X + part;
-      Epi er = epi(dR + e, ro);
-      er.accumulate = part;
-      er.scale = (e == 1 && part == 1) ? -1.f : 1.f;
-      NN_GEMM(k->gemm.run_batched(gr, ca, 2, xs, ca, 2, C, C, S, er, rbs, NM, st));
-    }
-  }
+  const long long nm2 = 2LL * NM;
+  const Addr xa = modes_rows_s_parts(k);
+  // dX: rows s, K = (part, o) of dY; B row (part, c), column (part', o) = R[o][c] (xor), - for (1, 0)
+  NN_GEMM(k->gemm.run_cplx(dY, xa, 2, R, 2, 2LL * C, 2LL * C * C, C, C, 2, S, epi(dX, xa), 2, NM, st));
+  // dR: rows o, K = (part, s) of dY; B row (part, c), column (part', s) = X[s][c] (xor), - for (1, 0);
+  // out (o, part, c) in R's layout
+  const Addr ya = Addr{nm2, 0, 1, 1, (long long)C * nm2, S};
+  const Addr ro = Addr{2LL * C, 0, 1, 1, 2, C};
+  NN_GEMM(k->gemm.run_cplx(dY, ya, 2, X, nm2, (long long)C * nm2, 2, C, S, 2, C, epi(dR, ro), 2LL * C * C, NM, st));
   return MSX_OK;
 }
 

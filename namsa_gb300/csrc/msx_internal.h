@@ -67,6 +67,13 @@ struct TcGemm {
   // b_ptr + b * b_bs and writes at e.y + b * y_bs (floats); no K split.
   int run_batched(const float* a, Addr aa, long long a_bs, const float* b, Addr ba, long long b_bs, long long M,
                   int N, long long K, const Epi& e, long long y_bs, int batch, cudaStream_t st);
+  // `batch` complex products in one real GEMM each: B (2 hn x 2 hk) is the real
+  // embedding of src (pack_cplx_kernel: element (i, j) at src + i si + j sj, parts
+  // interleaved, negated block neg = 1 for (0, 1), 2 for (1, 0)); src of batch b at
+  // src + b * src_bs.
+  int run_cplx(const float* a, Addr aa, long long a_bs, const float* src, long long si, long long sj,
+               long long src_bs, int hn, int hk, int neg, long long M, const Epi& e, long long y_bs, int batch,
+               cudaStream_t st);
   int check();
   void release();
 };

@@ -29,6 +29,7 @@
 
 #include <cuda_bf16.h>
 
+#include <algorithm>
 #include <atomic>
 #include <cstring>
 
@@ -111,6 +112,46 @@ __global__ void pack_kernel(const float* __restrict__ src, Addr a, long long row
   const long long tile = r / tile_rows;
   const int row = (int)(r - tile * tile_rows), kb = (int)(k0 / BK);
   const size_t byte = ((size_t)tile * kblocks + kb) * ((size_t)tile_rows * BK * 2) + sw128(row, (int)(k0 % BK));
+  img[byte / 16] = *reinterpret_cast<const uint4*>(v);
+}
+
+// Real embedding of a complex product, packed like pack_kernel: B is N x K with
+// N = 2 hn, K = 2 hk; row n = (bn, i) = (n / hn, n % hn), column k = (bk, j); the
+// element is src[i si + j sj + (bn xor bk)] (a complex array, parts interleaved),
+// negated where (bn, bk) = (0, 1) (neg = 1) or (1, 0) (neg = 2).  With the
+// right orientation of src, D = A B^T then gives real and imaginary parts of a
+// complex product in one GEMM: [Re, Im] of x z^T is [xr, xi] against rows
+// [zr, -zi] and [zi, zr].
+__global__ void pack_cplx_kernel(const float* __restrict__ src, long long si, long long sj, long long src_bs, int hn,
+                                 int hk, int neg, int tile_rows, int rows_pad, int kblocks, uint4* __restrict__ img,
+                                 int batch) {
+  long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long long chunks = (long long)kblocks * (BK / 8);
+  const long long per = (long long)rows_pad * chunks;
+  if (i >= per * batch) return;
+  const long long bt = i / per;
+  i -= bt * per;
+  src += bt * src_bs;
+  img += bt * (per * 8 * 2 / 16);
+  const int r = (int)(i / chunks);
+  const int ch = (int)(i - (long long)r * chunks);
+  const int k0 = ch * 8;
+  __align__(16) __nv_bfloat16 v[8];
+  const int N = 2 * hn, K = 2 * hk;
+  const int bn = r / hn, ii = r - (r / hn) * hn;
+#pragma unroll
+  for (int j = 0; j < 8; ++j) {
+    const int k = k0 + j;
+    float x = 0.f;
+    if (r < N && k < K) {
+      const int bk = k / hk, jj = k - bk * hk;
+      x = __ldg(src + ii * si + jj * sj + (bn ^ bk));
+      if ((neg == 1 && bn == 0 && bk == 1) || (neg == 2 && bn == 1 && bk == 0)) x = -x;
+    }
+    v[j] = __float2bfloat16_rn(x);
+  }
+  const int tile = r / tile_rows, row = r - tile * tile_rows, kb = k0 / BK;
+  const size_t byte = ((size_t)tile * kblocks + kb) * ((size_t)tile_rows * BK * 2) + sw128(row, k0 % BK);
   img[byte / 16] = *reinterpret_cast<const uint4*>(v);
 }
 
@@ -290,6 +331,495 @@ __global__ void splitk_reduce_kernel(const float* __restrict__ part, int splits,
   if (e.act) e.act[o] = gelu_t(z);
 }
 
+// ------------------------------------------------------------ persistent, warp-specialised GEMM
+// One CTA of 416 threads per SM loops over the output tiles (batch, mt, nt) =
+// blockIdx.x, blockIdx.x + gridDim.x, ... (nt fastest):
+//   warps 0-3   operand loaders: bring the FP32 rows of A for a K block into an FP32
+//               staging slot (bulk copies where A's rows or row groups are contiguous,
+//               else 4-byte asynchronous copies), then round them to bfloat16 into the
+//               swizzled stage (no packing pass over A); thread 0 also moves the stage's
+//               packed B block with one bulk copy;
+//   warps 4-11  epilogue, two groups of four taking alternate tiles; warp w reads
+//               TMEM lanes 32 (w mod 4) .. + 31 (tile rows);
+//   warp 12     holds two BN-column accumulators in TMEM; lane 0 issues the MMAs.
+// The accumulators alternate between tiles, so a tile's epilogue overlaps the next
+// tile's loads and MMAs.  Barriers: afull[slot] (staging slot filled: 128 loader
+// arrivals with the bulk bytes), full[s] (128 loader arrivals: bfloat16 A written),
+// bfull[s] (the B bytes), empty[s] (MMA commit), accf[b] (MMA commit of accumulator
+// b), acce[b] (one arrival per warp of the epilogue group).  Rows of A at or past M
+// are not converted (an MMA row depends on its own A row only, and those rows are not
+// stored); K steps of 16 past K are not issued, and the rest of the last K step is
+// zero.  Every wait is bounded; the loaders take each decision together (a barrier
+// reduction), on a timeout a role sets *err and stops, the MMA issuer waits (bounded)
+// for its MMAs and the loaders for their copies before the tensor memory is freed.
+namespace ws {
+constexpr int LOADERS = 128;  // warps 0-3
+constexpr int EPI_WARPS = 8;  // warps 4-11
+constexpr int MMA_WARP = 12;
+constexpr int THREADS = 13 * 32;
+constexpr int SLOT_FLOATS = BM * BK;  // one FP32 staging slot (32 KB)
+template <int BN>
+struct Cfg {
+  static constexpr int STAGES = BN == 256 ? 2 : 3;  // bfloat16 operand stages
+  static constexpr int DEPTH = BN <= 64 ? 3 : 2;    // FP32 staging slots: A stages in flight
+  static constexpr int B_BYTES = BN * BK * 2;
+  static constexpr int STAGE_BYTES = A_BYTES + B_BYTES;
+  static constexpr int EPI_FLOATS = EPI_WARPS * 32 * 33;
+  static constexpr int SMEM = STAGES * STAGE_BYTES + DEPTH * SLOT_FLOATS * 4 + EPI_FLOATS * 4 + 1024;
+  static constexpr uint32_t TMEM_COLS = 2 * BN;
+};
+
+__device__ __forceinline__ void cp4(float* dst, const float* src) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(smem_u32(dst)), "l"(src) : "memory");
+}
+// the barrier's phase completes (for this thread's arrival) once this thread's copies have landed
+__device__ __forceinline__ void cp_arrive(uint64_t* bar) {
+  asm volatile("cp.async.mbarrier.arrive.noinc.shared::cta.b64 [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+// barrier 1 over the 128 loader threads: true on all of them iff `ok` on all of them
+__device__ __forceinline__ bool loaders_all(bool ok) {
+  uint32_t r;
+  asm volatile(
+      "{\n .reg .pred p, q;\n setp.ne.u32 p, %1, 0;\n bar.red.and.pred q, 1, 128, p;\n selp.u32 %0, 1, 0, q;\n}\n"
+      : "=r"(r)
+      : "r"((uint32_t)ok)
+      : "memory");
+  return r != 0;
+}
+__device__ __forceinline__ void loaders_sync() { asm volatile("bar.sync 1, 128;" ::: "memory"); }
+
+__device__ __forceinline__ void store_chunk(uint8_t* sa, int row, int ch, const float (&x)[8]) {
+  __align__(16) __nv_bfloat162 h[4];
+#pragma unroll
+  for (int j = 0; j < 4; ++j) h[j] = __floats2bfloat162_rn(x[2 * j], x[2 * j + 1]);
+  *reinterpret_cast<uint4*>(sa + sw128(row, ch * 8)) = *reinterpret_cast<const uint4*>(h);
+}
+
+// How a stage of A (rows r0 .. r0 + 127, K block kb, nk = min(64, K - 64 kb) values)
+// reaches its staging slot:
+//   ROWRUN   k contiguous: thread i copies row r0 + i (nk values) to slot[i][0 .. nk)
+//            with one bulk copy (16-byte aligned runs), else with plain loads;
+//   GROUPRUN rows contiguous in groups of rc with k stride rc (a group's K block is one
+//            run of nk * rc values): thread i < 128 / rc copies group i to
+//            slot[i * 64 rc ..], element (k, r mod rc) at k rc + r mod rc;
+//   GENERIC  thread i copies row r0 + i value by value (4-byte asynchronous copies),
+//            element (r, k) at ((k / 8) 128 + i) 8 + k mod 8.
+enum { ROWRUN = 0, GROUPRUN = 1, GENERIC = 2 };
+
+__device__ __forceinline__ int a_mode(const float* A, const Addr& a, long long a_bs, long long M) {
+  if (a.kc == 1 && a.t1 == 1) return ROWRUN;
+  if (a.s2 == 1 && a.kc == 1 && a.t1 == a.rc && a.rc % 4 == 0 && BM % a.rc == 0 && M % a.rc == 0 && a.s1 % 4 == 0 &&
+      a_bs % 4 == 0 && (reinterpret_cast<uintptr_t>(A) & 15u) == 0)
+    return GROUPRUN;
+  return GENERIC;
+}
+
+// Thread i's part of filling one slot; every loader thread arrives once on `bar`.
+__device__ __forceinline__ void issue_a(float* stg, uint64_t* bar, int mode, const float* __restrict__ A,
+                                        const Addr& a, long long M, long long K, long long r0, int kb, int i) {
+  const long long kb0 = (long long)kb * BK;
+  const int nk = (int)(K - kb0 < BK ? K - kb0 : BK);
+  if (mode == ROWRUN) {
+    const long long r = r0 + i;
+    if (r < M) {
+      const float* src = A + (r / a.rc) * a.s1 + (r % a.rc) * a.s2 + kb0;
+      if ((nk & 3) == 0 && (reinterpret_cast<uintptr_t>(src) & 15u) == 0) {
+        mbar_expect_tx(bar, (uint32_t)nk * 4u);
+        bulk_g2s(stg + i * BK, src, (uint32_t)nk * 4u, bar);
+        return;
+      }
+      for (int k = 0; k < nk; ++k) stg[i * BK + k] = __ldg(src + k);
+    }
+    mbar_arrive(bar);
+  } else if (mode == GROUPRUN) {
+    const int rc = (int)a.rc;
+    const long long r = r0 + (long long)i * rc;
+    if (i < BM / rc && r < M) {
+      const uint32_t bytes = (uint32_t)nk * (uint32_t)rc * 4u;
+      mbar_expect_tx(bar, bytes);
+      bulk_g2s(stg + i * BK * rc, A + (r / rc) * a.s1 + kb0 * a.t1, bytes, bar);
+      return;
+    }
+    mbar_arrive(bar);
+  } else {
+    const long long r = r0 + i;
+    if (r < M) {
+      const float* row = A + (r / a.rc) * a.s1 + (r % a.rc) * a.s2;
+      long long q = kb0 / a.kc, rem = kb0 - q * a.kc;
+      for (int k = 0; k < nk; ++k) {
+        cp4(stg + ((k >> 3) * LOADERS + i) * 8 + (k & 7), row + q * a.t1 + rem * a.t2);
+        if (++rem == a.kc) { rem = 0; ++q; }
+      }
+    }
+    cp_arrive(bar);
+  }
+}
+
+// Converts a filled slot into the bfloat16 stage (any thread may convert any value).
+__device__ __forceinline__ void convert_a(uint8_t* sa, const float* stg, int mode, int rc, long long M, long long K,
+                                          long long r0, int kb, int i) {
+  const long long kb0 = (long long)kb * BK;
+  const int nk = (int)(K - kb0 < BK ? K - kb0 : BK);
+  const int nch = nk >= BK ? 8 : 2 * ((nk + 15) / 16);  // chunks the MMAs read
+  if (mode == ROWRUN) {
+    for (int t = i; t < BM * nch; t += LOADERS) {  // (row, chunk), chunk fastest
+      const int row = t / nch, ch = t - (t / nch) * nch;
+      if (r0 + row >= M) continue;
+      const float* src = stg + row * BK + ch * 8;
+      float x[8];
+      if (ch * 8 + 8 <= nk) {
+        const float4 lo = *reinterpret_cast<const float4*>(src), hi = *reinterpret_cast<const float4*>(src + 4);
+        x[0] = lo.x; x[1] = lo.y; x[2] = lo.z; x[3] = lo.w; x[4] = hi.x; x[5] = hi.y; x[6] = hi.z; x[7] = hi.w;
+      } else {
+#pragma unroll
+        for (int e = 0; e < 8; ++e) x[e] = ch * 8 + e < nk ? src[e] : 0.f;
+      }
+      store_chunk(sa, row, ch, x);
+    }
+  } else if (mode == GROUPRUN) {
+    for (int t = i; t < BM * nch; t += LOADERS) {  // (row, chunk), row fastest
+      const int row = t & (BM - 1), ch = t >> 7;
+      if (r0 + row >= M) continue;
+      const float* src = stg + (row / rc) * (BK * rc) + (ch * 8) * rc + (row % rc);
+      float x[8];
+#pragma unroll
+      for (int e = 0; e < 8; ++e) x[e] = ch * 8 + e < nk ? src[e * rc] : 0.f;
+      store_chunk(sa, row, ch, x);
+    }
+  } else {
+    if (r0 + i >= M) return;
+    for (int ch = 0; ch < nch; ++ch) {
+      const float* src = stg + (ch * LOADERS + i) * 8;
+      float x[8];
+#pragma unroll
+      for (int e = 0; e < 8; ++e) x[e] = ch * 8 + e < nk ? src[e] : 0.f;
+      store_chunk(sa, i, ch, x);
+    }
+  }
+}
+}  // namespace ws
+
+template <int BN>
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t (&v)[16]) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, "
+      "%15}, [%16];"
+      : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]), "=r"(v[8]),
+        "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15])
+      : "r"(taddr)
+      : "memory");
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+}
+
+template <int BN>
+__global__ void __launch_bounds__(ws::THREADS, 1)
+    gemm_ws_kernel(const float* __restrict__ A, Addr aa, long long a_bs, long long K, const uint8_t* __restrict__ B,
+                   int kblocks, long long mtiles, int ntiles, long long items, Epi e, int* __restrict__ err) {
+  using C = ws::Cfg<BN>;
+  constexpr int ST = C::STAGES, D = C::DEPTH;
+  extern __shared__ __align__(1024) uint8_t smem_raw[];
+  uint8_t* smem = smem_raw + ((1024u - (smem_u32(smem_raw) & 1023u)) & 1023u);
+  float* const stg0 = reinterpret_cast<float*>(smem + ST * C::STAGE_BYTES);
+  float* const epi_buf = stg0 + D * ws::SLOT_FLOATS;
+  __shared__ uint64_t full[ST], bfull[ST], empty[ST], afull[D], accf[2], acce[2], drain;
+  __shared__ uint32_t tmem_base;
+  __shared__ long long off_s[ws::EPI_WARPS][32];  // epilogue: per warp, 32 row (or column) offsets
+  __shared__ float bias_s[ws::EPI_WARPS][32];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (warp == ws::MMA_WARP) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_base)),
+                 "r"(C::TMEM_COLS)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < ST; ++s) {
+      mbar_init(&full[s], ws::LOADERS);
+      mbar_init(&bfull[s], 1);
+      mbar_init(&empty[s], 1);
+    }
+    for (int d = 0; d < D; ++d) mbar_init(&afull[d], ws::LOADERS);
+    for (int b = 0; b < 2; ++b) {
+      mbar_init(&accf[b], 1);
+      mbar_init(&acce[b], 4);
+    }
+    mbar_init(&drain, 1);
+    fence_mbar_init();
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const uint32_t tmem = tmem_base;
+  const long long per_batch = mtiles * ntiles;
+
+  if (warp < 4) {  // operand loaders
+    const int i = threadIdx.x;
+    const int mode = ws::a_mode(A, aa, a_bs, e.M);
+    const long long mine = (long long)blockIdx.x < items ? (items - 1 - blockIdx.x) / gridDim.x + 1 : 0;
+    const long long total = mine * kblocks;  // stages of this CTA
+    auto stage_at = [&](long long g, long long& bt, long long& mt, int& nt, int& kb) {
+      const long long it = blockIdx.x + (g / kblocks) * gridDim.x;
+      kb = (int)(g % kblocks);
+      bt = it / per_batch;
+      const long long rem = it - bt * per_batch;
+      mt = rem / ntiles;
+      nt = (int)(rem - mt * ntiles);
+    };
+    auto issue = [&](long long g) {
+      long long bt, mt;
+      int nt, kb;
+      stage_at(g, bt, mt, nt, kb);
+      const int d = (int)(g % D);
+      ws::issue_a(stg0 + d * ws::SLOT_FLOATS, &afull[d], mode, A + bt * a_bs, aa, e.M, K, mt * BM, kb, i);
+    };
+    long long issued = 0;
+    for (; issued < D && issued < total; ++issued) issue(issued);
+    long long g = 0;
+    for (; g < total; ++g) {
+      const int s = (int)(g % ST), d = (int)(g % D);
+      bool ok = mbar_wait_bounded(&afull[d], (uint32_t)((g / D) & 1));
+      if (ok && g >= ST) ok = mbar_wait_bounded(&empty[s], (uint32_t)(((g / ST) - 1) & 1));
+      if (!ws::loaders_all(ok)) {
+        if (i == 0) atomicOr(err, 2);
+        break;
+      }
+      long long bt, mt;
+      int nt, kb;
+      stage_at(g, bt, mt, nt, kb);
+      uint8_t* st = smem + s * C::STAGE_BYTES;
+      if (i == 0) {
+        mbar_expect_tx(&bfull[s], C::B_BYTES);
+        bulk_g2s(st + A_BYTES, B + (((size_t)bt * ntiles + nt) * kblocks + kb) * C::B_BYTES, C::B_BYTES, &bfull[s]);
+      }
+      ws::convert_a(st, stg0 + d * ws::SLOT_FLOATS, mode, (int)aa.rc, e.M, K, mt * BM, kb, i);
+      fence_proxy_async();  // the tensor cores read the stage through the async proxy
+      mbar_arrive(&full[s]);
+      ws::loaders_sync();  // every loader is done with slot d
+      if (issued < total) issue(issued++);
+    }
+    // copies in flight land before the CTA's shared memory is released
+    for (long long j = g; j < issued; ++j) mbar_wait_bounded(&afull[j % D], (uint32_t)((j / D) & 1));
+    if (i == 0)
+      for (long long j = g > ST ? g - ST : 0; j < g; ++j) mbar_wait_bounded(&bfull[j % ST], (uint32_t)((j / ST) & 1));
+  } else if (warp == ws::MMA_WARP) {  // MMA issuer
+    if (lane == 0) {
+      long long g = 0, n = 0;
+      bool ok = true;
+      for (long long it = blockIdx.x; it < items && ok; it += gridDim.x, ++n) {
+        const int buf = (int)(n & 1);
+        if (n >= 2 && !mbar_wait_bounded(&acce[buf], (uint32_t)(((n >> 1) - 1) & 1))) {
+          atomicOr(err, 16);
+          break;
+        }
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        const uint32_t dacc = tmem + (uint32_t)(buf * BN);
+        for (int kb = 0; kb < kblocks; ++kb, ++g) {
+          const int s = (int)(g % ST);
+          const uint32_t par = (uint32_t)((g / ST) & 1);
+          if (!mbar_wait_bounded(&full[s], par) || !mbar_wait_bounded(&bfull[s], par)) {
+            atomicOr(err, 4);
+            ok = false;
+            break;
+          }
+          asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+          const uint32_t sa = smem_u32(smem + s * C::STAGE_BYTES);
+          const long long krem = K - (long long)kb * BK;
+          const int nk = krem >= BK ? BK / 16 : (int)((krem + 15) / 16);
+          for (int j = 0; j < nk; ++j) {
+            const uint32_t off = (uint32_t)j * 32u;
+            const uint32_t acc = (kb > 0 || j > 0) ? 1u : 0u;
+            asm volatile(
+                "{\n\t .reg .pred p;\n\t setp.ne.b32 p, %4, 0;\n\t"
+                "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(dacc),
+                "l"(sdesc(sa + off)), "l"(sdesc(sa + A_BYTES + off)), "r"(tg::Cfg<BN>::IDESC), "r"(acc)
+                : "memory");
+          }
+          asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                           smem_u32(&empty[s]))
+                       : "memory");
+        }
+        if (!ok) break;
+        asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                         smem_u32(&accf[buf]))
+                     : "memory");
+      }
+      // every MMA issued has completed before the tensor memory and the stages are released
+      asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                       smem_u32(&drain))
+                   : "memory");
+      if (!mbar_wait_bounded(&drain, 0)) atomicOr(err, 32);
+    }
+    __syncwarp();
+  } else {  // epilogue, warps 4-11: group eg takes this CTA's tiles n = eg, eg + 2, ... (accumulator eg)
+    const int w = warp - 4, eg = w >> 2, q = warp & 3;
+    float* const blk = epi_buf + w * (32 * 33);
+    const bool split_cols = e.out.kc != 1;
+    const bool stage_cols = !split_cols && e.out.t1 == 1;
+    const uint32_t lanes = (uint32_t)(q * 32) << 16;
+    for (long long it = blockIdx.x + (long long)eg * gridDim.x, n = eg; it < items; it += 2LL * gridDim.x, n += 2) {
+      const int buf = (int)(n & 1);
+      if (!mbar_wait_bounded(&accf[buf], (uint32_t)((n >> 1) & 1))) {
+        if (lane == 0) atomicOr(err, 8);
+        break;
+      }
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      const long long bt = it / per_batch, rem = it - bt * per_batch;
+      const long long mt = rem / ntiles;
+      const int nt = (int)(rem - mt * ntiles);
+      float* const ey = e.y + bt * e.ybs;
+      const float* const eadd = e.add ? e.add + bt * e.ybs : nullptr;
+      float* const eact = e.act ? e.act + bt * e.ybs : nullptr;
+      const float* const p1 = eadd ? eadd : ey;  // first addend (add, else the accumulated output)
+      const bool have_prev = eadd || e.accumulate, both = eadd && e.accumulate;
+      const long long r = mt * BM + q * 32 + lane;
+      const bool row_ok = r < e.M;
+      const long long rbase = row_ok ? (r / e.out.rc) * e.out.s1 + (r % e.out.rc) * e.out.s2 : -1;
+      // Offsets and biases of the warp's 32 rows or columns go through shared memory, and
+      // the loads of add / accumulate are unconditional (an invalid element reads word 0
+      // of its array), so 16 of them are in flight before the first is used.
+      for (int c0 = 0; c0 < BN && nt * BN + c0 < e.N; c0 += 32) {
+        const int c = nt * BN + c0 + lane;  // this lane's column
+        const bool col_ok = c < e.N;
+        const uint32_t taddr = tmem + lanes + (uint32_t)(buf * BN + c0);
+        if (stage_cols) {
+          // columns contiguous in the output: the warp's 32 x 32 block goes through shared
+          // memory and each row is stored with the lanes along its columns
+#pragma unroll
+          for (int h = 0; h < 2; ++h) {
+            uint32_t v[16];
+            tmem_ld16<BN>(taddr + (uint32_t)(h * 16), v);
+#pragma unroll
+            for (int j = 0; j < 16; ++j) blk[lane * 33 + h * 16 + j] = __uint_as_float(v[j]);
+          }
+          off_s[w][lane] = rbase;
+          __syncwarp();
+          const float bias_c = (e.bias && col_ok) ? __ldg(e.bias + c) : 0.f;
+#pragma unroll
+          for (int h = 0; h < 32; h += 16) {
+            float prev[16];
+            if (have_prev) {
+#pragma unroll
+              for (int j = 0; j < 16; ++j) {
+                const long long ro = off_s[w][h + j];
+                prev[j] = p1[(ro >= 0 && col_ok) ? ro + c : 0];
+              }
+              if (both) {
+#pragma unroll
+                for (int j = 0; j < 16; ++j) {
+                  const long long ro = off_s[w][h + j];
+                  prev[j] += ey[(ro >= 0 && col_ok) ? ro + c : 0];
+                }
+              }
+            }
+#pragma unroll
+            for (int j = 0; j < 16; ++j) {
+              const long long ro = off_s[w][h + j];
+              if (ro >= 0 && col_ok) {
+                float z = fmaf(blk[(h + j) * 33 + lane], e.scale, bias_c);
+                if (have_prev) z += prev[j];
+                ey[ro + c] = z;
+                if (eact) eact[ro + c] = gelu_t(z);
+              }
+            }
+          }
+          __syncwarp();
+        } else {
+          // lanes along rows; the column offsets (this lane's for column c0 + lane) in shared memory
+          off_s[w][lane] = col_ok ? (split_cols ? (long long)(c / e.out.kc) * e.out.t1 +
+                                                      (long long)(c % e.out.kc) * e.out.t2
+                                                : (long long)c * e.out.t1)
+                                  : -1;
+          bias_s[w][lane] = (e.bias && col_ok) ? __ldg(e.bias + c) : 0.f;
+          __syncwarp();
+#pragma unroll
+          for (int h = 0; h < 32; h += 16) {
+            uint32_t v[16];
+            tmem_ld16<BN>(taddr + (uint32_t)h, v);
+            float prev[16];
+            if (have_prev) {
+#pragma unroll
+              for (int j = 0; j < 16; ++j) {
+                const long long cj = off_s[w][h + j];
+                prev[j] = p1[(row_ok && cj >= 0) ? rbase + cj : 0];
+              }
+              if (both) {
+#pragma unroll
+                for (int j = 0; j < 16; ++j) {
+                  const long long cj = off_s[w][h + j];
+                  prev[j] += ey[(row_ok && cj >= 0) ? rbase + cj : 0];
+                }
+              }
+            }
+#pragma unroll
+            for (int j = 0; j < 16; ++j) {
+              const long long cj = off_s[w][h + j];
+              if (row_ok && cj >= 0) {
+                float z = fmaf(__uint_as_float(v[j]), e.scale, bias_s[w][h + j]);
+                if (have_prev) z += prev[j];
+                ey[rbase + cj] = z;
+                if (eact) eact[rbase + cj] = gelu_t(z);
+              }
+            }
+          }
+          __syncwarp();
+        }
+      }
+      asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&acce[buf]);
+    }
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  if (warp == ws::MMA_WARP)
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(C::TMEM_COLS) : "memory");
+}
+
+// Resident CTAs per SM of gemm_ws_kernel<BN> (shared memory, registers and the two
+// accumulators' tensor-memory columns), per device.
+template <int BN>
+cudaError_t ws_slots(int& slots) {
+  static std::atomic<int> cache[64];
+  int dev = 0;
+  cudaError_t c = cudaGetDevice(&dev);
+  if (c != cudaSuccess) return c;
+  const int d = dev & 63;
+  int v = cache[d].load(std::memory_order_acquire);
+  if (v <= 0) {
+    c = cudaFuncSetAttribute(gemm_ws_kernel<BN>, cudaFuncAttributeMaxDynamicSharedMemorySize, ws::Cfg<BN>::SMEM);
+    if (c != cudaSuccess) return c;
+    // all of the unified L1 as shared memory, so that two CTAs fit where their stages allow
+    c = cudaFuncSetAttribute(gemm_ws_kernel<BN>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                             (int)cudaSharedmemCarveoutMaxShared);
+    if (c != cudaSuccess) return c;
+    int occ = 0, sms = 0;
+    c = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, gemm_ws_kernel<BN>, ws::THREADS, ws::Cfg<BN>::SMEM);
+    if (c != cudaSuccess) return c;
+    c = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (c != cudaSuccess) return c;
+    occ = std::min(occ, (int)(512 / ws::Cfg<BN>::TMEM_COLS));
+    if (occ < 1) return cudaErrorInvalidConfiguration;
+    v = occ * sms;
+    cache[d].store(v, std::memory_order_release);
+  }
+  slots = v;
+  return cudaSuccess;
+}
+
+template <int BN>
+cudaError_t launch_ws_bn(const float* a, const Addr& aa, long long a_bs, long long K, const uint8_t* b, int kblocks,
+                         long long mtiles, int ntiles, long long batch, const Epi& e, int* err, cudaStream_t st) {
+  int slots = 0;
+  cudaError_t c = ws_slots<BN>(slots);
+  if (c != cudaSuccess) return c;
+  const long long items = batch * mtiles * ntiles;
+  const unsigned grid = (unsigned)std::min<long long>(items, slots);
+  gemm_ws_kernel<BN><<<grid, ws::THREADS, ws::Cfg<BN>::SMEM, st>>>(a, aa, a_bs, K, b, kblocks, mtiles, ntiles, items,
+                                                                   e, err);
+  return cudaGetLastError();
+}
+
 template <int BN>
 cudaError_t launch_gemm_bn(const uint8_t* a, const uint8_t* b, long long mtiles, int ntiles, int kblocks, int kper,
                            float* part, const Epi& e, int* err, cudaStream_t st, int batch = 1) {
@@ -383,16 +913,26 @@ int TcGemm::run(const float* a, Addr aa, const float* b, Addr ba, long long M, i
   }
   const long long a_rows = mtiles * tg::BM, b_rows = (long long)ntiles * bn;
   const long long a_thr = a_rows * kblocks * (tg::BK / 8), b_thr = b_rows * kblocks * (tg::BK / 8);
-  tg::pack_kernel<<<(unsigned)((a_thr + 255) / 256), 256, 0, st>>>(a, aa, M, K, tg::BM, a_rows, kblocks,
-                                                                   reinterpret_cast<uint4*>(a_img));
   tg::pack_kernel<<<(unsigned)((b_thr + 255) / 256), 256, 0, st>>>(b, ba, N, K, bn, b_rows, kblocks,
                                                                    reinterpret_cast<uint4*>(b_img));
   Epi e = epi;
   e.M = M;
   e.N = N;
-  const uint8_t* ai = reinterpret_cast<const uint8_t*>(a_img);
+  e.ybs = 0;
   const uint8_t* bi = reinterpret_cast<const uint8_t*>(b_img);
   cudaError_t c;
+  if (splits == 1) {  // persistent kernel, A rounded to bfloat16 as it is loaded
+    switch (bn) {
+      case 32: c = tg::launch_ws_bn<32>(a, aa, 0, K, bi, kblocks, mtiles, ntiles, 1, e, err, st); break;
+      case 64: c = tg::launch_ws_bn<64>(a, aa, 0, K, bi, kblocks, mtiles, ntiles, 1, e, err, st); break;
+      case 128: c = tg::launch_ws_bn<128>(a, aa, 0, K, bi, kblocks, mtiles, ntiles, 1, e, err, st); break;
+      default: c = tg::launch_ws_bn<256>(a, aa, 0, K, bi, kblocks, mtiles, ntiles, 1, e, err, st); break;
+    }
+    return c == cudaSuccess ? MSX_OK : MSX_ERR_CUDA;
+  }
+  tg::pack_kernel<<<(unsigned)((a_thr + 255) / 256), 256, 0, st>>>(a, aa, M, K, tg::BM, a_rows, kblocks,
+                                                                   reinterpret_cast<uint4*>(a_img));
+  const uint8_t* ai = reinterpret_cast<const uint8_t*>(a_img);
   switch (bn) {
     case 32: c = tg::launch_gemm_bn<32>(ai, bi, mtiles, ntiles, kblocks, kper, pbuf, e, err, st); break;
     case 64: c = tg::launch_gemm_bn<64>(ai, bi, mtiles, ntiles, kblocks, kper, pbuf, e, err, st); break;
@@ -411,28 +951,58 @@ int TcGemm::run_batched(const float* a, Addr aa, long long a_bs, const float* b,
   const long long kbl = (K + tg::BK - 1) / tg::BK;
   if (kbl > (1LL << 30) || mtiles * ntiles * batch > (1LL << 30)) return MSX_ERR_INVALID;
   const int kblocks = (int)kbl;
-  const size_t a_bytes = (size_t)batch * mtiles * kblocks * tg::A_BYTES;
   const size_t b_bytes = (size_t)batch * ntiles * kblocks * bn * tg::BK * 2;
-  int rc = reserve(a_bytes, b_bytes);
+  int rc = reserve(0, b_bytes);
   if (rc != MSX_OK) return rc;
-  const long long a_rows = mtiles * tg::BM, b_rows = (long long)ntiles * bn;
-  const long long a_thr = a_rows * kblocks * (tg::BK / 8) * batch, b_thr = b_rows * kblocks * (tg::BK / 8) * batch;
-  tg::pack_kernel<<<(unsigned)((a_thr + 255) / 256), 256, 0, st>>>(a, aa, M, K, tg::BM, a_rows, kblocks,
-                                                                   reinterpret_cast<uint4*>(a_img), batch, a_bs);
+  const long long b_rows = (long long)ntiles * bn;
+  const long long b_thr = b_rows * kblocks * (tg::BK / 8) * batch;
   tg::pack_kernel<<<(unsigned)((b_thr + 255) / 256), 256, 0, st>>>(b, ba, N, K, bn, b_rows, kblocks,
                                                                    reinterpret_cast<uint4*>(b_img), batch, b_bs);
   Epi e = epi;
   e.M = M;
   e.N = N;
   e.ybs = y_bs;
-  const uint8_t* ai = reinterpret_cast<const uint8_t*>(a_img);
   const uint8_t* bi = reinterpret_cast<const uint8_t*>(b_img);
   cudaError_t c;
   switch (bn) {
-    case 32: c = tg::launch_gemm_bn<32>(ai, bi, mtiles, ntiles, kblocks, kblocks, nullptr, e, err, st, batch); break;
-    case 64: c = tg::launch_gemm_bn<64>(ai, bi, mtiles, ntiles, kblocks, kblocks, nullptr, e, err, st, batch); break;
-    case 128: c = tg::launch_gemm_bn<128>(ai, bi, mtiles, ntiles, kblocks, kblocks, nullptr, e, err, st, batch); break;
-    default: c = tg::launch_gemm_bn<256>(ai, bi, mtiles, ntiles, kblocks, kblocks, nullptr, e, err, st, batch); break;
+    case 32: c = tg::launch_ws_bn<32>(a, aa, a_bs, K, bi, kblocks, mtiles, ntiles, batch, e, err, st); break;
+    case 64: c = tg::launch_ws_bn<64>(a, aa, a_bs, K, bi, kblocks, mtiles, ntiles, batch, e, err, st); break;
+    case 128: c = tg::launch_ws_bn<128>(a, aa, a_bs, K, bi, kblocks, mtiles, ntiles, batch, e, err, st); break;
+    default: c = tg::launch_ws_bn<256>(a, aa, a_bs, K, bi, kblocks, mtiles, ntiles, batch, e, err, st); break;
+  }
+  return c == cudaSuccess ? MSX_OK : MSX_ERR_CUDA;
+}
+
+int TcGemm::run_cplx(const float* a, Addr aa, long long a_bs, const float* src, long long si, long long sj,
+                     long long src_bs, int hn, int hk, int neg, long long M, const Epi& epi, long long y_bs, int batch,
+                     cudaStream_t st) {
+  if (batch < 1 || M <= 0 || hn <= 0 || hk <= 0 || 2 * hn > 4096 || neg < 0 || neg > 2) return MSX_ERR_INVALID;
+  const int N = 2 * hn;
+  const long long K = 2LL * hk;
+  const int bn = bn_for(N);
+  const long long mtiles = (M + tg::BM - 1) / tg::BM;
+  const int ntiles = (N + bn - 1) / bn;
+  const int kblocks = (int)((K + tg::BK - 1) / tg::BK);
+  if (mtiles * ntiles * batch > (1LL << 30)) return MSX_ERR_INVALID;
+  const size_t b_bytes = (size_t)batch * ntiles * kblocks * bn * tg::BK * 2;
+  int rc = reserve(0, b_bytes);
+  if (rc != MSX_OK) return rc;
+  const int b_rows = ntiles * bn;
+  const long long b_thr = (long long)b_rows * kblocks * (tg::BK / 8) * batch;
+  tg::pack_cplx_kernel<<<(unsigned)((b_thr + 255) / 256), 256, 0, st>>>(src, si, sj, src_bs, hn, hk, neg, bn, b_rows,
+                                                                        kblocks, reinterpret_cast<uint4*>(b_img),
+                                                                        batch);
+  Epi e = epi;
+  e.M = M;
+  e.N = N;
+  e.ybs = y_bs;
+  const uint8_t* bi = reinterpret_cast<const uint8_t*>(b_img);
+  cudaError_t c;
+  switch (bn) {
+    case 32: c = tg::launch_ws_bn<32>(a, aa, a_bs, K, bi, kblocks, mtiles, ntiles, batch, e, err, st); break;
+    case 64: c = tg::launch_ws_bn<64>(a, aa, a_bs, K, bi, kblocks, mtiles, ntiles, batch, e, err, st); break;
+    case 128: c = tg::launch_ws_bn<128>(a, aa, a_bs, K, bi, kblocks, mtiles, ntiles, batch, e, err, st); break;
+    default: c = tg::launch_ws_bn<256>(a, aa, a_bs, K, bi, kblocks, mtiles, ntiles, batch, e, err, st); break;
   }
   return c == cudaSuccess ? MSX_OK : MSX_ERR_CUDA;
 }
