@@ -364,8 +364,11 @@ struct Cfg {
   static constexpr int DEPTH = BN <= 64 ? 3 : 2;    // FP32 staging slots: A stages in flight
   static constexpr int B_BYTES = BN * BK * 2;
   static constexpr int STAGE_BYTES = A_BYTES + B_BYTES;
+  static constexpr int BROWS = BN;                          // rows of a B tile
+  static constexpr int BSLOT_FLOATS = BN == 32 ? 32 * BK : 0;  // FP32 B staging slot (B from FP32: BN = 32)
   static constexpr int EPI_FLOATS = EPI_WARPS * 32 * 33;
-  static constexpr int SMEM = STAGES * STAGE_BYTES + DEPTH * SLOT_FLOATS * 4 + EPI_FLOATS * 4 + 1024;
+  static constexpr int SMEM =
+      STAGES * STAGE_BYTES + DEPTH * (SLOT_FLOATS + BSLOT_FLOATS) * 4 + EPI_FLOATS * 4 + 1024;
   static constexpr uint32_t TMEM_COLS = 2 * BN;
 };
 
@@ -395,79 +398,129 @@ __device__ __forceinline__ void store_chunk(uint8_t* sa, int row, int ch, const 
   *reinterpret_cast<uint4*>(sa + sw128(row, ch * 8)) = *reinterpret_cast<const uint4*>(h);
 }
 
-// How a stage of A (rows r0 .. r0 + 127, K block kb, nk = min(64, K - 64 kb) values)
-// reaches its staging slot:
-//   ROWRUN   k contiguous: thread i copies row r0 + i (nk values) to slot[i][0 .. nk)
-//            with one bulk copy (16-byte aligned runs), else with plain loads;
+// How the rows r0 .. r0 + R - 1 of an operand (R = 128 for A, BN for B), K block kb
+// (nk = min(64, K - 64 kb) values), reach a staging slot:
+//   ROWRUN   k contiguous: thread i copies row r0 + i to slot[i][0 .. nk) with one bulk
+//            copy (16-byte aligned runs), else with plain loads;
 //   GROUPRUN rows contiguous in groups of rc with k stride rc (a group's K block is one
-//            run of nk * rc values): thread i < 128 / rc copies group i to
-//            slot[i * 64 rc ..], element (k, r mod rc) at k rc + r mod rc;
+//            run of nk * rc values; rc may be all the operand's rows): thread i < R / rc
+//            copies group i to slot[i * 64 rc ..], element (k, r mod rc) at k rc + r mod rc;
 //   GENERIC  thread i copies row r0 + i value by value (4-byte asynchronous copies),
-//            element (r, k) at ((k / 8) 128 + i) 8 + k mod 8.
-enum { ROWRUN = 0, GROUPRUN = 1, GENERIC = 2 };
+//            element (r, k) at ((k / 8) R + i) 8 + k mod 8;
+//   TILERUN  rows of K <= 64 values stored back to back: thread 0 copies the tile's rows
+//            as one run (or the loaders load it, when the run is not 16-byte aligned),
+//            element (r, k) at r K + k.
+// Bulk bytes are announced on the slot's barrier without arriving; each loader thread
+// arrives once per slot after its copies of A and B are issued (through the async-copy
+// unit when it issued 4-byte copies, so the arrival waits for them).
+enum { ROWRUN = 0, GROUPRUN = 1, GENERIC = 2, TILERUN = 3 };
 
-__device__ __forceinline__ int a_mode(const float* A, const Addr& a, long long a_bs, long long M) {
-  if (a.kc == 1 && a.t1 == 1) return ROWRUN;
-  if (a.s2 == 1 && a.kc == 1 && a.t1 == a.rc && a.rc % 4 == 0 && BM % a.rc == 0 && M % a.rc == 0 && a.s1 % 4 == 0 &&
-      a_bs % 4 == 0 && (reinterpret_cast<uintptr_t>(A) & 15u) == 0)
-    return GROUPRUN;
-  return GENERIC;
+__device__ __forceinline__ void expect_tx_only(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.expect_tx.relaxed.cta.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
 }
 
-// Thread i's part of filling one slot; every loader thread arrives once on `bar`.
-__device__ __forceinline__ void issue_a(float* stg, uint64_t* bar, int mode, const float* __restrict__ A,
-                                        const Addr& a, long long M, long long K, long long r0, int kb, int i) {
-  const long long kb0 = (long long)kb * BK;
-  const int nk = (int)(K - kb0 < BK ? K - kb0 : BK);
-  if (mode == ROWRUN) {
-    const long long r = r0 + i;
-    if (r < M) {
-      const float* src = A + (r / a.rc) * a.s1 + (r % a.rc) * a.s2 + kb0;
-      if ((nk & 3) == 0 && (reinterpret_cast<uintptr_t>(src) & 15u) == 0) {
-        mbar_expect_tx(bar, (uint32_t)nk * 4u);
-        bulk_g2s(stg + i * BK, src, (uint32_t)nk * 4u, bar);
-        return;
-      }
-      for (int k = 0; k < nk; ++k) stg[i * BK + k] = __ldg(src + k);
-    }
-    mbar_arrive(bar);
-  } else if (mode == GROUPRUN) {
-    const int rc = (int)a.rc;
-    const long long r = r0 + (long long)i * rc;
-    if (i < BM / rc && r < M) {
-      const uint32_t bytes = (uint32_t)nk * (uint32_t)rc * 4u;
-      mbar_expect_tx(bar, bytes);
-      bulk_g2s(stg + i * BK * rc, A + (r / rc) * a.s1 + kb0 * a.t1, bytes, bar);
-      return;
-    }
-    mbar_arrive(bar);
-  } else {
-    const long long r = r0 + i;
-    if (r < M) {
-      const float* row = A + (r / a.rc) * a.s1 + (r % a.rc) * a.s2;
-      long long q = kb0 / a.kc, rem = kb0 - q * a.kc;
-      for (int k = 0; k < nk; ++k) {
-        cp4(stg + ((k >> 3) * LOADERS + i) * 8 + (k & 7), row + q * a.t1 + rem * a.t2);
-        if (++rem == a.kc) { rem = 0; ++q; }
-      }
-    }
-    cp_arrive(bar);
+struct Op {
+  const float* p;  // FP32 operand (batch 0)
+  Addr a;
+  long long bs;    // batch stride (floats)
+  long long rows;  // M or N
+  int mode, rc;
+};
+
+__host__ __device__ inline void op_mode(Op& o, int tile_rows, long long k_total) {
+  const Addr& a = o.a;
+  o.rc = (int)a.rc;
+  o.mode = GENERIC;
+  if (a.kc == 1 && a.t1 == 1) {
+    o.mode = ROWRUN;
+    if (a.rc == 1 && k_total <= BK && a.s1 == k_total) o.mode = TILERUN;
+    return;
+  }
+  long long g = -1;
+  if (a.s2 == 1 && a.rc > 1) g = a.rc;
+  else if (a.rc == 1 && a.s1 == 1) g = o.rows;  // all rows contiguous
+  if (g > 0 && g <= tile_rows && a.kc == 1 && a.t1 == g && g % 4 == 0 && tile_rows % g == 0 && o.rows % g == 0 &&
+      (g == o.rows || a.s1 % 4 == 0) && o.bs % 4 == 0 && (reinterpret_cast<uintptr_t>(o.p) & 15u) == 0) {
+    o.mode = GROUPRUN;
+    o.rc = (int)g;
   }
 }
 
-// Converts a filled slot into the bfloat16 stage (any thread may convert any value).
-__device__ __forceinline__ void convert_a(uint8_t* sa, const float* stg, int mode, int rc, long long M, long long K,
-                                          long long r0, int kb, int i) {
+// Thread i's copies of rows r0 .. r0 + R - 1 of operand o (batch bt) into slot stg;
+// returns true when it issued 4-byte asynchronous copies.
+template <int R>
+__device__ __forceinline__ bool issue_op(float* stg, uint64_t* bar, const Op& o, long long bt, long long K,
+                                         long long r0, int kb, int i) {
+  const long long kb0 = (long long)kb * BK;
+  const int nk = (int)(K - kb0 < BK ? K - kb0 : BK);
+  const float* const P = o.p + bt * o.bs;
+  const Addr& a = o.a;
+  if (o.mode == TILERUN) {
+    const long long nrow = o.rows - r0 < R ? o.rows - r0 : R;
+    const float* src = P + r0 * a.s1;
+    const int n = (int)(nrow * nk);
+    if (nrow > 0 && (n & 3) == 0 && (reinterpret_cast<uintptr_t>(src) & 15u) == 0) {
+      if (i == 0) {
+        expect_tx_only(bar, (uint32_t)n * 4u);
+        bulk_g2s(stg, src, (uint32_t)n * 4u, bar);
+      }
+    } else {
+      for (int j = i; j < n; j += LOADERS) stg[j] = __ldg(src + j);
+    }
+    return false;
+  }
+  if (i >= R && o.mode != GROUPRUN) return false;
+  if (o.mode == ROWRUN) {
+    const long long r = r0 + i;
+    if (r < o.rows) {
+      const float* src = P + (r / a.rc) * a.s1 + (r % a.rc) * a.s2 + kb0;
+      if ((nk & 3) == 0 && (reinterpret_cast<uintptr_t>(src) & 15u) == 0) {
+        expect_tx_only(bar, (uint32_t)nk * 4u);
+        bulk_g2s(stg + i * BK, src, (uint32_t)nk * 4u, bar);
+      } else {
+        for (int k = 0; k < nk; ++k) stg[i * BK + k] = __ldg(src + k);
+      }
+    }
+    return false;
+  }
+  if (o.mode == GROUPRUN) {
+    const int rc = o.rc;
+    const long long r = r0 + (long long)i * rc;
+    if (i < R / rc && r < o.rows) {
+      const uint32_t bytes = (uint32_t)nk * (uint32_t)rc * 4u;
+      expect_tx_only(bar, bytes);
+      bulk_g2s(stg + i * BK * rc, P + (r / a.rc) * a.s1 + kb0 * a.t1, bytes, bar);
+    }
+    return false;
+  }
+  const long long r = r0 + i;
+  if (r >= o.rows) return false;
+  const float* row = P + (r / a.rc) * a.s1 + (r % a.rc) * a.s2;
+  long long q = kb0 / a.kc, rem = kb0 - q * a.kc;
+  for (int k = 0; k < nk; ++k) {
+    cp4(stg + ((k >> 3) * R + i) * 8 + (k & 7), row + q * a.t1 + rem * a.t2);
+    if (++rem == a.kc) { rem = 0; ++q; }
+  }
+  return nk > 0;
+}
+
+// Converts the rows r0 .. r0 + R - 1 of a filled slot into the bfloat16 operand image at
+// sa (R rows of 128 bytes, swizzled); any loader thread may convert any value.
+template <int R>
+__device__ __forceinline__ void convert_op(uint8_t* sa, const float* stg, const Op& o, long long K, long long r0,
+                                           int kb, int i) {
   const long long kb0 = (long long)kb * BK;
   const int nk = (int)(K - kb0 < BK ? K - kb0 : BK);
   const int nch = nk >= BK ? 8 : 2 * ((nk + 15) / 16);  // chunks the MMAs read
-  if (mode == ROWRUN) {
-    for (int t = i; t < BM * nch; t += LOADERS) {  // (row, chunk), chunk fastest
+  const int nrow = (int)(o.rows - r0 < R ? o.rows - r0 : R);  // rows to convert
+  if (nrow <= 0) return;
+  if (o.mode == ROWRUN || o.mode == TILERUN) {
+    const int ld = o.mode == ROWRUN ? BK : nk;
+    for (int t = i; t < nrow * nch; t += LOADERS) {  // (row, chunk), chunk fastest
       const int row = t / nch, ch = t - (t / nch) * nch;
-      if (r0 + row >= M) continue;
-      const float* src = stg + row * BK + ch * 8;
+      const float* src = stg + row * ld + ch * 8;
       float x[8];
-      if (ch * 8 + 8 <= nk) {
+      if (ch * 8 + 8 <= nk && o.mode == ROWRUN) {
         const float4 lo = *reinterpret_cast<const float4*>(src), hi = *reinterpret_cast<const float4*>(src + 4);
         x[0] = lo.x; x[1] = lo.y; x[2] = lo.z; x[3] = lo.w; x[4] = hi.x; x[5] = hi.y; x[6] = hi.z; x[7] = hi.w;
       } else {
@@ -476,10 +529,10 @@ __device__ __forceinline__ void convert_a(uint8_t* sa, const float* stg, int mod
       }
       store_chunk(sa, row, ch, x);
     }
-  } else if (mode == GROUPRUN) {
-    for (int t = i; t < BM * nch; t += LOADERS) {  // (row, chunk), row fastest
-      const int row = t & (BM - 1), ch = t >> 7;
-      if (r0 + row >= M) continue;
+  } else if (o.mode == GROUPRUN) {
+    const int rc = o.rc;
+    for (int t = i; t < nrow * nch; t += LOADERS) {  // (row, chunk), row fastest
+      const int ch = t / nrow, row = t - ch * nrow;
       const float* src = stg + (row / rc) * (BK * rc) + (ch * 8) * rc + (row % rc);
       float x[8];
 #pragma unroll
@@ -487,13 +540,13 @@ __device__ __forceinline__ void convert_a(uint8_t* sa, const float* stg, int mod
       store_chunk(sa, row, ch, x);
     }
   } else {
-    if (r0 + i >= M) return;
-    for (int ch = 0; ch < nch; ++ch) {
-      const float* src = stg + (ch * LOADERS + i) * 8;
+    for (int t = i; t < nrow * nch; t += LOADERS) {  // (row, chunk), row fastest
+      const int ch = t / nrow, row = t - ch * nrow;
+      const float* src = stg + (ch * R + row) * 8;
       float x[8];
 #pragma unroll
       for (int e = 0; e < 8; ++e) x[e] = ch * 8 + e < nk ? src[e] : 0.f;
-      store_chunk(sa, i, ch, x);
+      store_chunk(sa, row, ch, x);
     }
   }
 }
@@ -511,21 +564,39 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t (&v)[16]) {
   asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 }
 
+// The work of one launch.  Items (batch, split, mt, nt), nt fastest; item `split` sums K
+// blocks [split * kper, min(kblocks, (split + 1) * kper)).  B comes either packed
+// (b_img, one image per batch) or, for BN = 32, as an FP32 operand (b.p) staged and
+// rounded like A.  With part set the epilogue writes raw partial tiles
+// part[((batch * splits + split) * tiles + tile) * 128 * BN + row * BN + col] instead.
+struct WsArgs {
+  ws::Op a, b;
+  const uint8_t* b_img;
+  long long K;
+  int kblocks, kper, splits, ntiles;
+  long long mtiles, items;
+  float* part;
+};
+
 template <int BN>
-__global__ void __launch_bounds__(ws::THREADS, 1)
-    gemm_ws_kernel(const float* __restrict__ A, Addr aa, long long a_bs, long long K, const uint8_t* __restrict__ B,
-                   int kblocks, long long mtiles, int ntiles, long long items, Epi e, int* __restrict__ err) {
+__global__ void __launch_bounds__(ws::THREADS, 1) gemm_ws_kernel(WsArgs w, Epi e, int* __restrict__ err) {
   using C = ws::Cfg<BN>;
   constexpr int ST = C::STAGES, D = C::DEPTH;
   extern __shared__ __align__(1024) uint8_t smem_raw[];
   uint8_t* smem = smem_raw + ((1024u - (smem_u32(smem_raw) & 1023u)) & 1023u);
   float* const stg0 = reinterpret_cast<float*>(smem + ST * C::STAGE_BYTES);
-  float* const epi_buf = stg0 + D * ws::SLOT_FLOATS;
+  float* const stgb = stg0 + D * ws::SLOT_FLOATS;  // B staging (BN = 32 only)
+  float* const epi_buf = stgb + D * C::BSLOT_FLOATS;
   __shared__ uint64_t full[ST], bfull[ST], empty[ST], afull[D], accf[2], acce[2], drain;
   __shared__ uint32_t tmem_base;
   __shared__ long long off_s[ws::EPI_WARPS][32];  // epilogue: per warp, 32 row (or column) offsets
   __shared__ float bias_s[ws::EPI_WARPS][32];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const bool fuse_b = w.b_img == nullptr;
+  if (fuse_b && C::BSLOT_FLOATS == 0) {  // host error: FP32 B needs BN = 32
+    if (threadIdx.x == 0) atomicOr(err, 64);
+    return;
+  }
   if (warp == ws::MMA_WARP) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_base)),
                  "r"(C::TMEM_COLS)
@@ -550,32 +621,49 @@ __global__ void __launch_bounds__(ws::THREADS, 1)
   __syncthreads();
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   const uint32_t tmem = tmem_base;
-  const long long per_batch = mtiles * ntiles;
+  const long long tiles = w.mtiles * w.ntiles;
+  // item -> (batch, split, mt, nt) and its K blocks
+  auto decode = [&](long long it, long long& bt, int& split, long long& mt, int& nt, int& kb0, int& kb1) {
+    nt = (int)(it % w.ntiles);
+    const long long t2 = it / w.ntiles;
+    mt = t2 % w.mtiles;
+    const long long t3 = t2 / w.mtiles;
+    split = (int)(t3 % w.splits);
+    bt = t3 / w.splits;
+    kb0 = split * w.kper;
+    kb1 = kb0 + w.kper < w.kblocks ? kb0 + w.kper : w.kblocks;
+  };
 
   if (warp < 4) {  // operand loaders
     const int i = threadIdx.x;
-    const int mode = ws::a_mode(A, aa, a_bs, e.M);
-    const long long mine = (long long)blockIdx.x < items ? (items - 1 - blockIdx.x) / gridDim.x + 1 : 0;
-    const long long total = mine * kblocks;  // stages of this CTA
-    auto stage_at = [&](long long g, long long& bt, long long& mt, int& nt, int& kb) {
-      const long long it = blockIdx.x + (g / kblocks) * gridDim.x;
-      kb = (int)(g % kblocks);
-      bt = it / per_batch;
-      const long long rem = it - bt * per_batch;
-      mt = rem / ntiles;
-      nt = (int)(rem - mt * ntiles);
+    // stages of this CTA in order: a cursor over (item, K block)
+    struct Cur {
+      long long it, bt, mt;
+      int nt, split, kb, kb1;
     };
-    auto issue = [&](long long g) {
-      long long bt, mt;
-      int nt, kb;
-      stage_at(g, bt, mt, nt, kb);
+    auto start = [&](Cur& c, long long it) {
+      c.it = it;
+      if (it < w.items) decode(it, c.bt, c.split, c.mt, c.nt, c.kb, c.kb1);
+    };
+    auto advance = [&](Cur& c) {
+      if (++c.kb >= c.kb1) start(c, c.it + gridDim.x);
+    };
+    auto issue = [&](const Cur& c, long long g) {
       const int d = (int)(g % D);
-      ws::issue_a(stg0 + d * ws::SLOT_FLOATS, &afull[d], mode, A + bt * a_bs, aa, e.M, K, mt * BM, kb, i);
+      bool cp = ws::issue_op<BM>(stg0 + d * ws::SLOT_FLOATS, &afull[d], w.a, c.bt, w.K, c.mt * BM, c.kb, i);
+      if (fuse_b)
+        cp |= ws::issue_op<C::BROWS>(stgb + d * C::BSLOT_FLOATS, &afull[d], w.b, c.bt, w.K, (long long)c.nt * BN,
+                                     c.kb, i);
+      if (cp) ws::cp_arrive(&afull[d]);
+      else mbar_arrive(&afull[d]);
     };
+    Cur cur, ahead;
+    start(cur, blockIdx.x);
+    start(ahead, blockIdx.x);
     long long issued = 0;
-    for (; issued < D && issued < total; ++issued) issue(issued);
+    for (; issued < D && ahead.it < w.items; ++issued, advance(ahead)) issue(ahead, issued);
     long long g = 0;
-    for (; g < total; ++g) {
+    for (; cur.it < w.items; ++g, advance(cur)) {
       const int s = (int)(g % ST), d = (int)(g % D);
       bool ok = mbar_wait_bounded(&afull[d], (uint32_t)((g / D) & 1));
       if (ok && g >= ST) ok = mbar_wait_bounded(&empty[s], (uint32_t)(((g / ST) - 1) & 1));
@@ -583,29 +671,37 @@ __global__ void __launch_bounds__(ws::THREADS, 1)
         if (i == 0) atomicOr(err, 2);
         break;
       }
-      long long bt, mt;
-      int nt, kb;
-      stage_at(g, bt, mt, nt, kb);
       uint8_t* st = smem + s * C::STAGE_BYTES;
-      if (i == 0) {
+      if (fuse_b) {
+        ws::convert_op<C::BROWS>(st + A_BYTES, stgb + d * C::BSLOT_FLOATS, w.b, w.K, (long long)cur.nt * BN, cur.kb,
+                                 i);
+      } else if (i == 0) {
         mbar_expect_tx(&bfull[s], C::B_BYTES);
-        bulk_g2s(st + A_BYTES, B + (((size_t)bt * ntiles + nt) * kblocks + kb) * C::B_BYTES, C::B_BYTES, &bfull[s]);
+        bulk_g2s(st + A_BYTES, w.b_img + (((size_t)cur.bt * w.ntiles + cur.nt) * w.kblocks + cur.kb) * C::B_BYTES,
+                 C::B_BYTES, &bfull[s]);
       }
-      ws::convert_a(st, stg0 + d * ws::SLOT_FLOATS, mode, (int)aa.rc, e.M, K, mt * BM, kb, i);
+      ws::convert_op<BM>(st, stg0 + d * ws::SLOT_FLOATS, w.a, w.K, cur.mt * BM, cur.kb, i);
       fence_proxy_async();  // the tensor cores read the stage through the async proxy
       mbar_arrive(&full[s]);
+      if (fuse_b && i == 0) mbar_arrive(&bfull[s]);
       ws::loaders_sync();  // every loader is done with slot d
-      if (issued < total) issue(issued++);
+      if (ahead.it < w.items) {
+        issue(ahead, issued++);
+        advance(ahead);
+      }
     }
     // copies in flight land before the CTA's shared memory is released
     for (long long j = g; j < issued; ++j) mbar_wait_bounded(&afull[j % D], (uint32_t)((j / D) & 1));
-    if (i == 0)
+    if (i == 0 && !fuse_b)
       for (long long j = g > ST ? g - ST : 0; j < g; ++j) mbar_wait_bounded(&bfull[j % ST], (uint32_t)((j / ST) & 1));
   } else if (warp == ws::MMA_WARP) {  // MMA issuer
     if (lane == 0) {
       long long g = 0, n = 0;
       bool ok = true;
-      for (long long it = blockIdx.x; it < items && ok; it += gridDim.x, ++n) {
+      for (long long it = blockIdx.x; it < w.items && ok; it += gridDim.x, ++n) {
+        long long bt, mt;
+        int split, nt, kb0, kb1;
+        decode(it, bt, split, mt, nt, kb0, kb1);
         const int buf = (int)(n & 1);
         if (n >= 2 && !mbar_wait_bounded(&acce[buf], (uint32_t)(((n >> 1) - 1) & 1))) {
           atomicOr(err, 16);
@@ -613,7 +709,7 @@ __global__ void __launch_bounds__(ws::THREADS, 1)
         }
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
         const uint32_t dacc = tmem + (uint32_t)(buf * BN);
-        for (int kb = 0; kb < kblocks; ++kb, ++g) {
+        for (int kb = kb0; kb < kb1; ++kb, ++g) {
           const int s = (int)(g % ST);
           const uint32_t par = (uint32_t)((g / ST) & 1);
           if (!mbar_wait_bounded(&full[s], par) || !mbar_wait_bounded(&bfull[s], par)) {
@@ -623,11 +719,11 @@ __global__ void __launch_bounds__(ws::THREADS, 1)
           }
           asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
           const uint32_t sa = smem_u32(smem + s * C::STAGE_BYTES);
-          const long long krem = K - (long long)kb * BK;
+          const long long krem = w.K - (long long)kb * BK;
           const int nk = krem >= BK ? BK / 16 : (int)((krem + 15) / 16);
           for (int j = 0; j < nk; ++j) {
             const uint32_t off = (uint32_t)j * 32u;
-            const uint32_t acc = (kb > 0 || j > 0) ? 1u : 0u;
+            const uint32_t acc = (kb > kb0 || j > 0) ? 1u : 0u;
             asm volatile(
                 "{\n\t .reg .pred p;\n\t setp.ne.b32 p, %4, 0;\n\t"
                 "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(dacc),
@@ -651,28 +747,48 @@ __global__ void __launch_bounds__(ws::THREADS, 1)
     }
     __syncwarp();
   } else {  // epilogue, warps 4-11: group eg takes this CTA's tiles n = eg, eg + 2, ... (accumulator eg)
-    const int w = warp - 4, eg = w >> 2, q = warp & 3;
-    float* const blk = epi_buf + w * (32 * 33);
+    const int wi = warp - 4, eg = wi >> 2, q = warp & 3;
+    float* const blk = epi_buf + wi * (32 * 33);
     const bool split_cols = e.out.kc != 1;
     const bool stage_cols = !split_cols && e.out.t1 == 1;
     const uint32_t lanes = (uint32_t)(q * 32) << 16;
-    for (long long it = blockIdx.x + (long long)eg * gridDim.x, n = eg; it < items; it += 2LL * gridDim.x, n += 2) {
+    for (long long it = blockIdx.x + (long long)eg * gridDim.x, n = eg; it < w.items;
+         it += 2LL * gridDim.x, n += 2) {
       const int buf = (int)(n & 1);
       if (!mbar_wait_bounded(&accf[buf], (uint32_t)((n >> 1) & 1))) {
         if (lane == 0) atomicOr(err, 8);
         break;
       }
       asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-      const long long bt = it / per_batch, rem = it - bt * per_batch;
-      const long long mt = rem / ntiles;
-      const int nt = (int)(rem - mt * ntiles);
+      long long bt, mt;
+      int split, nt, kb0, kb1;
+      decode(it, bt, split, mt, nt, kb0, kb1);
+      const long long r = mt * BM + q * 32 + lane;
+      const bool row_ok = r < e.M;
+      if (w.part) {  // raw partial tile: each lane stores its row's BN values
+        float* pp = w.part + ((bt * w.splits + split) * tiles + mt * w.ntiles + nt) * (long long)(BM * BN) +
+                    (long long)(q * 32 + lane) * BN;
+        for (int c0 = 0; c0 < BN; c0 += 16) {
+          uint32_t v[16];
+          tmem_ld16<BN>(tmem + lanes + (uint32_t)(buf * BN + c0), v);
+          if (row_ok) {
+#pragma unroll
+            for (int j = 0; j < 16; j += 4)
+              *reinterpret_cast<float4*>(pp + c0 + j) = make_float4(__uint_as_float(v[j]), __uint_as_float(v[j + 1]),
+                                                                    __uint_as_float(v[j + 2]),
+                                                                    __uint_as_float(v[j + 3]));
+          }
+        }
+        asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+        __syncwarp();
+        if (lane == 0) mbar_arrive(&acce[buf]);
+        continue;
+      }
       float* const ey = e.y + bt * e.ybs;
       const float* const eadd = e.add ? e.add + bt * e.ybs : nullptr;
       float* const eact = e.act ? e.act + bt * e.ybs : nullptr;
       const float* const p1 = eadd ? eadd : ey;  // first addend (add, else the accumulated output)
       const bool have_prev = eadd || e.accumulate, both = eadd && e.accumulate;
-      const long long r = mt * BM + q * 32 + lane;
-      const bool row_ok = r < e.M;
       const long long rbase = row_ok ? (r / e.out.rc) * e.out.s1 + (r % e.out.rc) * e.out.s2 : -1;
       // Offsets and biases of the warp's 32 rows or columns go through shared memory, and
       // the loads of add / accumulate are unconditional (an invalid element reads word 0
@@ -691,7 +807,7 @@ __global__ void __launch_bounds__(ws::THREADS, 1)
 #pragma unroll
             for (int j = 0; j < 16; ++j) blk[lane * 33 + h * 16 + j] = __uint_as_float(v[j]);
           }
-          off_s[w][lane] = rbase;
+          off_s[wi][lane] = rbase;
           __syncwarp();
           const float bias_c = (e.bias && col_ok) ? __ldg(e.bias + c) : 0.f;
 #pragma unroll
@@ -700,20 +816,20 @@ __global__ void __launch_bounds__(ws::THREADS, 1)
             if (have_prev) {
 #pragma unroll
               for (int j = 0; j < 16; ++j) {
-                const long long ro = off_s[w][h + j];
+                const long long ro = off_s[wi][h + j];
                 prev[j] = p1[(ro >= 0 && col_ok) ? ro + c : 0];
               }
               if (both) {
 #pragma unroll
                 for (int j = 0; j < 16; ++j) {
-                  const long long ro = off_s[w][h + j];
+                  const long long ro = off_s[wi][h + j];
                   prev[j] += ey[(ro >= 0 && col_ok) ? ro + c : 0];
                 }
               }
             }
 #pragma unroll
             for (int j = 0; j < 16; ++j) {
-              const long long ro = off_s[w][h + j];
+              const long long ro = off_s[wi][h + j];
               if (ro >= 0 && col_ok) {
                 float z = fmaf(blk[(h + j) * 33 + lane], e.scale, bias_c);
                 if (have_prev) z += prev[j];
@@ -725,11 +841,11 @@ __global__ void __launch_bounds__(ws::THREADS, 1)
           __syncwarp();
         } else {
           // lanes along rows; the column offsets (this lane's for column c0 + lane) in shared memory
-          off_s[w][lane] = col_ok ? (split_cols ? (long long)(c / e.out.kc) * e.out.t1 +
-                                                      (long long)(c % e.out.kc) * e.out.t2
-                                                : (long long)c * e.out.t1)
-                                  : -1;
-          bias_s[w][lane] = (e.bias && col_ok) ? __ldg(e.bias + c) : 0.f;
+          off_s[wi][lane] = col_ok ? (split_cols ? (long long)(c / e.out.kc) * e.out.t1 +
+                                                       (long long)(c % e.out.kc) * e.out.t2
+                                                 : (long long)c * e.out.t1)
+                                   : -1;
+          bias_s[wi][lane] = (e.bias && col_ok) ? __ldg(e.bias + c) : 0.f;
           __syncwarp();
 #pragma unroll
           for (int h = 0; h < 32; h += 16) {
@@ -739,22 +855,22 @@ __global__ void __launch_bounds__(ws::THREADS, 1)
             if (have_prev) {
 #pragma unroll
               for (int j = 0; j < 16; ++j) {
-                const long long cj = off_s[w][h + j];
+                const long long cj = off_s[wi][h + j];
                 prev[j] = p1[(row_ok && cj >= 0) ? rbase + cj : 0];
               }
               if (both) {
 #pragma unroll
                 for (int j = 0; j < 16; ++j) {
-                  const long long cj = off_s[w][h + j];
+                  const long long cj = off_s[wi][h + j];
                   prev[j] += ey[(row_ok && cj >= 0) ? rbase + cj : 0];
                 }
               }
             }
 #pragma unroll
             for (int j = 0; j < 16; ++j) {
-              const long long cj = off_s[w][h + j];
+              const long long cj = off_s[wi][h + j];
               if (row_ok && cj >= 0) {
-                float z = fmaf(__uint_as_float(v[j]), e.scale, bias_s[w][h + j]);
+                float z = fmaf(__uint_as_float(v[j]), e.scale, bias_s[wi][h + j]);
                 if (have_prev) z += prev[j];
                 ey[rbase + cj] = z;
                 if (eact) eact[rbase + cj] = gelu_t(z);
@@ -789,7 +905,7 @@ cudaError_t ws_slots(int& slots) {
   if (v <= 0) {
     c = cudaFuncSetAttribute(gemm_ws_kernel<BN>, cudaFuncAttributeMaxDynamicSharedMemorySize, ws::Cfg<BN>::SMEM);
     if (c != cudaSuccess) return c;
-    // all of the unified L1 as shared memory, so that two CTAs fit where their stages allow
+    // all of the unified L1 as shared memory
     c = cudaFuncSetAttribute(gemm_ws_kernel<BN>, cudaFuncAttributePreferredSharedMemoryCarveout,
                              (int)cudaSharedmemCarveoutMaxShared);
     if (c != cudaSuccess) return c;
@@ -808,16 +924,32 @@ cudaError_t ws_slots(int& slots) {
 }
 
 template <int BN>
-cudaError_t launch_ws_bn(const float* a, const Addr& aa, long long a_bs, long long K, const uint8_t* b, int kblocks,
-                         long long mtiles, int ntiles, long long batch, const Epi& e, int* err, cudaStream_t st) {
+cudaError_t launch_ws_bn(WsArgs w, const Epi& e, int* err, cudaStream_t st, long long batch) {
   int slots = 0;
   cudaError_t c = ws_slots<BN>(slots);
   if (c != cudaSuccess) return c;
-  const long long items = batch * mtiles * ntiles;
-  const unsigned grid = (unsigned)std::min<long long>(items, slots);
-  gemm_ws_kernel<BN><<<grid, ws::THREADS, ws::Cfg<BN>::SMEM, st>>>(a, aa, a_bs, K, b, kblocks, mtiles, ntiles, items,
-                                                                   e, err);
+  ws::op_mode(w.a, BM, w.K);
+  if (!w.b_img) ws::op_mode(w.b, BN, w.K);
+  w.items = batch * w.splits * w.mtiles * w.ntiles;
+  const unsigned grid = (unsigned)std::min<long long>(w.items, slots);
+  gemm_ws_kernel<BN><<<grid, ws::THREADS, ws::Cfg<BN>::SMEM, st>>>(w, e, err);
   return cudaGetLastError();
+}
+
+cudaError_t launch_ws(int bn, const WsArgs& w, const Epi& e, int* err, cudaStream_t st, long long batch) {
+  switch (bn) {
+    case 32: return launch_ws_bn<32>(w, e, err, st, batch);
+    case 64: return launch_ws_bn<64>(w, e, err, st, batch);
+    case 128: return launch_ws_bn<128>(w, e, err, st, batch);
+    default: return launch_ws_bn<256>(w, e, err, st, batch);
+  }
+}
+
+// Split-K with B from FP32 (BN = 32): one split per resident CTA.
+int ws_split_count(int kblocks, int ksplit) {
+  int slots = 0;
+  if (ws_slots<32>(slots) != cudaSuccess) slots = 1;
+  return std::max(1, std::min(kblocks, std::max(ksplit, slots)));
 }
 
 template <int BN>
@@ -892,16 +1024,18 @@ int TcGemm::run(const float* a, Addr aa, const float* b, Addr ba, long long M, i
   const long long kbl = (K + tg::BK - 1) / tg::BK;
   if (kbl > (1LL << 30) || mtiles * ntiles > (1LL << 30)) return MSX_ERR_INVALID;
   const int kblocks = (int)kbl;
-  int kper = kblocks;
-  if (ksplit > 1) kper = (kblocks + ksplit - 1) / ksplit;
-  const int splits = (kblocks + kper - 1) / kper;
-  const size_t a_bytes = (size_t)mtiles * kblocks * tg::A_BYTES;
-  const size_t b_bytes = (size_t)ntiles * kblocks * bn * tg::BK * 2;
-  int rc = reserve(a_bytes, b_bytes);
-  if (rc != MSX_OK) return rc;
-  float* pbuf = nullptr;
-  if (splits > 1) {
-    const size_t need = (size_t)splits * mtiles * ntiles * tg::BM * bn;
+  Epi e = epi;
+  e.M = M;
+  e.N = N;
+  e.ybs = 0;
+  tg::WsArgs w{};
+  w.a = tg::ws::Op{a, aa, 0, M, 0, 0};
+  w.b = tg::ws::Op{b, ba, 0, N, 0, 0};
+  w.K = K;
+  w.kblocks = kblocks;
+  w.ntiles = ntiles;
+  w.mtiles = mtiles;
+  auto ensure_part = [&](size_t need) -> int {
     if (need > part_cap) {
       if (part) cudaFree(part);
       part = nullptr;
@@ -909,35 +1043,58 @@ int TcGemm::run(const float* a, Addr aa, const float* b, Addr ba, long long M, i
       if (cudaMalloc(&part, need * sizeof(float)) != cudaSuccess) return MSX_ERR_ALLOC;
       part_cap = need;
     }
-    pbuf = part;
+    return MSX_OK;
+  };
+  if (ksplit > 1 && bn == 32) {
+    // long K, narrow output (weight gradients): split K over the persistent CTAs, both
+    // operands rounded to bfloat16 as they are loaded, partial tiles summed in split order
+    const int splits = tg::ws_split_count(kblocks, ksplit);
+    w.kper = (kblocks + splits - 1) / splits;
+    w.splits = (kblocks + w.kper - 1) / w.kper;
+    int rc = reserve(0, 0);
+    if (rc != MSX_OK) return rc;
+    rc = ensure_part((size_t)w.splits * mtiles * ntiles * tg::BM * bn);
+    if (rc != MSX_OK) return rc;
+    w.part = part;
+    w.b_img = nullptr;
+    cudaError_t c = tg::launch_ws(bn, w, e, err, st, 1);
+    if (c != cudaSuccess) return MSX_ERR_CUDA;
+    const long long n = M * (long long)N;
+    tg::splitk_reduce_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(part, w.splits, (int)(mtiles * ntiles),
+                                                                          ntiles, bn, e);
+    return cudaGetLastError() == cudaSuccess ? MSX_OK : MSX_ERR_CUDA;
   }
+  int kper = kblocks;
+  if (ksplit > 1) kper = (kblocks + ksplit - 1) / ksplit;
+  const int splits = (kblocks + kper - 1) / kper;
+  const size_t a_bytes = splits > 1 ? (size_t)mtiles * kblocks * tg::A_BYTES : 0;
+  const size_t b_bytes = (size_t)ntiles * kblocks * bn * tg::BK * 2;
+  int rc = reserve(a_bytes, b_bytes);
+  if (rc != MSX_OK) return rc;
   const long long a_rows = mtiles * tg::BM, b_rows = (long long)ntiles * bn;
   const long long a_thr = a_rows * kblocks * (tg::BK / 8), b_thr = b_rows * kblocks * (tg::BK / 8);
   tg::pack_kernel<<<(unsigned)((b_thr + 255) / 256), 256, 0, st>>>(b, ba, N, K, bn, b_rows, kblocks,
                                                                    reinterpret_cast<uint4*>(b_img));
-  Epi e = epi;
-  e.M = M;
-  e.N = N;
-  e.ybs = 0;
   const uint8_t* bi = reinterpret_cast<const uint8_t*>(b_img);
   cudaError_t c;
   if (splits == 1) {  // persistent kernel, A rounded to bfloat16 as it is loaded
-    switch (bn) {
-      case 32: c = tg::launch_ws_bn<32>(a, aa, 0, K, bi, kblocks, mtiles, ntiles, 1, e, err, st); break;
-      case 64: c = tg::launch_ws_bn<64>(a, aa, 0, K, bi, kblocks, mtiles, ntiles, 1, e, err, st); break;
-      case 128: c = tg::launch_ws_bn<128>(a, aa, 0, K, bi, kblocks, mtiles, ntiles, 1, e, err, st); break;
-      default: c = tg::launch_ws_bn<256>(a, aa, 0, K, bi, kblocks, mtiles, ntiles, 1, e, err, st); break;
-    }
+    w.kper = kblocks;
+    w.splits = 1;
+    w.b_img = bi;
+    c = tg::launch_ws(bn, w, e, err, st, 1);
     return c == cudaSuccess ? MSX_OK : MSX_ERR_CUDA;
   }
+  // split K with a wide output: both operands packed, one CTA per (tile, split)
+  rc = ensure_part((size_t)splits * mtiles * ntiles * tg::BM * bn);
+  if (rc != MSX_OK) return rc;
   tg::pack_kernel<<<(unsigned)((a_thr + 255) / 256), 256, 0, st>>>(a, aa, M, K, tg::BM, a_rows, kblocks,
                                                                    reinterpret_cast<uint4*>(a_img));
   const uint8_t* ai = reinterpret_cast<const uint8_t*>(a_img);
   switch (bn) {
-    case 32: c = tg::launch_gemm_bn<32>(ai, bi, mtiles, ntiles, kblocks, kper, pbuf, e, err, st); break;
-    case 64: c = tg::launch_gemm_bn<64>(ai, bi, mtiles, ntiles, kblocks, kper, pbuf, e, err, st); break;
-    case 128: c = tg::launch_gemm_bn<128>(ai, bi, mtiles, ntiles, kblocks, kper, pbuf, e, err, st); break;
-    default: c = tg::launch_gemm_bn<256>(ai, bi, mtiles, ntiles, kblocks, kper, pbuf, e, err, st); break;
+    case 32: c = tg::launch_gemm_bn<32>(ai, bi, mtiles, ntiles, kblocks, kper, part, e, err, st); break;
+    case 64: c = tg::launch_gemm_bn<64>(ai, bi, mtiles, ntiles, kblocks, kper, part, e, err, st); break;
+    case 128: c = tg::launch_gemm_bn<128>(ai, bi, mtiles, ntiles, kblocks, kper, part, e, err, st); break;
+    default: c = tg::launch_gemm_bn<256>(ai, bi, mtiles, ntiles, kblocks, kper, part, e, err, st); break;
   }
   return c == cudaSuccess ? MSX_OK : MSX_ERR_CUDA;
 }
@@ -964,12 +1121,16 @@ int TcGemm::run_batched(const float* a, Addr aa, long long a_bs, const float* b,
   e.ybs = y_bs;
   const uint8_t* bi = reinterpret_cast<const uint8_t*>(b_img);
   cudaError_t c;
-  switch (bn) {
-    case 32: c = tg::launch_ws_bn<32>(a, aa, a_bs, K, bi, kblocks, mtiles, ntiles, batch, e, err, st); break;
-    case 64: c = tg::launch_ws_bn<64>(a, aa, a_bs, K, bi, kblocks, mtiles, ntiles, batch, e, err, st); break;
-    case 128: c = tg::launch_ws_bn<128>(a, aa, a_bs, K, bi, kblocks, mtiles, ntiles, batch, e, err, st); break;
-    default: c = tg::launch_ws_bn<256>(a, aa, a_bs, K, bi, kblocks, mtiles, ntiles, batch, e, err, st); break;
-  }
+  tg::WsArgs w{};
+  w.a = tg::ws::Op{a, aa, a_bs, M, 0, 0};
+  w.b_img = bi;
+  w.K = K;
+  w.kblocks = kblocks;
+  w.kper = kblocks;
+  w.splits = 1;
+  w.ntiles = ntiles;
+  w.mtiles = mtiles;
+  c = tg::launch_ws(bn, w, e, err, st, batch);
   return c == cudaSuccess ? MSX_OK : MSX_ERR_CUDA;
 }
 
@@ -998,12 +1159,16 @@ int TcGemm::run_cplx(const float* a, Addr aa, long long a_bs, const float* src, 
   e.ybs = y_bs;
   const uint8_t* bi = reinterpret_cast<const uint8_t*>(b_img);
   cudaError_t c;
-  switch (bn) {
-    case 32: c = tg::launch_ws_bn<32>(a, aa, a_bs, K, bi, kblocks, mtiles, ntiles, batch, e, err, st); break;
-    case 64: c = tg::launch_ws_bn<64>(a, aa, a_bs, K, bi, kblocks, mtiles, ntiles, batch, e, err, st); break;
-    case 128: c = tg::launch_ws_bn<128>(a, aa, a_bs, K, bi, kblocks, mtiles, ntiles, batch, e, err, st); break;
-    default: c = tg::launch_ws_bn<256>(a, aa, a_bs, K, bi, kblocks, mtiles, ntiles, batch, e, err, st); break;
-  }
+  tg::WsArgs w{};
+  w.a = tg::ws::Op{a, aa, a_bs, M, 0, 0};
+  w.b_img = bi;
+  w.K = K;
+  w.kblocks = kblocks;
+  w.kper = kblocks;
+  w.splits = 1;
+  w.ntiles = ntiles;
+  w.mtiles = mtiles;
+  c = tg::launch_ws(bn, w, e, err, st, batch);
   return c == cudaSuccess ? MSX_OK : MSX_ERR_CUDA;
 }
 

@@ -91,7 +91,7 @@ def test_tc_dft_norm_compensation_keeps_parseval():
 
 @pytest.mark.parametrize('m,n,k', [(128, 32, 64), (300, 64, 100), (1000, 4, 32), (256, 200, 512), (129, 256, 64), (32, 40, 20000),
                                    (64, 640, 192), (200000, 32, 32), (5000, 128, 6), (70000, 256, 40),
-                                   (40000, 64, 1000)])
+                                   (40000, 64, 1000), (32, 32, 50000), (100, 6, 30000), (200, 20, 9000)])
 def test_gemm_bf16_matches_fp32_matmul_of_rounded_operands(m, n, k):
     """The general tcgen05 GEMM against a plain PyTorch FP32 matmul of the same
     bfloat16-rounded operands (only the accumulation order differs)."""
