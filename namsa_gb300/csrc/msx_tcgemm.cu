@@ -1,29 +1,26 @@
 // General BF16 GEMM on the 5th-generation tensor cores (tcgen05) with FP32
 // accumulation, for the contractions of the learned corrector (pointwise
-// channel mixing, its weight gradients and the partial DFT stages of its
-// spectral layers).
+// channel mixing, its weight gradients, the per-mode complex channel mixing and
+// the partial DFT stages of its spectral layers).
 //
 //   D (M x N) = A (M x K) . B (N x K)^T,   A and B rounded to bfloat16.
 //
 // Operands are read from FP32 arrays of any 2-level strided layout: element
 // (r, k) of an operand sits at (r / rc) * s1 + (r % rc) * s2 + (k / kc) * t1 +
-// (k % kc) * t2.  A pack
-// kernel rounds them to bfloat16 into the tensor-core shared-memory image
-// (K-major, 128-byte swizzle, 8-row atoms of 128 B, 16-byte chunk c of row r
-// at chunk c ^ (r mod 8)), tile by tile and K block (64) by K block, zero
-// padded to whole tiles; the GEMM kernel then moves each (tile, K block) with
-// one 1-D bulk copy.  Output element (r, c) is written at the same kind of
+// (k % kc) * t2.  The tensor cores read both from shared memory in the K-major,
+// 128-byte-swizzled layout (8-row atoms of 128 B, 16-byte chunk c of row r at
+// chunk c ^ (r mod 8)).  Output element (r, c) is written at the same kind of
 // strided address, so results land directly in pixel-major or transposed
 // layouts.  Epilogue: z = acc (+ bias[c]) (+ add[r, c]); out = z or out += z;
 // optionally act = gelu(z) (tanh form) into a second array.
 //
-// Kernel: one CTA of 128 threads per 128 x BN tile of D.  Thread 0 produces
-// (bulk copies into STAGES stages, full/empty mbarriers), thread 32 issues
-// tcgen05.mma (M = 128, N = BN, K = 16) and commits each stage to its empty
-// barrier; all four warps read the accumulator with tcgen05.ld (warp w owns
-// TMEM lanes 32w..32w+31 = tile rows).  Every wait is bounded; on a timeout
-// the kernel sets *err, waits (bounded) for its MMAs, frees its tensor memory
-// and returns.
+// Main path (gemm_ws_kernel): a persistent, warp-specialised kernel; A is
+// staged in FP32 by bulk or asynchronous copies and rounded to bfloat16 in
+// shared memory, B comes from a small packed image (pack_kernel, or
+// pack_cplx_kernel for the real embedding of a complex product) or, for the
+// long-K weight gradients (N <= 32), is staged and rounded like A while K is
+// split over the CTAs.  The per-tile kernel (gemm_kernel, both operands packed)
+// remains for split-K products with N > 32.
 #include "msx.h"
 #include "msx_internal.h"
 
@@ -155,6 +152,13 @@ __global__ void pack_cplx_kernel(const float* __restrict__ src, long long si, lo
   img[byte / 16] = *reinterpret_cast<const uint4*>(v);
 }
 
+// Per-tile kernel: one CTA of 128 threads per 128 x BN tile of D and K split.
+// Thread 0 moves each (tile, K block) of the packed images with one bulk copy into
+// STAGES stages (full/empty mbarriers), thread 32 issues tcgen05.mma (M = 128,
+// N = BN, K = 16) and commits each stage to its empty barrier; all four warps read
+// the accumulator with tcgen05.ld (warp w owns TMEM lanes 32w..32w+31 = tile rows).
+// Every wait is bounded; on a timeout the kernel sets *err, waits (bounded) for its
+// MMAs, frees its tensor memory and returns.
 // With part != null the CTA (tile, split) sums K blocks [split * kper, ...) and
 // writes its raw 128 x BN partial to part[(split * tiles + tile) * 128 * BN].
 template <int BN>
@@ -520,7 +524,7 @@ __device__ __forceinline__ void convert_op(uint8_t* sa, const float* stg, const 
       const int row = t / nch, ch = t - (t / nch) * nch;
       const float* src = stg + row * ld + ch * 8;
       float x[8];
-      if (ch * 8 + 8 <= nk && o.mode == ROWRUN) {
+      if (ch * 8 + 8 <= nk && (ld & 3) == 0) {
         const float4 lo = *reinterpret_cast<const float4*>(src), hi = *reinterpret_cast<const float4*>(src + 4);
         x[0] = lo.x; x[1] = lo.y; x[2] = lo.z; x[3] = lo.w; x[4] = hi.x; x[5] = hi.y; x[6] = hi.z; x[7] = hi.w;
       } else {
