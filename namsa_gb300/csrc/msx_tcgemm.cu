@@ -315,17 +315,24 @@ __global__ void __launch_bounds__(128) gemm_kernel(const uint8_t* __restrict__ A
   if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(BN) : "memory");
 }
 
-// Sums the split-K partials in split order and applies the epilogue; one thread per (row, column).
+// Sums the split-K partials and applies the epilogue; one warp per (row, column): lane l
+// adds splits l, l + 32, ... in order, then the lanes combine by a fixed butterfly, so
+// the result does not depend on scheduling.
+constexpr int REDUCE_WARPS = 8;  // outputs per block of the reduction
 __global__ void splitk_reduce_kernel(const float* __restrict__ part, int splits, int tiles, int ntiles_n, int bn, Epi e) {
-  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= e.M * (long long)e.N) return;
+  const long long i = (long long)blockIdx.x * REDUCE_WARPS + (threadIdx.x >> 5);
+  const int lane = threadIdx.x & 31;
+  if (i >= e.M * (long long)e.N) return;  // warp-uniform
   const long long r = i / e.N;
   const int c = (int)(i % e.N);
   const int mt = (int)(r / BM), nt = c / bn;
   const int tile = mt * ntiles_n + nt;
   const size_t off = (size_t)tile * (BM * bn) + (size_t)(r % BM) * bn + (c % bn);
   float z = 0.f;
-  for (int s = 0; s < splits; ++s) z += part[(size_t)s * tiles * (BM * bn) + off];
+  for (int s = lane; s < splits; s += 32) z += part[(size_t)s * tiles * (BM * bn) + off];
+#pragma unroll
+  for (int m = 16; m > 0; m >>= 1) z += __shfl_xor_sync(0xffffffffu, z, m);
+  if (lane != 0) return;
   z *= e.scale;
   const long long o = addr_of(e.out, r, c);
   if (e.bias) z += e.bias[c];
@@ -975,8 +982,8 @@ cudaError_t launch_gemm_bn(const uint8_t* a, const uint8_t* b, long long mtiles,
       a, b, kblocks, ntiles, (int)(mtiles * ntiles), kper, part, e, err);
   if (part) {
     const long long n = e.M * (long long)e.N;
-    splitk_reduce_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(part, splits, (int)(mtiles * ntiles), ntiles, BN,
-                                                                      e);
+    splitk_reduce_kernel<<<(unsigned)((n + REDUCE_WARPS - 1) / REDUCE_WARPS), 32 * REDUCE_WARPS, 0, st>>>(
+        part, splits, (int)(mtiles * ntiles), ntiles, BN, e);
   }
   return cudaGetLastError();
 }
@@ -1064,8 +1071,8 @@ int TcGemm::run(const float* a, Addr aa, const float* b, Addr ba, long long M, i
     cudaError_t c = tg::launch_ws(bn, w, e, err, st, 1);
     if (c != cudaSuccess) return MSX_ERR_CUDA;
     const long long n = M * (long long)N;
-    tg::splitk_reduce_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(part, w.splits, (int)(mtiles * ntiles),
-                                                                          ntiles, bn, e);
+    tg::splitk_reduce_kernel<<<(unsigned)((n + tg::REDUCE_WARPS - 1) / tg::REDUCE_WARPS), 32 * tg::REDUCE_WARPS, 0,
+                               st>>>(part, w.splits, (int)(mtiles * ntiles), ntiles, bn, e);
     return cudaGetLastError() == cudaSuccess ? MSX_OK : MSX_ERR_CUDA;
   }
   int kper = kblocks;
