@@ -589,7 +589,14 @@ def run_corrector(args):
         maps = CR.crystal_maps(net, cr)
         torch.cuda.synchronize()
         net_s = time.perf_counter() - t2
-        out = {'network_s_per_crystal': net_s, 'coarse_slices': int(cr.coarse_steps)}
+        t2 = time.perf_counter()
+        maps_every = CR.crystal_maps(net, cr, dedup=False)
+        torch.cuda.synchronize()
+        net_every_s = time.perf_counter() - t2
+        distinct = len(CR.distinct_slices(cr.features())[0])
+        out = {'network_s_per_crystal': net_s, 'network_s_every_slice': net_every_s,
+               'distinct_slices': distinct, 'maps_equal_every_slice': bool(torch.equal(maps, maps_every)),
+               'coarse_slices': int(cr.coarse_steps)}
         for thick in (200.0, 500.0, 1000.0):
             steps = min(cr.coarse_steps, int(round(thick / (cr.ratio * cr.slice_t))))
             trans = cr.effective_slices(maps[:steps].contiguous(), args.corr_form)
@@ -607,7 +614,10 @@ def run_corrector(args):
                 'speedup_corrected_vs_fine': t_fine / t_corr,
                 'speedup_incl_network_per_1024_positions': (t_fine * 1024 / len(pos)) /
                                                            (t_corr * 1024 / len(pos) +
-                                                            net_s * steps / cr.coarse_steps)}
+                                                            net_s * steps / cr.coarse_steps),
+                'speedup_incl_network_every_slice_per_1024_positions': (t_fine * 1024 / len(pos)) /
+                                                                      (t_corr * 1024 / len(pos) +
+                                                                       net_every_s * steps / cr.coarse_steps)}
         res[name] = out
     si = res['Si[001]']['1000A']
     line = {'metric': METRIC, 'value': si['corrected_probes_per_s'], 'unit': UNIT, 'n_gpus': 1,

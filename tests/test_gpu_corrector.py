@@ -66,6 +66,25 @@ def test_network_forward_backward_match_oracle(H, W, Cin, C, L, MX, MY, S):
     net.close()
 
 
+def test_repeated_slices_share_their_maps():
+    """The network runs once per distinct coarse slice; the maps equal those of a run
+    over every slice (a periodic crystal repeats its coarse slices)."""
+    torch.cuda.set_device(0)
+    cr = CR.Crystal(structures.silicon((2, 2, 8)), 64, 5.431 / 4)
+    net = engine.Corrector(64, 64, 6, 8, 1, 8, 16, max_samples=4)
+    net.params.copy_(torch.from_numpy(CR.init_params(net, seed=0)))
+    first, index = CR.distinct_slices(cr.features())
+    assert len(index) == cr.coarse_steps and len(first) < cr.coarse_steps, (len(first), cr.coarse_steps)
+    f = cr.features()
+    for s, j in enumerate(index):
+        assert torch.equal(f[s], f[first[j]])
+    a = CR.crystal_maps(net, cr)
+    b = CR.crystal_maps(net, cr, dedup=False)
+    net.check()
+    assert torch.equal(a, b)
+    net.close()
+
+
 @pytest.mark.parametrize('form', [0, 1])
 def test_rollout_adjoint_matches_central_difference(form):
     torch.cuda.set_device(0)

@@ -158,3 +158,23 @@ def test_band_columns_contain_every_column_the_mask_keeps():
         kept = np.nonzero((k < k_band).any(axis=0))[0]
         if kept.size:
             assert lo <= kept.min() and kept.max() < hi, (nx, tile, lo, hi, kept.min(), kept.max())
+
+
+def test_distinct_slices_groups_bitwise_equal_inputs():
+    """The corrector runs its network once per group of coarse slices with bitwise equal
+    inputs; a slice that differs in one value keeps its own group."""
+    import torch
+    from namsa_gb300 import corrector as CR
+    g = torch.Generator().manual_seed(0)
+    f = torch.randn(8, 6, 5, 6, generator=g)
+    f[3] = f[0]
+    f[5] = f[1]
+    f[4] = f[0].clone()
+    f[4][2, 3, 1] += 0.25
+    f[6] = f[4]
+    f[7] = f[0]
+    first, index = CR.distinct_slices(f)
+    assert first == [0, 1, 2, 4]
+    assert index == [0, 1, 2, 0, 3, 1, 3, 0]
+    for s, j in enumerate(index):
+        assert torch.equal(f[s], f[first[j]])
