@@ -585,14 +585,8 @@ def run_corrector(args):
     res = {}
     for name, cr, a in crystals[:2]:
         pos = np.random.default_rng(7).uniform(0, a, size=(args.corr_positions, 2))
-        t2 = time.perf_counter()
-        maps = CR.crystal_maps(net, cr)
-        torch.cuda.synchronize()
-        net_s = time.perf_counter() - t2
-        t2 = time.perf_counter()
-        maps_every = CR.crystal_maps(net, cr, dedup=False)
-        torch.cuda.synchronize()
-        net_every_s = time.perf_counter() - t2
+        maps, net_s = CR.timed(lambda: CR.crystal_maps(net, cr))
+        maps_every, net_every_s = CR.timed(lambda: CR.crystal_maps(net, cr, dedup=False))
         distinct = len(CR.distinct_slices(cr.features())[0])
         out = {'network_s_per_crystal': net_s, 'network_s_every_slice': net_every_s,
                'distinct_slices': distinct, 'maps_equal_every_slice': bool(torch.equal(maps, maps_every)),

@@ -152,16 +152,21 @@ def distinct_slices(features):
     """The coarse slices whose network inputs are bitwise equal to an earlier slice's (the
     repeated slices of a periodic crystal): returns (first, index), `first` the slices
     that start a group and `index[s]` the group of slice s.  Candidates share a weighted
-    sum of their inputs; every candidate is confirmed by exact comparison (one batched
-    comparison), and an unconfirmed one keeps a group of its own."""
+    sum of their inputs' bit patterns; every candidate is confirmed by exact comparison,
+    and an unconfirmed one keeps a group of its own."""
     S = features.shape[0]
     flat = features.reshape(S, -1)
-    w = 1.0 + (torch.arange(flat.shape[1], device=flat.device) % 251).to(torch.float32) / 251.0
-    keys = (flat * w).sum(1).tolist()
+    # integer key: the bit patterns times fixed weights, summed exactly in int64 (bitwise
+    # equal slices get equal keys whatever the summation order)
+    w = 1 + torch.arange(flat.shape[1], device=flat.device) % 251
+    B = 16  # slices per chunk: bounds the temporaries
+    keys = torch.cat([(flat[i:i + B].contiguous().view(torch.int32).to(torch.int64) * w).sum(1)
+                      for i in range(0, S, B)]).tolist()
     cand, seen = [], {}
     for s in range(S):
         cand.append(seen.setdefault(keys[s], s))
-    same = (flat == flat[torch.as_tensor(cand, device=flat.device)]).all(1).tolist()
+    idx = torch.as_tensor(cand, device=flat.device)
+    same = torch.cat([(flat[i:i + B] == flat[idx[i:i + B]]).all(1) for i in range(0, S, B)]).tolist()
     first, index, group = [], [], {}
     for s in range(S):
         c = cand[s] if same[s] else s
