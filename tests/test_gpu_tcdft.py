@@ -110,3 +110,18 @@ def test_gemm_bf16_matches_fp32_matmul_of_rounded_operands(m, n, k):
     torch.cuda.synchronize()
     assert torch.allclose(out, ref - bias + 1, rtol=1e-4, atol=1e-4 * k ** 0.5)
     assert (big[:, :3] == 1).all() and (big[:, 3 + n:] == 1).all()
+
+
+@pytest.mark.parametrize('m,n,k,pad_a,pad_b', [(5000, 32, 40, 3, 0), (5000, 64, 40, 4, 1), (3000, 200, 100, 8, 3),
+                                               (64, 32, 40000, 3, 5), (32, 16, 30000, 4, 0)])
+def test_gemm_bf16_padded_operand_rows(m, n, k, pad_a, pad_b):
+    """Operands whose rows are padded (leading dimension > k): rows that stay 16-byte
+    aligned arrive by one bulk copy each, the others by plain loads; split K included."""
+    g = torch.Generator().manual_seed(m + n + k + pad_a)
+    a_big = torch.randn(m, k + pad_a, generator=g).to(DEV)
+    b_big = torch.randn(n, k + pad_b, generator=g).to(DEV)
+    a, b = a_big[:, :k], b_big[:, :k]
+    ref = a.to(torch.bfloat16).float() @ b.to(torch.bfloat16).float().T
+    got = engine.gemm_bf16(a, b)
+    engine.gemm_check()
+    assert torch.allclose(got, ref, rtol=1e-4, atol=1e-4 * k ** 0.5), (got - ref).abs().max().item()
