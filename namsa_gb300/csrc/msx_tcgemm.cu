@@ -563,7 +563,7 @@ __device__ __forceinline__ void convert_op(uint8_t* sa, const float* stg, const 
 }
 }  // namespace ws
 
-template <int BN>
+// 16 consecutive accumulator columns of this warp's 32 TMEM lanes (one per lane).
 __device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t (&v)[16]) {
   asm volatile(
       "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, "
@@ -781,7 +781,7 @@ __global__ void __launch_bounds__(ws::THREADS, 1) gemm_ws_kernel(WsArgs w, Epi e
                     (long long)(q * 32 + lane) * BN;
         for (int c0 = 0; c0 < BN; c0 += 16) {
           uint32_t v[16];
-          tmem_ld16<BN>(tmem + lanes + (uint32_t)(buf * BN + c0), v);
+          tmem_ld16(tmem + lanes + (uint32_t)(buf * BN + c0), v);
           if (row_ok) {
 #pragma unroll
             for (int j = 0; j < 16; j += 4)
@@ -814,7 +814,7 @@ __global__ void __launch_bounds__(ws::THREADS, 1) gemm_ws_kernel(WsArgs w, Epi e
 #pragma unroll
           for (int h = 0; h < 2; ++h) {
             uint32_t v[16];
-            tmem_ld16<BN>(taddr + (uint32_t)(h * 16), v);
+            tmem_ld16(taddr + (uint32_t)(h * 16), v);
 #pragma unroll
             for (int j = 0; j < 16; ++j) blk[lane * 33 + h * 16 + j] = __uint_as_float(v[j]);
           }
@@ -861,7 +861,7 @@ __global__ void __launch_bounds__(ws::THREADS, 1) gemm_ws_kernel(WsArgs w, Epi e
 #pragma unroll
           for (int h = 0; h < 32; h += 16) {
             uint32_t v[16];
-            tmem_ld16<BN>(taddr + (uint32_t)h, v);
+            tmem_ld16(taddr + (uint32_t)h, v);
             float prev[16];
             if (have_prev) {
 #pragma unroll
