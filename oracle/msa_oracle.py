@@ -475,6 +475,20 @@ def srtio3_supercell(nx, ny, nz, a=3.905):
     return _tile(basis, np.array([38, 22, 8, 8, 8]), (nx, ny, nz), a)
 
 
+def random_supercell(seed, nx, ny, nz):
+    """A seeded random cubic crystal of the uneven-batch kind: a ~ U[3, 8] Angstrom, 1-4
+    species with Z ~ U{3..83}, 2-16 atoms at uniform fractional positions, each of one of
+    the drawn species; tiled face-inclusive like si_supercell."""
+    rng = np.random.default_rng(seed)
+    a = rng.uniform(3.0, 8.0)
+    ns = int(rng.integers(1, 5))
+    zs = rng.integers(3, 84, size=ns)
+    na = int(rng.integers(2, 17))
+    basis = rng.uniform(0.0, 1.0, size=(na, 3))
+    species = zs[rng.integers(0, ns, size=na)]
+    return _tile(basis, species, (nx, ny, nz), a)
+
+
 def _tile(basis, zs, n, a):
     n = np.asarray(n)
     cells = np.stack(np.meshgrid(*[np.arange(k + 1) for k in n], indexing='ij'), -1).reshape(-1, 3)

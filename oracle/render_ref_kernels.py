@@ -14,6 +14,8 @@ workloads the parity tests use, and writes the rendered sources into
   c5  SrTiO3 18x12x8 cells (x, y, z), a rectangular 256 x 384 (y, x) grid, 200 keV
   c6  Si 12x12x20 cells (face-inclusive), 768^2, 300 keV, t = a/4 (80 slices)
   c7  SrTiO3 40x40x12 cells, 1024^2, 300 keV, t = a/2 (24 slices)
+  c8  a seeded random cubic crystal (seed 1: a = 5.56 A, Au, B, Si and Tm, 16 atoms per
+      cell), 22x11x18 cells, a rectangular 384 x 768 (y, x) grid, 120 keV, t = 1.5 A
 
 plus ``oracle/_ref/workloads.json`` with the rendered parameters.  The sources
 are then compiled against the stand-in header ``oracle/pycuda-complex.hpp`` and
@@ -46,11 +48,14 @@ WORKLOADS = {
     'c5': dict(crystal='srtio3', cells=(18, 12, 8), n=(256, 384), kv=200.0, semi=25e-3, slice_t=A_STO / 2),
     'c6': dict(crystal='si', cells=(12, 12, 20), n=768, kv=300.0, semi=25e-3, slice_t=A_SI / 4),
     'c7': dict(crystal='srtio3', cells=(40, 40, 12), n=1024, kv=300.0, semi=25e-3, slice_t=A_STO / 2),
+    'c8': dict(crystal='random1', cells=(22, 11, 18), n=(384, 768), kv=120.0, semi=20e-3, slice_t=1.5),
 }
 
 
 def supercell(crystal, cells):
     from oracle import msa_oracle as O
+    if crystal.startswith('random'):
+        return O.random_supercell(int(crystal[len('random'):]), *cells)
     return O.si_supercell(*cells) if crystal == 'si' else O.srtio3_supercell(*cells)
 
 

@@ -9,8 +9,10 @@ driven in MSAGPU's order (oracle/refgpu_harness.cu), on identical inputs.
 * CBED: relative L2 <= 1e-4 per pattern (FP32 engine vs FP32 reference path), for
   the single-probe Si 256^2 case, all 1024 positions of the Si 512^2 scan, a
   three-species SrTiO3 256^2 case at 300 keV with defocus and Cs, a rectangular
-  256 x 384 SrTiO3 grid, a Si 768^2 grid (three-stage radix schedules) and a
-  SrTiO3 1024^2 grid, the line lengths of the uneven batch and the precision study
+  256 x 384 SrTiO3 grid, a Si 768^2 grid (three-stage radix schedules), a
+  SrTiO3 1024^2 grid (the line lengths of the uneven batch and the precision study)
+  and a seeded random four-species crystal (Au, B, Si, Tm) on a rectangular
+  384 x 768 grid at 120 keV
 
 The harness libraries are built by oracle/build_ref.py from kernels rendered where
 the reference checkout exists; without them these tests skip with that reason.
@@ -30,6 +32,8 @@ PROBE_C2 = {'smooth_apert': True, 'apert_smooth': 50, 'spherical_phase': True,
             'aberration_dict': {'C1': 0., 'C3': 1e4, 'C5': 0.}, 'scherzer': False}
 PROBE_C4 = {'smooth_apert': False, 'apert_smooth': 50, 'spherical_phase': True,
             'aberration_dict': {'C1': 50., 'C3': 1e4, 'C5': 1e6}, 'scherzer': False}
+PROBE_C8 = {'smooth_apert': True, 'apert_smooth': 50, 'spherical_phase': True,
+            'aberration_dict': {'C1': -30., 'C3': 5e3, 'C5': 0.}, 'scherzer': False}
 
 
 def _ref(tag):
@@ -58,7 +62,7 @@ def _case(tag):
     return ref, sim, geom, win
 
 
-@pytest.mark.parametrize('tag', ['c1', 'c2', 'c4', 'c5', 'c6', 'c7'])
+@pytest.mark.parametrize('tag', ['c1', 'c2', 'c4', 'c5', 'c6', 'c7', 'c8'])
 def test_transmission_bit_identical_to_reference_kernel(tag):
     ref, sim, geom, win = _case(tag)
     t_ref = ref.build_potential(geom, ref.meta['slice_t'], win)
@@ -69,7 +73,7 @@ def test_transmission_bit_identical_to_reference_kernel(tag):
 
 
 @pytest.mark.parametrize('tag,pd', [('c1', PROBE_C1), ('c2', PROBE_C2), ('c4', PROBE_C4), ('c5', PROBE_C2),
-                                    ('c6', PROBE_C4), ('c7', PROBE_C2)])
+                                    ('c6', PROBE_C4), ('c7', PROBE_C2), ('c8', PROBE_C8)])
 def test_probe_matches_reference_kernels(tag, pd):
     ref, sim, geom, _ = _case(tag)
     sim.build_probe(pd)
@@ -143,4 +147,14 @@ def test_cbed_srtio3_1024_matches_reference_gpu_path():
     pos = np.array([[0., 0.], [1.9, -1.0]])
     err, got, want = _cbed_parity('c7', PROBE_C2, pos)
     assert got.shape == (2, 1024, 1024)
+    assert err.max() <= 1e-4, err
+
+
+def test_cbed_random_crystal_rectangular_384x768_matches_reference_gpu_path():
+    """A seeded random crystal of the uneven-batch kind (a = 5.56 A; Au, B, Si and Tm, 16
+    atoms per cell; 22 x 11 x 18 cells) on a 384 x 768 grid, 120 keV, defocus and Cs,
+    66 slices of 1.5 A."""
+    pos = np.array([[0., 0.], [2.1, -3.3], [-1.2, 4.4]])
+    err, got, want = _cbed_parity('c8', PROBE_C8, pos)
+    assert got.shape == (3, 384, 768)
     assert err.max() <= 1e-4, err
