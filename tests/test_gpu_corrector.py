@@ -1,7 +1,8 @@
 """The learned coarse-slice corrector on the GPU.
 
 * Network: the CUDA forward maps and backward gradients (every contraction a
-  bfloat16 tensor-core GEMM with FP32 accumulation) against the FP64 oracle
+  bfloat16 tensor-core GEMM with FP32 accumulation) at 32 x 48, 64^2 and 512^2
+  against the FP64 oracle
   (oracle/corrector_oracle.py, itself checked by finite differences) run with
   the same bfloat16 operand rounding, and against the plain FP64 oracle.
 * Rollout adjoint: the map gradients of a windowed corrected rollout,
@@ -28,7 +29,8 @@ def _rel(a, b):
     return float(np.linalg.norm(np.ravel(a) - np.ravel(b)) / max(np.linalg.norm(np.ravel(b)), 1e-30))
 
 
-@pytest.mark.parametrize('H,W,Cin,C,L,MX,MY,S', [(32, 48, 6, 8, 2, 6, 8, 3), (64, 64, 6, 32, 4, 16, 32, 2)])
+@pytest.mark.parametrize('H,W,Cin,C,L,MX,MY,S', [(32, 48, 6, 8, 2, 6, 8, 3), (64, 64, 6, 32, 4, 16, 32, 2),
+                                                  (512, 512, 6, 8, 1, 16, 32, 1)])
 def test_network_forward_backward_match_oracle(H, W, Cin, C, L, MX, MY, S):
     torch.cuda.set_device(0)
     rng = np.random.default_rng(H + C)
@@ -83,6 +85,28 @@ def test_repeated_slices_share_their_maps():
     net.check()
     assert torch.equal(a, b)
     net.close()
+
+
+@pytest.mark.parametrize('n,form', [(256, 1), (512, 1), (256, 0)])
+def test_effective_slices_fold_the_corrected_steps(n, form):
+    """The production multislice on the effective slices (t'_0 = b_0 t_0, t'_k = a_{k-1} b_k t_k,
+    t'_S = a_{S-1}) gives the CBED of the corrected rollout run step by step (b_k t_k, coarse
+    step, a_k; a last masked propagation), for random maps."""
+    torch.cuda.set_device(0)
+    cr = CR.Crystal(structures.silicon((4, 4, 6)), n, 5.431 / 4)
+    S = cr.coarse_steps
+    maps = (0.05 * torch.randn(S, n, n, 4, generator=torch.Generator().manual_seed(n + form))).to(DEV)
+    pos = np.array([[0.3, 1.1], [2.0, 3.0], [4.4, 0.7]], np.float32)
+    got = CR.corrected_multislice(None, cr, pos, S, trans=cr.effective_slices(maps, form)).cpu().numpy()
+    w = cr.waves(pos)
+    tb = torch.empty((n, n), dtype=torch.complex64, device=DEV)
+    for k in range(S):
+        engine.map_trans(cr.trans_coarse[k], maps[k], 1, out=tb, form=form)
+        cr.plan.step_waves(w, tb, cr.ptab_coarse)
+        engine.apply_map(w, maps[k], 0, form=form)
+    cr.plan.step_waves(w, cr.ones, cr.ptab_coarse)
+    want = cr.plan.cbed_waves(w, cr.sim.norm_dev).cpu().numpy()
+    assert _rel(got, want) < 2e-5, _rel(got, want)
 
 
 @pytest.mark.parametrize('form', [0, 1])
