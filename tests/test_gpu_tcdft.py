@@ -125,3 +125,40 @@ def test_gemm_bf16_padded_operand_rows(m, n, k, pad_a, pad_b):
     got = engine.gemm_bf16(a, b)
     engine.gemm_check()
     assert torch.allclose(got, ref, rtol=1e-4, atol=1e-4 * k ** 0.5), (got - ref).abs().max().item()
+
+
+def _gemm_cases(seed=11, count=36):
+    rng = np.random.default_rng(seed)
+    cases = []
+    for i in range(count):
+        if i % 6 == 5:  # long K, narrow output: split K
+            m, n, k = int(rng.integers(1, 129)), int(rng.integers(1, 33)), int(rng.integers(4096, 40000))
+        else:
+            m, n, k = int(rng.integers(1, 5000)), int(rng.integers(1, 600)), int(rng.integers(1, 3000))
+        cases.append((m, n, k, int(rng.integers(0, 6)), int(rng.integers(0, 6)), int(rng.integers(0, 6)),
+                      bool(rng.integers(0, 2)), bool(rng.integers(0, 2))))
+    return cases
+
+
+@pytest.mark.parametrize('m,n,k,pad_a,pad_b,pad_c,acc,bias', _gemm_cases())
+def test_gemm_bf16_random_shapes(m, n, k, pad_a, pad_b, pad_c, acc, bias):
+    """Seeded random sizes, padded rows, accumulation and bias through every loader mode of
+    the tensor-core GEMM, against a plain PyTorch FP32 matmul of the bfloat16-rounded
+    operands."""
+    g = torch.Generator().manual_seed(m * 7 + n * 13 + k)
+    a = torch.randn(m, k + pad_a, generator=g).to(DEV)[:, :k]
+    b = torch.randn(n, k + pad_b, generator=g).to(DEV)[:, :k]
+    c_big = torch.randn(m, n + pad_c, generator=g).to(DEV)
+    before = c_big.clone()
+    c0 = c_big[:, :n].clone()
+    bv = torch.randn(n, generator=g).to(DEV) if bias else None
+    ref = a.to(torch.bfloat16).float() @ b.to(torch.bfloat16).float().T
+    if bias:
+        ref = ref + bv
+    if acc:
+        ref = ref + c0
+    engine.gemm_bf16(a, b, bv, out=c_big[:, :n], accumulate=acc)
+    engine.gemm_check()
+    got = c_big[:, :n]
+    assert torch.allclose(got, ref, rtol=1e-4, atol=1e-4 * (k ** 0.5) + 1e-5), (got - ref).abs().max().item()
+    assert torch.equal(c_big[:, n:], before[:, n:])  # the padding of the output rows is untouched
