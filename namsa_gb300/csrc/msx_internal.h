@@ -59,8 +59,10 @@ struct TcGemm {
   int reserve(size_t a_bytes, size_t b_bytes);
   float* part = nullptr;  // split-K partial sums
   size_t part_cap = 0;
-  // ksplit > 1 splits K over that many CTAs per tile; partial tiles are summed
-  // in a fixed order before the epilogue (for the long-K weight gradients).
+  // ksplit > 1 splits K (for the long-K weight gradients): with N <= 32 over
+  // max(ksplit, one per resident CTA) splits of the persistent kernel, both operands
+  // staged from FP32; otherwise over ksplit CTAs per tile with packed operands.
+  // Partial tiles are summed in a fixed order before the epilogue.
   int run(const float* a, Addr aa, const float* b, Addr ba, long long M, int N, long long K, const Epi& e,
           cudaStream_t st, int ksplit = 1);
   // `batch` independent GEMMs of the same shape; batch b reads A at a + b * a_bs, B at
