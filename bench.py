@@ -583,7 +583,7 @@ def run_corrector(args):
     train_s = time.perf_counter() - t1
     net.check()
     res = {}
-    for name, cr, a in crystals[:2]:
+    for name, cr, a in crystals[:3]:  # Si [001], SrTiO3 [001] and the first random crystal
         pos = np.random.default_rng(7).uniform(0, a, size=(args.corr_positions, 2))
         maps, net_s = CR.timed(lambda: CR.crystal_maps(net, cr))
         maps_every, net_every_s = CR.timed(lambda: CR.crystal_maps(net, cr, dedup=False))
